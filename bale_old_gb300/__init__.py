@@ -1,0 +1,347 @@
+"""bale_old_gb300 -- bale's irregular-access core (histo, ig, triangles) on one
+GB300 (sm_103a), behind the reference's own entry points.
+
+The compute is in libbale_gb300.so (hand-written CUDA + host C, C ABI in
+include/bale_gb300.h).  This module is the host-side mirror of the reference
+interface for Python callers: the same names as the reference's apps
+(histo_agi, ig_exstack, triangle_agi, ...), the same argument meaning
+(histo ADDS into counts, ig OVERWRITES tgt, triangles return the count and a
+work tally), the same return value (wall seconds).  Where the reference
+returns -1.0 for a failure, these raise BaleError with the library's message.
+There is no CPU path: every call goes through the CUDA library, and importing
+the package fails if the library is not built.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Iterable, Optional, Sequence
+
+import numpy as np
+
+from ._lib import LIB_PATH, P64, PSM, load, sparsemat_t
+
+__all__ = [
+    "BaleError", "SparseMatrix", "LIB_PATH",
+    "histo_agi", "histo_exstack", "histo_exstack2", "histo_conveyor",
+    "ig_agi", "ig_exstack", "ig_exstack2", "ig_conveyor",
+    "triangle_agi", "triangle_exstack_push", "triangle_exstack2_push",
+    "triangle_convey_push", "triangle_agi_iter",
+    "histo_dev", "ig_dev", "triangle_dev",
+    "splitmix64", "gen_uniform", "gen_values", "gen_negative_table", "gen_zipf",
+    "keyed_perm", "gen_rmat", "gen_erdos_renyi", "gen_kronecker", "kronecker_triangles",
+    "set_host_threads", "release_buffers", "version", "pack_index",
+]
+
+_lib = load()
+
+
+class BaleError(RuntimeError):
+    """A drop-in returned -1.0 or a device entry point returned a status."""
+
+
+def _last_error() -> str:
+    msg = _lib.bale_last_error()
+    return msg.decode() if msg else ""
+
+
+def _arr(a: np.ndarray, name: str, writable: bool = False) -> np.ndarray:
+    if not isinstance(a, np.ndarray) or a.dtype != np.int64 or not a.flags.c_contiguous:
+        raise TypeError(f"{name} must be a C-contiguous numpy int64 array")
+    if writable and not a.flags.writeable:
+        raise ValueError(f"{name} must be writable")
+    return a
+
+
+def _p(a: np.ndarray):
+    return a.ctypes.data_as(P64)
+
+
+def _seconds(t: float, what: str) -> float:
+    if t < 0:
+        raise BaleError(f"{what}: {_last_error()}")
+    return t
+
+
+def pack_index(index: np.ndarray) -> np.ndarray:
+    """The reference's packed index for one PE: (index << 16) | 0
+    (apps/histo_src/histo.upc:150, apps/ig_src/ig.upc:174)."""
+    return (np.asarray(index, dtype=np.int64) << 16).astype(np.int64)
+
+
+# --------------------------------------------------------------------------
+# sparse matrices
+# --------------------------------------------------------------------------
+class SparseMatrix:
+    """A one-PE sparsemat_t whose arrays are numpy int64 buffers:
+    ``offset`` (numrows+1 row offsets) and ``nonzero`` (ascending columns)."""
+
+    def __init__(self, offset: np.ndarray, nonzero: np.ndarray, numcols: Optional[int] = None):
+        self.offset = np.ascontiguousarray(offset, dtype=np.int64)
+        self.nonzero = np.ascontiguousarray(nonzero, dtype=np.int64)
+        n = int(self.offset.shape[0]) - 1
+        if n < 0:
+            raise ValueError("offset needs at least one entry")
+        self.numrows = n
+        self.numcols = n if numcols is None else int(numcols)
+        nnz = int(self.nonzero.shape[0])
+        po, pn = _p(self.offset), _p(self.nonzero)
+        self._struct = sparsemat_t(0, n, n, self.numcols, nnz, nnz, po, po, pn, pn)
+
+    @property
+    def nnz(self) -> int:
+        return int(self.nonzero.shape[0])
+
+    @property
+    def struct(self) -> sparsemat_t:
+        return self._struct
+
+    def ptr(self):
+        return C.pointer(self._struct)
+
+    @classmethod
+    def _from_c(cls, m, what: str) -> "SparseMatrix":
+        if not m:
+            raise BaleError(f"{what}: generator failed (bad parameters or out of memory)")
+        try:
+            s = m.contents
+            n, nnz = int(s.numrows), int(s.nnz)
+            off = np.ctypeslib.as_array(s.loffset, shape=(n + 1,)).copy()
+            col = (np.ctypeslib.as_array(s.lnonzero, shape=(nnz,)).copy() if nnz
+                   else np.zeros(0, np.int64))
+            return cls(off, col, int(s.numcols))
+        finally:
+            _lib.bale_free_matrix(m)
+
+    def row(self, i: int) -> np.ndarray:
+        return self.nonzero[self.offset[i]:self.offset[i + 1]]
+
+
+# --------------------------------------------------------------------------
+# drop-ins: histogram (apps/histo_src/histo.h:47-50)
+# --------------------------------------------------------------------------
+def histo_agi(index: np.ndarray, counts: np.ndarray, length: Optional[int] = None) -> float:
+    """counts[index[i]] += 1 for i < length (default len(index))."""
+    _arr(index, "index"), _arr(counts, "counts", True)
+    n = index.size if length is None else int(length)
+    return _seconds(_lib.histo_agi(_p(index), n, _p(counts)), "histo_agi")
+
+
+def histo_exstack(pckindx: np.ndarray, lcounts: np.ndarray, buf_cnt: int = 1024,
+                  length: Optional[int] = None) -> float:
+    """lcounts[pckindx[i] >> 16] += 1 (one PE)."""
+    _arr(pckindx, "pckindx"), _arr(lcounts, "lcounts", True)
+    n = pckindx.size if length is None else int(length)
+    return _seconds(_lib.histo_exstack(_p(pckindx), n, _p(lcounts), buf_cnt), "histo_exstack")
+
+
+def histo_exstack2(pckindx: np.ndarray, lcounts: np.ndarray, buf_cnt: int = 1024,
+                   length: Optional[int] = None) -> float:
+    _arr(pckindx, "pckindx"), _arr(lcounts, "lcounts", True)
+    n = pckindx.size if length is None else int(length)
+    return _seconds(_lib.histo_exstack2(_p(pckindx), n, _p(lcounts), buf_cnt), "histo_exstack2")
+
+
+def histo_conveyor(pckindx: np.ndarray, lcounts: np.ndarray, length: Optional[int] = None) -> float:
+    _arr(pckindx, "pckindx"), _arr(lcounts, "lcounts", True)
+    n = pckindx.size if length is None else int(length)
+    return _seconds(_lib.histo_conveyor(_p(pckindx), n, _p(lcounts)), "histo_conveyor")
+
+
+# --------------------------------------------------------------------------
+# drop-ins: index gather (apps/ig_src/ig.h:49-52)
+# --------------------------------------------------------------------------
+def ig_agi(tgt: np.ndarray, index: np.ndarray, table: np.ndarray, length: Optional[int] = None) -> float:
+    """tgt[i] = table[index[i]] for i < length (default len(index))."""
+    _arr(tgt, "tgt", True), _arr(index, "index"), _arr(table, "table")
+    n = index.size if length is None else int(length)
+    if tgt.size < n:
+        raise ValueError("tgt is shorter than the request count")
+    return _seconds(_lib.ig_agi(_p(tgt), _p(index), n, _p(table)), "ig_agi")
+
+
+def ig_exstack(tgt: np.ndarray, pckindx: np.ndarray, ltable: np.ndarray, buf_cnt: int = 1024,
+               length: Optional[int] = None) -> float:
+    """tgt[i] = ltable[pckindx[i] >> 16] (one PE)."""
+    _arr(tgt, "tgt", True), _arr(pckindx, "pckindx"), _arr(ltable, "ltable")
+    n = pckindx.size if length is None else int(length)
+    if tgt.size < n:
+        raise ValueError("tgt is shorter than the request count")
+    return _seconds(_lib.ig_exstack(_p(tgt), _p(pckindx), n, _p(ltable), buf_cnt), "ig_exstack")
+
+
+def ig_exstack2(tgt: np.ndarray, pckindx: np.ndarray, ltable: np.ndarray, buf_cnt: int = 1024,
+                length: Optional[int] = None) -> float:
+    _arr(tgt, "tgt", True), _arr(pckindx, "pckindx"), _arr(ltable, "ltable")
+    n = pckindx.size if length is None else int(length)
+    if tgt.size < n:
+        raise ValueError("tgt is shorter than the request count")
+    return _seconds(_lib.ig_exstack2(_p(tgt), _p(pckindx), n, _p(ltable), buf_cnt), "ig_exstack2")
+
+
+def ig_conveyor(tgt: np.ndarray, pckindx: np.ndarray, ltable: np.ndarray,
+                length: Optional[int] = None) -> float:
+    _arr(tgt, "tgt", True), _arr(pckindx, "pckindx"), _arr(ltable, "ltable")
+    n = pckindx.size if length is None else int(length)
+    if tgt.size < n:
+        raise ValueError("tgt is shorter than the request count")
+    return _seconds(_lib.ig_conveyor(_p(tgt), _p(pckindx), n, _p(ltable)), "ig_conveyor")
+
+
+# --------------------------------------------------------------------------
+# drop-ins: triangles (apps/triangle_src/triangle.h:50-61)
+# --------------------------------------------------------------------------
+def _tri(fn, name: str, L: SparseMatrix, U: Optional[SparseMatrix], alg: int, *extra):
+    if not isinstance(L, SparseMatrix):
+        raise TypeError("L must be a SparseMatrix")
+    cnt, sr = C.c_int64(0), C.c_int64(0)
+    u = U.ptr() if U is not None else None
+    t = fn(C.byref(cnt), C.byref(sr), L.ptr(), u, alg, *extra)
+    return int(cnt.value), int(sr.value), _seconds(t, name)
+
+
+def triangle_agi(L: SparseMatrix, U: Optional[SparseMatrix] = None, alg: int = 0):
+    """(count, sr, seconds): triangles of the strictly lower tidy L."""
+    return _tri(_lib.triangle_agi, "triangle_agi", L, U, alg)
+
+
+def triangle_exstack_push(L: SparseMatrix, U: Optional[SparseMatrix] = None, alg: int = 0,
+                          bufsiz: int = 1024):
+    return _tri(_lib.triangle_exstack_push, "triangle_exstack_push", L, U, alg, bufsiz)
+
+
+def triangle_exstack2_push(L: SparseMatrix, U: Optional[SparseMatrix] = None, alg: int = 0,
+                           bufsiz: int = 1024):
+    return _tri(_lib.triangle_exstack2_push, "triangle_exstack2_push", L, U, alg, bufsiz)
+
+
+def triangle_convey_push(L: SparseMatrix, U: Optional[SparseMatrix] = None, alg: int = 0):
+    return _tri(_lib.triangle_convey_push, "triangle_convey_push", L, U, alg)
+
+
+def triangle_agi_iter(L: SparseMatrix, U: Optional[SparseMatrix] = None, alg: int = 0):
+    return _tri(_lib.triangle_agi_iter, "triangle_agi_iter", L, U, alg)
+
+
+# --------------------------------------------------------------------------
+# device-resident entry points (torch CUDA tensors as plumbing)
+# --------------------------------------------------------------------------
+def _dptr(t, name: str, dtype=None) -> int:
+    import torch
+
+    if not isinstance(t, torch.Tensor) or not t.is_cuda:
+        raise TypeError(f"{name} must be a CUDA tensor")
+    if t.dtype != torch.int64 or not t.is_contiguous():
+        raise TypeError(f"{name} must be a contiguous int64 tensor")
+    return t.data_ptr()
+
+
+def _stream(stream) -> int:
+    if stream is None:
+        import torch
+
+        return torch.cuda.current_stream().cuda_stream
+    return int(getattr(stream, "cuda_stream", stream))
+
+
+def _status(rc: int, what: str) -> None:
+    if rc != 0:
+        raise BaleError(f"{what}: status {rc}: {_last_error()}")
+
+
+def histo_dev(counts, index, shift: int = 0, bad=None, stream=None, n: Optional[int] = None) -> None:
+    """counts[index[i] >> shift] += 1 on the device (asynchronous)."""
+    nn = index.numel() if n is None else int(n)
+    _status(_lib.bale_histo_dev(_dptr(counts, "counts"), counts.numel(), _dptr(index, "index"), nn,
+                                shift, _dptr(bad, "bad") if bad is not None else None,
+                                _stream(stream)), "bale_histo_dev")
+
+
+def ig_dev(tgt, index, table, shift: int = 0, bad=None, stream=None, n: Optional[int] = None) -> None:
+    """tgt[i] = table[index[i] >> shift] on the device (asynchronous)."""
+    nn = index.numel() if n is None else int(n)
+    _status(_lib.bale_ig_dev(_dptr(tgt, "tgt"), _dptr(index, "index"), nn, _dptr(table, "table"),
+                             table.numel(), shift, _dptr(bad, "bad") if bad is not None else None,
+                             _stream(stream)), "bale_ig_dev")
+
+
+def triangle_dev(offset, nonzero, count, work=None, bad=None, stream=None) -> None:
+    """count[0] += triangles of the device CSR (asynchronous)."""
+    _status(_lib.bale_triangle_dev(_dptr(offset, "offset"), _dptr(nonzero, "nonzero"),
+                                   offset.numel() - 1, nonzero.numel(), _dptr(count, "count"),
+                                   _dptr(work, "work") if work is not None else None,
+                                   _dptr(bad, "bad") if bad is not None else None,
+                                   _stream(stream)), "bale_triangle_dev")
+
+
+# --------------------------------------------------------------------------
+# seeded inputs (include/bale_inputs.h)
+# --------------------------------------------------------------------------
+def splitmix64(seed: int, i: int) -> int:
+    return int(_lib.bale_splitmix64(seed & (2**64 - 1), i))
+
+
+def _gen_status(rc: int, what: str) -> None:
+    if rc != 0:
+        raise BaleError(f"{what}: invalid parameters")
+
+
+def gen_uniform(n: int, rng: int, seed: int, packed: bool = False) -> np.ndarray:
+    out = np.empty(n, np.int64)
+    _gen_status(_lib.bale_gen_uniform(_p(out), n, rng, seed & (2**64 - 1), int(packed)), "gen_uniform")
+    return out
+
+
+def gen_values(n: int, seed: int) -> np.ndarray:
+    out = np.empty(n, np.int64)
+    _gen_status(_lib.bale_gen_values(_p(out), n, seed & (2**64 - 1)), "gen_values")
+    return out
+
+
+def gen_negative_table(n: int) -> np.ndarray:
+    out = np.empty(n, np.int64)
+    _gen_status(_lib.bale_gen_negative_table(_p(out), n), "gen_negative_table")
+    return out
+
+
+def gen_zipf(n: int, rng: int, s: float, seed_rank: int, seed_perm: int,
+             packed: bool = False) -> np.ndarray:
+    out = np.empty(n, np.int64)
+    _gen_status(_lib.bale_gen_zipf(_p(out), n, rng, s, seed_rank & (2**64 - 1),
+                                   seed_perm & (2**64 - 1), int(packed)), "gen_zipf")
+    return out
+
+
+def keyed_perm(r: int, rng: int, key: int) -> int:
+    return int(_lib.bale_keyed_perm(r, rng, key & (2**64 - 1)))
+
+
+def gen_rmat(scale: int, edgefactor: int = 16, a: float = 0.57, b: float = 0.19, c: float = 0.19,
+             seed: int = 6) -> SparseMatrix:
+    return SparseMatrix._from_c(_lib.bale_gen_rmat(scale, edgefactor, a, b, c, seed & (2**64 - 1)),
+                                "gen_rmat")
+
+
+def gen_erdos_renyi(n: int, p: float, seed: int = 7) -> SparseMatrix:
+    return SparseMatrix._from_c(_lib.bale_gen_erdos_renyi(n, p, seed & (2**64 - 1)), "gen_erdos_renyi")
+
+
+def gen_kronecker(mode: int, specs: Sequence[int]) -> SparseMatrix:
+    arr = np.ascontiguousarray(np.asarray(list(specs), dtype=np.int64))
+    return SparseMatrix._from_c(_lib.bale_gen_kronecker(mode, _p(arr), arr.size), "gen_kronecker")
+
+
+def kronecker_triangles(mode: int, specs: Iterable[int]) -> int:
+    arr = np.ascontiguousarray(np.asarray(list(specs), dtype=np.int64))
+    return int(_lib.bale_kronecker_triangles(mode, _p(arr), arr.size))
+
+
+def set_host_threads(n: int) -> None:
+    _lib.bale_set_host_threads(int(n))
+
+
+def release_buffers() -> None:
+    _lib.bale_release_buffers()
+
+
+def version() -> str:
+    return _lib.bale_version().decode()

@@ -1,0 +1,90 @@
+"""ctypes binding of libbale_gb300.so (the C ABI in include/bale_gb300.h and
+include/bale_inputs.h).  Importing this module never falls back to anything:
+if the shared library is missing it raises, naming the build command."""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+PKG = Path(__file__).resolve().parent
+LIB_PATH = PKG / "libbale_gb300.so"
+
+i64 = C.c_int64
+u64 = C.c_uint64
+P64 = C.POINTER(C.c_int64)
+VP = C.c_void_p
+
+
+class sparsemat_t(C.Structure):
+    """Layout of the reference's sparsemat_t (spmat/spmat.h:73-86)."""
+
+    _fields_ = [
+        ("local", i64), ("numrows", i64), ("lnumrows", i64), ("numcols", i64),
+        ("nnz", i64), ("lnnz", i64),
+        ("offset", P64), ("loffset", P64), ("nonzero", P64), ("lnonzero", P64),
+    ]
+
+
+PSM = C.POINTER(sparsemat_t)
+
+# name -> (restype, argtypes)
+SIGNATURES: dict[str, tuple[object, list[object]]] = {
+    # drop-ins (apps/histo_src/histo.h:47-50)
+    "histo_agi": (C.c_double, [P64, i64, P64]),
+    "histo_exstack": (C.c_double, [P64, i64, P64, i64]),
+    "histo_exstack2": (C.c_double, [P64, i64, P64, i64]),
+    "histo_conveyor": (C.c_double, [P64, i64, P64]),
+    # apps/ig_src/ig.h:49-52
+    "ig_agi": (C.c_double, [P64, P64, i64, P64]),
+    "ig_exstack": (C.c_double, [P64, P64, i64, P64, i64]),
+    "ig_exstack2": (C.c_double, [P64, P64, i64, P64, i64]),
+    "ig_conveyor": (C.c_double, [P64, P64, i64, P64]),
+    # apps/triangle_src/triangle.h:50-61
+    "triangle_agi": (C.c_double, [P64, P64, PSM, PSM, i64]),
+    "triangle_exstack_push": (C.c_double, [P64, P64, PSM, PSM, i64, i64]),
+    "triangle_exstack2_push": (C.c_double, [P64, P64, PSM, PSM, i64, i64]),
+    "triangle_convey_push": (C.c_double, [P64, P64, PSM, PSM, i64]),
+    "triangle_agi_iter": (C.c_double, [P64, P64, PSM, PSM, i64]),
+    # library state
+    "bale_last_error": (C.c_char_p, []),
+    "bale_version": (C.c_char_p, []),
+    "bale_release_buffers": (None, []),
+    # device-resident
+    "bale_histo_dev": (C.c_int, [VP, i64, VP, i64, C.c_int, VP, VP]),
+    "bale_ig_dev": (C.c_int, [VP, VP, i64, VP, i64, C.c_int, VP, VP]),
+    "bale_triangle_dev": (C.c_int, [VP, VP, i64, i64, VP, VP, VP, VP]),
+    # inputs
+    "bale_splitmix64": (u64, [u64, u64]),
+    "bale_gen_uniform": (C.c_int, [P64, i64, i64, u64, C.c_int]),
+    "bale_gen_values": (C.c_int, [P64, i64, u64]),
+    "bale_gen_negative_table": (C.c_int, [P64, i64]),
+    "bale_gen_zipf": (C.c_int, [P64, i64, i64, C.c_double, u64, u64, C.c_int]),
+    "bale_keyed_perm": (i64, [i64, i64, u64]),
+    "bale_gen_rmat": (PSM, [i64, i64, C.c_double, C.c_double, C.c_double, u64]),
+    "bale_gen_erdos_renyi": (PSM, [i64, C.c_double, u64]),
+    "bale_gen_kronecker": (PSM, [C.c_int, P64, i64]),
+    "bale_kronecker_triangles": (i64, [C.c_int, P64, i64]),
+    "bale_make_matrix": (PSM, [i64, i64, i64]),
+    "bale_free_matrix": (None, [PSM]),
+    "bale_set_host_threads": (None, [C.c_int]),
+}
+
+_lib: C.CDLL | None = None
+
+
+def load() -> C.CDLL:
+    """Load libbale_gb300.so once and declare every exported signature."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB_PATH.exists():
+        raise ImportError(
+            f"{LIB_PATH} is not built; run `python -m bale_old_gb300.build` "
+            "(or __graft_entry__.build())")
+    lib = C.CDLL(str(LIB_PATH))
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib

@@ -1,0 +1,389 @@
+// capi.cu -- the C ABI of libbale_gb300.so (declared in include/bale_gb300.h).
+//
+// Drop-ins keep the reference signatures (apps/histo_src/histo.h:47-50,
+// apps/ig_src/ig.h:49-52, apps/triangle_src/triangle.h:50-61): host arrays
+// in, host arrays out, synchronous, wall seconds returned, -1.0 on failure.
+// The reference's signatures carry no table length (the SHARED arrays'
+// extents are implied by the app), so the drop-ins derive the extent the
+// call can touch from the data: the largest index, computed on the device
+// after the index array is uploaded.  Exactly counts[0..max] / table[0..max]
+// are moved, which the reference would also have been allowed to access.
+#include <chrono>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+
+#include "common.cuh"
+
+namespace bale {
+
+// ---------------------------------------------------------------------------
+// errors, device facts, scratch
+// ---------------------------------------------------------------------------
+static thread_local char t_err[512] = "";
+
+void set_error(const char *fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(t_err, sizeof(t_err), fmt, ap);
+  va_end(ap);
+}
+
+int current_device() {
+  int d = 0;
+  if (cudaGetDevice(&d) != cudaSuccess) return 0;
+  return d;
+}
+
+int num_sms() {
+  static int cache[64] = {0};
+  int d = current_device();
+  if (d < 0 || d >= 64) d = 0;
+  if (cache[d] == 0) {
+    int v = 0;
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, d) != cudaSuccess || v <= 0) v = 1;
+    cache[d] = v;
+  }
+  return cache[d];
+}
+
+static std::mutex g_scratch_mu;
+static DeviceScratch g_scratch[64];
+
+DeviceScratch *device_scratch() {
+  int d = current_device();
+  if (d < 0 || d >= 64) return nullptr;
+  std::lock_guard<std::mutex> lk(g_scratch_mu);
+  DeviceScratch &s = g_scratch[d];
+  if (!s.words) {
+    void *p = nullptr;
+    if (cudaMalloc(&p, kScratchWords * sizeof(unsigned long long)) != cudaSuccess) {
+      set_error("cudaMalloc of %d scratch words failed", kScratchWords);
+      return nullptr;
+    }
+    if (cudaMemset(p, 0, kScratchWords * sizeof(unsigned long long)) != cudaSuccess) {
+      cudaFree(p);
+      set_error("cudaMemset of scratch words failed");
+      return nullptr;
+    }
+    s.words = static_cast<unsigned long long *>(p);
+  }
+  return &s;
+}
+
+// Scratch word layout used by the synchronous drop-ins (serialised by
+// g_dropin_mu): [0] bad-input count, [1] index max, [2] triangle count,
+// [3] triangle work.  [7] absorbs bad counts the caller does not want.
+enum { kWordBad = 0, kWordMax = 1, kWordCount = 2, kWordWork = 3, kWordDiscard = 7 };
+
+// ---------------------------------------------------------------------------
+// drop-in state: a stream and grow-only device buffers per device
+// ---------------------------------------------------------------------------
+struct DevBuf {
+  void *p = nullptr;
+  size_t cap = 0;
+  int ensure(size_t bytes) {
+    if (bytes <= cap && p) return BALE_OK;
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+    size_t want = bytes < 256 ? 256 : bytes;
+    if (cudaMalloc(&p, want) != cudaSuccess) {
+      cudaGetLastError();
+      set_error("cudaMalloc(%zu bytes) failed", want);
+      return BALE_ENOMEM;
+    }
+    cap = want;
+    return BALE_OK;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+  }
+};
+
+struct DropinState {
+  cudaStream_t stream = nullptr;
+  DevBuf buf[4];
+};
+
+static std::mutex g_dropin_mu;
+static DropinState g_state[64];
+
+static DropinState *dropin_state() {
+  int d = current_device();
+  if (d < 0 || d >= 64) return nullptr;
+  DropinState &s = g_state[d];
+  if (!s.stream) {
+    if (cudaStreamCreateWithFlags(&s.stream, cudaStreamNonBlocking) != cudaSuccess) {
+      set_error("cudaStreamCreate failed");
+      s.stream = nullptr;
+      return nullptr;
+    }
+  }
+  return &s;
+}
+
+static double now_seconds() {
+  using namespace std::chrono;
+  return duration_cast<duration<double>>(steady_clock::now().time_since_epoch()).count();
+}
+
+#define DROPIN_TRY(expr)             \
+  do {                               \
+    int _rc = (expr);                \
+    if (_rc != BALE_OK) return -1.0; \
+  } while (0)
+
+#define DROPIN_CUDA(expr)                                                          \
+  do {                                                                             \
+    cudaError_t _e = (expr);                                                       \
+    if (_e != cudaSuccess) {                                                       \
+      set_error("%s failed: %s", #expr, cudaGetErrorString(_e));                   \
+      return -1.0;                                                                 \
+    }                                                                              \
+  } while (0)
+
+// Upload index[0,n) into buf[0] and find the largest (shifted) index; the
+// result is the number of table entries the call touches (max + 1).
+static double extent_of(DropinState *st, DeviceScratch *ds, const int64_t *index, int64_t n,
+                        int shift, int64_t *extent) {
+  const size_t bytes = static_cast<size_t>(n) * sizeof(int64_t);
+  DROPIN_TRY(st->buf[0].ensure(bytes));
+  DROPIN_CUDA(cudaMemsetAsync(ds->words, 0, 8 * sizeof(unsigned long long), st->stream));
+  DROPIN_CUDA(cudaMemcpyAsync(st->buf[0].p, index, bytes, cudaMemcpyHostToDevice, st->stream));
+  DROPIN_TRY(launch_index_max(static_cast<const int64_t *>(st->buf[0].p), n, shift,
+                              ds->words + kWordMax, st->stream));
+  unsigned long long mx = 0;
+  DROPIN_CUDA(cudaMemcpyAsync(&mx, ds->words + kWordMax, sizeof(mx), cudaMemcpyDeviceToHost, st->stream));
+  DROPIN_CUDA(cudaStreamSynchronize(st->stream));
+  if (mx >= (1ull << 60)) {
+    set_error("index out of range (negative or >= 2^60): max index %llu", mx);
+    return -1.0;
+  }
+  *extent = static_cast<int64_t>(mx) + 1;
+  return 0.0;
+}
+
+static double histo_dropin(const int64_t *index, int64_t n, int64_t *counts, int shift) {
+  const double t0 = now_seconds();
+  if (n < 0 || (n > 0 && (!index || !counts))) {
+    set_error("histo: bad arguments (len=%lld)", static_cast<long long>(n));
+    return -1.0;
+  }
+  if (n == 0) return now_seconds() - t0;
+  std::lock_guard<std::mutex> lk(g_dropin_mu);
+  DropinState *st = dropin_state();
+  DeviceScratch *ds = device_scratch();
+  if (!st || !ds) return -1.0;
+  int64_t extent = 0;
+  if (extent_of(st, ds, index, n, shift, &extent) < 0) return -1.0;
+  const size_t cbytes = static_cast<size_t>(extent) * sizeof(int64_t);
+  DROPIN_TRY(st->buf[1].ensure(cbytes));
+  int64_t *d_counts = static_cast<int64_t *>(st->buf[1].p);
+  DROPIN_CUDA(cudaMemcpyAsync(d_counts, counts, cbytes, cudaMemcpyHostToDevice, st->stream));
+  DROPIN_TRY(launch_histo(d_counts, extent, static_cast<const int64_t *>(st->buf[0].p), n, shift,
+                          ds->words + kWordBad, st->stream));
+  DROPIN_CUDA(cudaMemcpyAsync(counts, d_counts, cbytes, cudaMemcpyDeviceToHost, st->stream));
+  unsigned long long bad = 0;
+  DROPIN_CUDA(cudaMemcpyAsync(&bad, ds->words + kWordBad, sizeof(bad), cudaMemcpyDeviceToHost, st->stream));
+  DROPIN_CUDA(cudaStreamSynchronize(st->stream));
+  if (bad) {
+    set_error("histo: %llu out-of-range indices", bad);
+    return -1.0;
+  }
+  return now_seconds() - t0;
+}
+
+static double ig_dropin(int64_t *tgt, const int64_t *index, int64_t n, const int64_t *table,
+                        int shift) {
+  const double t0 = now_seconds();
+  if (n < 0 || (n > 0 && (!index || !tgt || !table))) {
+    set_error("ig: bad arguments (l_num_req=%lld)", static_cast<long long>(n));
+    return -1.0;
+  }
+  if (n == 0) return now_seconds() - t0;
+  std::lock_guard<std::mutex> lk(g_dropin_mu);
+  DropinState *st = dropin_state();
+  DeviceScratch *ds = device_scratch();
+  if (!st || !ds) return -1.0;
+  int64_t extent = 0;
+  if (extent_of(st, ds, index, n, shift, &extent) < 0) return -1.0;
+  const size_t tbytes = static_cast<size_t>(extent) * sizeof(int64_t);
+  const size_t obytes = static_cast<size_t>(n) * sizeof(int64_t);
+  DROPIN_TRY(st->buf[1].ensure(tbytes));
+  DROPIN_TRY(st->buf[2].ensure(obytes));
+  DROPIN_CUDA(cudaMemcpyAsync(st->buf[1].p, table, tbytes, cudaMemcpyHostToDevice, st->stream));
+  DROPIN_TRY(launch_ig(static_cast<int64_t *>(st->buf[2].p), static_cast<const int64_t *>(st->buf[0].p), n,
+                       static_cast<const int64_t *>(st->buf[1].p), extent, shift, ds->words + kWordBad,
+                       st->stream));
+  DROPIN_CUDA(cudaMemcpyAsync(tgt, st->buf[2].p, obytes, cudaMemcpyDeviceToHost, st->stream));
+  unsigned long long bad = 0;
+  DROPIN_CUDA(cudaMemcpyAsync(&bad, ds->words + kWordBad, sizeof(bad), cudaMemcpyDeviceToHost, st->stream));
+  DROPIN_CUDA(cudaStreamSynchronize(st->stream));
+  if (bad) {
+    set_error("ig: %llu out-of-range indices", bad);
+    return -1.0;
+  }
+  return now_seconds() - t0;
+}
+
+static double triangle_dropin(int64_t *count, int64_t *sr, sparsemat_t *L) {
+  const double t0 = now_seconds();
+  if (!count || !sr || !L) {
+    set_error("triangle: NULL count, sr or L");
+    return -1.0;
+  }
+  const int64_t n = L->lnumrows;
+  if (n < 0 || (n > 0 && !L->loffset)) {
+    set_error("triangle: bad matrix (lnumrows=%lld)", static_cast<long long>(n));
+    return -1.0;
+  }
+  const int64_t nnz = n > 0 ? L->loffset[n] : 0;
+  if (nnz < 0 || (nnz > 0 && !L->lnonzero)) {
+    set_error("triangle: bad matrix (nnz=%lld)", static_cast<long long>(nnz));
+    return -1.0;
+  }
+  std::lock_guard<std::mutex> lk(g_dropin_mu);
+  DropinState *st = dropin_state();
+  DeviceScratch *ds = device_scratch();
+  if (!st || !ds) return -1.0;
+  const size_t obytes = static_cast<size_t>(n + 1) * sizeof(int64_t);
+  const size_t cbytes = static_cast<size_t>(nnz > 0 ? nnz : 1) * sizeof(int64_t);
+  DROPIN_TRY(st->buf[0].ensure(obytes));
+  DROPIN_TRY(st->buf[1].ensure(cbytes));
+  DROPIN_CUDA(cudaMemsetAsync(ds->words, 0, 8 * sizeof(unsigned long long), st->stream));
+  DROPIN_CUDA(cudaMemcpyAsync(st->buf[0].p, L->loffset, obytes, cudaMemcpyHostToDevice, st->stream));
+  if (nnz > 0)
+    DROPIN_CUDA(cudaMemcpyAsync(st->buf[1].p, L->lnonzero, static_cast<size_t>(nnz) * sizeof(int64_t),
+                                cudaMemcpyHostToDevice, st->stream));
+  DROPIN_TRY(launch_triangle(static_cast<const int64_t *>(st->buf[0].p),
+                             static_cast<const int64_t *>(st->buf[1].p), n, nnz,
+                             ds->words + kWordCount, ds->words + kWordWork, ds->words + kWordBad,
+                             st->stream));
+  unsigned long long w[4] = {0, 0, 0, 0};
+  DROPIN_CUDA(cudaMemcpyAsync(w, ds->words, sizeof(w), cudaMemcpyDeviceToHost, st->stream));
+  DROPIN_CUDA(cudaStreamSynchronize(st->stream));
+  if (w[kWordBad]) {
+    set_error("triangle: L is not a strictly lower-triangular tidy CSR (%llu bad rows/offsets)",
+              w[kWordBad]);
+    return -1.0;
+  }
+  *count = static_cast<int64_t>(w[kWordCount]);
+  *sr = static_cast<int64_t>(w[kWordWork]);
+  return now_seconds() - t0;
+}
+
+}  // namespace bale
+
+using namespace bale;
+
+extern "C" {
+
+double histo_agi(int64_t *index, int64_t len, int64_t *counts) {
+  return histo_dropin(index, len, counts, 0);
+}
+double histo_exstack(int64_t *pckindx, int64_t len, int64_t *lcounts, int64_t buf_cnt) {
+  (void)buf_cnt;
+  return histo_dropin(pckindx, len, lcounts, 16);
+}
+double histo_exstack2(int64_t *pckindx, int64_t len, int64_t *lcounts, int64_t buf_cnt) {
+  (void)buf_cnt;
+  return histo_dropin(pckindx, len, lcounts, 16);
+}
+double histo_conveyor(int64_t *pckindx, int64_t len, int64_t *lcounts) {
+  return histo_dropin(pckindx, len, lcounts, 16);
+}
+
+double ig_agi(int64_t *tgt, int64_t *index, int64_t l_num_req, int64_t *table) {
+  return ig_dropin(tgt, index, l_num_req, table, 0);
+}
+double ig_exstack(int64_t *tgt, int64_t *pckindx, int64_t l_num_req, int64_t *ltable, int64_t buf_cnt) {
+  (void)buf_cnt;
+  return ig_dropin(tgt, pckindx, l_num_req, ltable, 16);
+}
+double ig_exstack2(int64_t *tgt, int64_t *pckindx, int64_t l_num_req, int64_t *ltable, int64_t buf_cnt) {
+  (void)buf_cnt;
+  return ig_dropin(tgt, pckindx, l_num_req, ltable, 16);
+}
+double ig_conveyor(int64_t *tgt, int64_t *pckindx, int64_t l_num_req, int64_t *ltable) {
+  return ig_dropin(tgt, pckindx, l_num_req, ltable, 16);
+}
+
+double triangle_agi(int64_t *count, int64_t *sr, sparsemat_t *L, sparsemat_t *U, int64_t alg) {
+  (void)U; (void)alg;
+  return triangle_dropin(count, sr, L);
+}
+double triangle_exstack_push(int64_t *count, int64_t *sr, sparsemat_t *L, sparsemat_t *U, int64_t alg,
+                             int64_t bufsiz) {
+  (void)U; (void)alg; (void)bufsiz;
+  return triangle_dropin(count, sr, L);
+}
+double triangle_exstack2_push(int64_t *count, int64_t *sr, sparsemat_t *L, sparsemat_t *U, int64_t alg,
+                              int64_t bufsiz) {
+  (void)U; (void)alg; (void)bufsiz;
+  return triangle_dropin(count, sr, L);
+}
+double triangle_convey_push(int64_t *count, int64_t *sr, sparsemat_t *L, sparsemat_t *U, int64_t alg) {
+  (void)U; (void)alg;
+  return triangle_dropin(count, sr, L);
+}
+double triangle_agi_iter(int64_t *count, int64_t *sr, sparsemat_t *L, sparsemat_t *U, int64_t alg) {
+  (void)U; (void)alg;
+  return triangle_dropin(count, sr, L);
+}
+
+const char *bale_last_error(void) { return t_err; }
+const char *bale_version(void) { return "bale_gb300 0.1 (sm_103a)"; }
+
+void bale_release_buffers(void) {
+  std::lock_guard<std::mutex> lk(g_dropin_mu);
+  for (int d = 0; d < 64; d++)
+    for (auto &b : g_state[d].buf) b.release();
+}
+
+int bale_histo_dev(int64_t *d_counts, int64_t ncounts, const int64_t *d_index, int64_t n, int shift,
+                   int64_t *d_bad, void *stream) {
+  if (n < 0 || ncounts < 0 || (shift != 0 && shift != 16) || (n > 0 && (!d_counts || !d_index))) {
+    set_error("bale_histo_dev: bad arguments");
+    return BALE_EINVAL;
+  }
+  if (n == 0) return BALE_OK;
+  DeviceScratch *ds = device_scratch();
+  if (!ds) return BALE_ECUDA;
+  unsigned long long *bad = d_bad ? reinterpret_cast<unsigned long long *>(d_bad) : ds->words + kWordDiscard;
+  return launch_histo(d_counts, ncounts, d_index, n, shift, bad, static_cast<cudaStream_t>(stream));
+}
+
+int bale_ig_dev(int64_t *d_tgt, const int64_t *d_index, int64_t n, const int64_t *d_table, int64_t table_len,
+                int shift, int64_t *d_bad, void *stream) {
+  if (n < 0 || table_len < 0 || (shift != 0 && shift != 16) ||
+      (n > 0 && (!d_tgt || !d_index || (table_len > 0 && !d_table)))) {
+    set_error("bale_ig_dev: bad arguments");
+    return BALE_EINVAL;
+  }
+  if (n == 0) return BALE_OK;
+  DeviceScratch *ds = device_scratch();
+  if (!ds) return BALE_ECUDA;
+  unsigned long long *bad = d_bad ? reinterpret_cast<unsigned long long *>(d_bad) : ds->words + kWordDiscard;
+  return launch_ig(d_tgt, d_index, n, d_table, table_len, shift, bad, static_cast<cudaStream_t>(stream));
+}
+
+int bale_triangle_dev(const int64_t *d_offset, const int64_t *d_nonzero, int64_t numrows, int64_t nnz,
+                      int64_t *d_count, int64_t *d_work, int64_t *d_bad, void *stream) {
+  if (numrows < 0 || nnz < 0 || !d_count || (numrows > 0 && !d_offset) || (nnz > 0 && !d_nonzero)) {
+    set_error("bale_triangle_dev: bad arguments");
+    return BALE_EINVAL;
+  }
+  if (numrows == 0) return BALE_OK;
+  DeviceScratch *ds = device_scratch();
+  if (!ds) return BALE_ECUDA;
+  unsigned long long *bad = d_bad ? reinterpret_cast<unsigned long long *>(d_bad) : ds->words + kWordDiscard;
+  return launch_triangle(d_offset, d_nonzero, numrows, nnz, reinterpret_cast<unsigned long long *>(d_count),
+                         reinterpret_cast<unsigned long long *>(d_work), bad,
+                         static_cast<cudaStream_t>(stream));
+}
+
+}  // extern "C"

@@ -1,0 +1,87 @@
+// common.cuh -- shared device helpers and host plumbing for libbale_gb300.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "bale_gb300.h"
+
+namespace bale {
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+// Records a printf-style message as the calling thread's last error.
+void set_error(const char *fmt, ...);
+// Number of SMs of the current device (cached per device).
+int num_sms();
+// Current device ordinal (cached per call site use).
+int current_device();
+
+// Device-wide scratch words owned by the library (per device): the in-kernel
+// bad-input counter and the triangle work cursor.  Allocated once.
+struct DeviceScratch {
+  unsigned long long *words;  // kScratchWords zero-initialised u64
+};
+constexpr int kScratchWords = 1024;
+DeviceScratch *device_scratch();
+
+#define BALE_CUDA_OK(expr)                                                        \
+  do {                                                                            \
+    cudaError_t _e = (expr);                                                      \
+    if (_e != cudaSuccess) {                                                      \
+      ::bale::set_error("%s failed: %s (%s:%d)", #expr, cudaGetErrorString(_e),   \
+                        __FILE__, __LINE__);                                      \
+      return BALE_ECUDA;                                                          \
+    }                                                                             \
+  } while (0)
+
+// Launch entry points used by the C ABI (all asynchronous on `stream`).
+int launch_ig(int64_t *tgt, const int64_t *index, int64_t n, const int64_t *table,
+              int64_t table_len, int shift, unsigned long long *bad, cudaStream_t stream);
+int launch_histo(int64_t *counts, int64_t ncounts, const int64_t *index, int64_t n, int shift,
+                 unsigned long long *bad, cudaStream_t stream);
+int launch_triangle(const int64_t *offset, const int64_t *nonzero, int64_t numrows, int64_t nnz,
+                    unsigned long long *count, unsigned long long *work,
+                    unsigned long long *bad, cudaStream_t stream);
+// max over index[i] >> shift into *out (u64, must start at 0); negatives count as huge.
+int launch_index_max(const int64_t *index, int64_t n, int shift, unsigned long long *out,
+                     cudaStream_t stream);
+
+// ---------------------------------------------------------------------------
+// device side
+// ---------------------------------------------------------------------------
+#ifdef __CUDACC__
+__device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
+
+// Streaming 16-byte load that does not allocate in L1 and is marked
+// evict-first in L2 (the index stream is read once).
+__device__ __forceinline__ longlong2 ld_stream_v2(const longlong2 *p) { return __ldcs(p); }
+__device__ __forceinline__ int64_t ld_stream(const int64_t *p) {
+  return __ldcs(reinterpret_cast<const long long *>(p));
+}
+// Streaming 16-byte store (evict-first): outputs are written once.
+__device__ __forceinline__ void st_stream_v2(longlong2 *p, longlong2 v) { __stcs(p, v); }
+__device__ __forceinline__ void st_stream(int64_t *p, int64_t v) {
+  __stcs(reinterpret_cast<long long *>(p), static_cast<long long>(v));
+}
+// Read-only random 8-byte load: non-coherent path, no L1 allocation (a
+// random table entry is never reused by the same SM soon enough).
+__device__ __forceinline__ int64_t ld_table(const int64_t *p) {
+  int64_t v;
+  asm("ld.global.nc.L1::no_allocate.s64 %0, [%1];" : "=l"(v) : "l"(p));
+  return v;
+}
+// Fire-and-forget 64-bit add performed at L2 (no return value).
+__device__ __forceinline__ void red_add_u64(int64_t *p, unsigned long long v) {
+  asm volatile("red.global.relaxed.gpu.add.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
+__device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+#endif
+
+}  // namespace bale

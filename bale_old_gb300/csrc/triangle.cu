@@ -1,0 +1,195 @@
+// triangle.cu -- exact triangle count of a strictly lower-triangular CSR L:
+//   count = sum over nonzeros L[i][j] of |row_i(L) and row_j(L)|
+// (apps/triangle_src/triangle_agi.upc:69-99, alg 0).  Every element w of
+// row j is < j, and row i is ascending, so each triangle k < j < i is found
+// exactly once: when row j's element k is matched inside row i.
+//
+// GPU layout of the work ("pull" form of the reference's AGI variant):
+//  * a warp owns a row i at a time, fetched dynamically in small groups of
+//    rows from a device cursor (row work is very uneven on skewed graphs);
+//  * row i is staged in the warp's slice of shared memory (as u32 when the
+//    matrix has < 2^32 rows), so each probe costs shared-memory loads only;
+//  * the neighbours j of row i are taken 32 at a time; a warp prefix sum over
+//    their row lengths flattens the concatenation of those rows so that
+//    consecutive lanes read consecutive elements of row j (coalesced), and
+//    each lane binary-searches its element in the prefix of row i that lies
+//    before j;
+//  * counts accumulate per lane in u64, then one atomic per warp.
+// The first element of row i is skipped as in the reference (it has no
+// smaller partner in row i).  Inputs are validated on the fly: a malformed
+// row offset, a column outside [0,i) or a non-ascending row is counted in
+// *bad and skipped, so no access ever leaves the arrays.
+#include "common.cuh"
+
+namespace bale {
+
+namespace {
+
+constexpr int kTriThreads = 256;
+constexpr int kTriWarps = kTriThreads / 32;
+constexpr int kTriCap = 1024;      // row-i elements cached per warp
+constexpr int kRowsPerFetch = 16;  // rows claimed per cursor increment
+constexpr unsigned kFull = 0xffffffffu;
+
+// Is w in the ascending u32 run rs[0,len) (shared memory)?
+__device__ __forceinline__ bool probe_smem(const uint32_t *__restrict__ rs, int64_t len, int64_t w) {
+  if (w < 0 || w > 0xffffffffll) return false;
+  const uint32_t ww = static_cast<uint32_t>(w);
+  int64_t lo = 0, hi = len;
+  while (lo < hi) {
+    const int64_t mid = (lo + hi) >> 1;
+    if (rs[mid] < ww) lo = mid + 1; else hi = mid;
+  }
+  return lo < len && rs[lo] == ww;
+}
+
+// Is w in the ascending int64 run rg[0,len) (global memory)?
+__device__ __forceinline__ bool probe_global(const int64_t *__restrict__ rg, int64_t len, int64_t w) {
+  int64_t lo = 0, hi = len;
+  while (lo < hi) {
+    const int64_t mid = (lo + hi) >> 1;
+    if (rg[mid] < w) lo = mid + 1; else hi = mid;
+  }
+  return lo < len && rg[lo] == w;
+}
+
+template <bool U32>
+__global__ void __launch_bounds__(kTriThreads)
+    tri_rows_kernel(const int64_t *__restrict__ off, const int64_t *__restrict__ col, int64_t n,
+                    int64_t nnz, unsigned long long *__restrict__ count,
+                    unsigned long long *__restrict__ work, unsigned long long *__restrict__ bad,
+                    unsigned long long *__restrict__ cursor) {
+  __shared__ uint32_t rowbuf[kTriWarps][kTriCap];
+  const unsigned lane = lane_id();
+  uint32_t *rb = rowbuf[threadIdx.x >> 5];
+  unsigned long long cnt = 0, wk = 0, nbad = 0;
+
+  for (;;) {
+    unsigned long long r0 = 0;
+    if (lane == 0) r0 = atomicAdd(cursor, static_cast<unsigned long long>(kRowsPerFetch));
+    r0 = __shfl_sync(kFull, r0, 0);
+    if (r0 >= static_cast<unsigned long long>(n)) break;
+    const int64_t r1 = static_cast<int64_t>(r0) + kRowsPerFetch < n ? static_cast<int64_t>(r0) + kRowsPerFetch : n;
+
+    for (int64_t i = static_cast<int64_t>(r0); i < r1; i++) {
+      const int64_t b = off[i], e = off[i + 1];
+      if (b < 0 || e < b || e > nnz) {
+        if (lane == 0) nbad++;
+        continue;
+      }
+      const int64_t d = e - b;
+      if (d < 2) {
+        if (d == 1 && lane == 0) {
+          const int64_t c = col[b];
+          if (c < 0 || c >= i) nbad++;
+        }
+        continue;
+      }
+      const bool cached = U32 && d <= kTriCap;
+      // Stage (when it fits) and validate row i: columns in [0,i), ascending.
+      bool ok = true;
+      for (int64_t k = lane; k < d; k += 32) {
+        const int64_t c = col[b + k];
+        ok &= (c >= 0 && c < i);
+        if (k > 0) ok &= c > col[b + k - 1];
+        if (cached) rb[k] = static_cast<uint32_t>(c);
+      }
+      __syncwarp();
+      if (!__all_sync(kFull, ok)) {
+        if (lane == 0) nbad++;
+        __syncwarp();
+        continue;
+      }
+      const int64_t *__restrict__ rg = col + b;
+
+      for (int64_t q0 = 1; q0 < d; q0 += 32) {
+        const int64_t q = q0 + lane;
+        int64_t jb = 0, jl = 0;
+        if (q < d) {
+          const int64_t j = cached ? static_cast<int64_t>(rb[q]) : rg[q];
+          const int64_t s = off[j], t = off[j + 1];
+          if (s < 0 || t < s || t > nnz) nbad++;
+          else { jb = s; jl = t - s; }
+        }
+        int64_t inc = jl;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const int64_t y = __shfl_up_sync(kFull, inc, o);
+          if (static_cast<int>(lane) >= o) inc += y;
+        }
+        const int64_t total = __shfl_sync(kFull, inc, 31);
+        if (lane == 0) wk += static_cast<unsigned long long>(total);
+        for (int64_t base = 0; base < total; base += 32) {
+          const int64_t kk = base + lane;
+          // owner lane: the first lane whose inclusive prefix exceeds kk
+          int lo = 0, hi = 31;
+#pragma unroll
+          for (int s = 0; s < 5; s++) {
+            const int mid = (lo + hi) >> 1;
+            const int64_t v = __shfl_sync(kFull, inc, mid);
+            if (v > kk) hi = mid; else lo = mid + 1;
+          }
+          const int o = lo < 31 ? lo : 31;
+          const int64_t o_inc = __shfl_sync(kFull, inc, o);
+          const int64_t o_jl = __shfl_sync(kFull, jl, o);
+          const int64_t o_jb = __shfl_sync(kFull, jb, o);
+          if (kk < total) {
+            const int64_t w = col[o_jb + (kk - (o_inc - o_jl))];
+            const bool hit = cached ? probe_smem(rb, q0 + o, w) : probe_global(rg, q0 + o, w);
+            cnt += hit ? 1ull : 0ull;
+          }
+        }
+      }
+      __syncwarp();  // rb is rewritten by the next row
+    }
+  }
+  cnt = warp_sum_u64(cnt);
+  wk = warp_sum_u64(wk);
+  nbad = warp_sum_u64(nbad);
+  if (lane == 0) {
+    if (cnt) atomicAdd(count, cnt);
+    if (wk && work) atomicAdd(work, wk);
+    if (nbad) atomicAdd(bad, nbad);
+  }
+}
+
+int g_tri_blocks_per_sm[2][64] = {{0}, {0}};
+
+}  // namespace
+
+int launch_triangle(const int64_t *offset, const int64_t *nonzero, int64_t numrows, int64_t nnz,
+                    unsigned long long *count, unsigned long long *work, unsigned long long *bad,
+                    cudaStream_t stream) {
+  if (numrows <= 0) return BALE_OK;
+  DeviceScratch *ds = device_scratch();
+  if (!ds) return BALE_ECUDA;
+  // Each launch takes its own cursor word from a ring so that launches on
+  // different streams do not share one.
+  static unsigned long long ring = 0;
+  const int slot = 8 + static_cast<int>(__atomic_fetch_add(&ring, 1ull, __ATOMIC_RELAXED) % (kScratchWords - 8));
+  unsigned long long *cursor = ds->words + slot;
+  BALE_CUDA_OK(cudaMemsetAsync(cursor, 0, sizeof(unsigned long long), stream));
+
+  const bool u32 = numrows <= 0xffffffffll;
+  const int dev = current_device();
+  int &bps = g_tri_blocks_per_sm[u32 ? 1 : 0][dev >= 0 && dev < 64 ? dev : 0];
+  if (bps == 0) {
+    cudaError_t e = u32 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, tri_rows_kernel<true>, kTriThreads, 0)
+                        : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, tri_rows_kernel<false>, kTriThreads, 0);
+    if (e != cudaSuccess || bps < 1) bps = 1;
+  }
+  int64_t blocks = static_cast<int64_t>(num_sms()) * bps;
+  int64_t need = (numrows + kRowsPerFetch - 1) / kRowsPerFetch;
+  need = (need + kTriWarps - 1) / kTriWarps;
+  if (blocks > need) blocks = need > 0 ? need : 1;
+  if (u32)
+    tri_rows_kernel<true><<<static_cast<int>(blocks), kTriThreads, 0, stream>>>(
+        offset, nonzero, numrows, nnz, count, work, bad, cursor);
+  else
+    tri_rows_kernel<false><<<static_cast<int>(blocks), kTriThreads, 0, stream>>>(
+        offset, nonzero, numrows, nnz, count, work, bad, cursor);
+  BALE_CUDA_OK(cudaGetLastError());
+  return BALE_OK;
+}
+
+}  // namespace bale

@@ -1,0 +1,141 @@
+/*
+ * bale_gb300.h -- C ABI of the GB300 (sm_103a) implementation of bale's
+ * irregular-access core: histogram scatter-add (histo), index gather (ig)
+ * and triangle counting on a strictly lower-triangular CSR (triangles).
+ *
+ * Two layers are exported from libbale_gb300.so:
+ *
+ *  1. Drop-ins with the reference's exact signatures.  An app that links this
+ *     library instead of the reference kernels runs on one GPU unchanged.
+ *     All pointers are HOST pointers (the reference's SHMEM build has
+ *     SHARED == empty, libgetput/libgetput.h:151), the call is synchronous
+ *     and returns the wall time in seconds of the whole call (copies
+ *     included), like the reference's lgp_min_avg_max_d(...)->avg.
+ *     -1.0 means failure (bad input or CUDA error), the reference's own
+ *     failure return (apps/histo_src/histo_exstack.upc:58).  The message of
+ *     the last failure is available from bale_last_error().
+ *     Ownership follows the reference: the caller owns every array; histo
+ *     ADDS into counts, ig OVERWRITES tgt, triangles write *count and *sr.
+ *
+ *  2. Device-resident entry points (bale_*_dev): device pointers, explicit
+ *     sizes, a CUDA stream passed as void*, asynchronous.  Used for resident
+ *     tables, batching and serving.
+ *
+ * Every index/offset is int64_t as in the reference.  Inputs are checked on
+ * the device: an index outside its table, a column outside [0,row) or a
+ * malformed row offset is skipped (ig writes 0 for it), counted, and reported
+ * as BALE_EINPUT / -1.0 -- never an out-of-bounds access.
+ */
+#ifndef BALE_GB300_H
+#define BALE_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------------ */
+/* sparsemat_t: layout-identical to the reference (spmat/spmat.h:73-86).     */
+/* With one PE, loffset/lnonzero are a plain CSR: int64[numrows+1] row       */
+/* offsets and int64[nnz] column indices (pattern only, no values).          */
+/* ------------------------------------------------------------------------ */
+#ifndef spmat_INCLUDED
+typedef struct sparsemat_t {
+  int64_t local;     /* 0/1: local or distributed matrix */
+  int64_t numrows;   /* total rows */
+  int64_t lnumrows;  /* rows on this PE (== numrows with one PE) */
+  int64_t numcols;   /* columns are in [0, numcols) */
+  int64_t nnz;       /* total nonzeros */
+  int64_t lnnz;      /* nonzeros on this PE */
+  int64_t *offset;   /* global row offsets (== loffset with one PE) */
+  int64_t *loffset;  /* row offsets, int64[lnumrows+1] */
+  int64_t *nonzero;  /* global nonzeros (== lnonzero with one PE) */
+  int64_t *lnonzero; /* column indices, int64[lnnz], ascending per row */
+} sparsemat_t;
+#endif
+
+/* Status codes of the bale_* entry points. */
+enum {
+  BALE_OK = 0,
+  BALE_EINVAL = 1,    /* bad argument (negative size, NULL pointer, ...) */
+  BALE_EINPUT = 2,    /* input data out of range (index >= table, bad CSR) */
+  BALE_ECUDA = 3,     /* a CUDA runtime call failed */
+  BALE_ENOMEM = 4,    /* device or pinned allocation failed */
+  BALE_ETIMEDOUT = 5, /* a bounded device-side wait gave up */
+  BALE_EBUSY = 6      /* admission refused: not enough free device memory */
+};
+
+/* ======================= drop-ins: histogram ============================ */
+/* apps/histo_src/histo.h:47 -- counts[index[i]] += 1 for i < len.          */
+double histo_agi(int64_t *index, int64_t len, int64_t *counts);
+/* apps/histo_src/histo.h:48 -- pckindx[i] = (lindex << 16) | pe; with one  */
+/* PE, lcounts[pckindx[i] >> 16] += 1.  buf_cnt (exstack buffer size) is    */
+/* accepted and ignored: there is no message buffering on one GPU.          */
+double histo_exstack(int64_t *pckindx, int64_t len, int64_t *lcounts, int64_t buf_cnt);
+/* apps/histo_src/histo.h:49 -- same contract as histo_exstack.             */
+double histo_exstack2(int64_t *pckindx, int64_t len, int64_t *lcounts, int64_t buf_cnt);
+/* apps/histo_src/histo.h:50 -- same contract, without buf_cnt.             */
+double histo_conveyor(int64_t *pckindx, int64_t len, int64_t *lcounts);
+
+/* ======================= drop-ins: index gather ========================= */
+/* apps/ig_src/ig.h:49 -- tgt[i] = table[index[i]] for i < l_num_req.        */
+double ig_agi(int64_t *tgt, int64_t *index, int64_t l_num_req, int64_t *table);
+/* apps/ig_src/ig.h:50 -- tgt[i] = ltable[pckindx[i] >> 16] (one PE).       */
+double ig_exstack(int64_t *tgt, int64_t *pckindx, int64_t l_num_req, int64_t *ltable, int64_t buf_cnt);
+/* apps/ig_src/ig.h:51 -- same contract as ig_exstack.                     */
+double ig_exstack2(int64_t *tgt, int64_t *pckindx, int64_t l_num_req, int64_t *ltable, int64_t buf_cnt);
+/* apps/ig_src/ig.h:52 -- same contract, without buf_cnt.                   */
+double ig_conveyor(int64_t *tgt, int64_t *pckindx, int64_t l_num_req, int64_t *ltable);
+
+/* ======================= drop-ins: triangles ============================ */
+/* apps/triangle_src/triangle.h:50 -- *count = sum over nonzeros L[i][j] of  */
+/* |row_i(L) and row_j(L)| (each triangle once).  L must be strictly lower   */
+/* triangular with ascending columns per row.  alg 0 and alg 1 give the same */
+/* count; both are computed from L (U may be NULL).  *sr receives the number */
+/* of row-j elements examined on the device (not a parity field).            */
+double triangle_agi(int64_t *count, int64_t *sr, sparsemat_t *L, sparsemat_t *U, int64_t alg);
+/* apps/triangle_src/triangle.h:51 -- same contract; bufsiz ignored.        */
+double triangle_exstack_push(int64_t *count, int64_t *sr, sparsemat_t *L, sparsemat_t *U, int64_t alg, int64_t bufsiz);
+/* apps/triangle_src/triangle.h:53 -- same contract; bufsiz ignored.        */
+double triangle_exstack2_push(int64_t *count, int64_t *sr, sparsemat_t *L, sparsemat_t *U, int64_t alg, int64_t bufsiz);
+/* apps/triangle_src/triangle.h:54 -- same contract.                        */
+double triangle_convey_push(int64_t *count, int64_t *sr, sparsemat_t *L, sparsemat_t *U, int64_t alg);
+/* apps/triangle_src/triangle.h:61 (the ALTERNATE model) -- same contract.  */
+double triangle_agi_iter(int64_t *count, int64_t *sr, sparsemat_t *L, sparsemat_t *U, int64_t alg);
+
+/* ======================= library state ================================== */
+/* Message describing the most recent failure on the calling thread ("" if */
+/* none).  Replaces the reference's fprintf-and-exit error paths.          */
+const char *bale_last_error(void);
+/* Library version string. */
+const char *bale_version(void);
+/* Release the cached device and pinned buffers the drop-ins keep between  */
+/* calls (they are re-created on demand).                                  */
+void bale_release_buffers(void);
+
+/* ======================= device-resident entry points =================== */
+/* All pointers below are device pointers; stream is a cudaStream_t (NULL  */
+/* = the legacy default stream).  The calls are asynchronous; a nonzero     */
+/* return is an argument or launch error.  Data errors (out-of-range        */
+/* indices, malformed CSR) are counted into *d_bad (one int64 in device     */
+/* memory, may be NULL), which the kernels ADD to.                          */
+
+/* counts[index[i] >> shift] += 1 for i < n (shift is 0, or 16 for packed   */
+/* exstack indices).  Counters are int64, ncounts of them.                  */
+int bale_histo_dev(int64_t *d_counts, int64_t ncounts, const int64_t *d_index, int64_t n,
+                   int shift, int64_t *d_bad, void *stream);
+/* tgt[i] = table[index[i] >> shift] for i < n; out-of-range -> tgt[i] = 0. */
+int bale_ig_dev(int64_t *d_tgt, const int64_t *d_index, int64_t n, const int64_t *d_table,
+                int64_t table_len, int shift, int64_t *d_bad, void *stream);
+/* *d_count += triangle count of the strictly lower CSR (d_offset[n+1],     */
+/* d_nonzero[nnz]); *d_work (may be NULL) += row-j elements examined.       */
+int bale_triangle_dev(const int64_t *d_offset, const int64_t *d_nonzero, int64_t numrows,
+                      int64_t nnz, int64_t *d_count, int64_t *d_work, int64_t *d_bad,
+                      void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* BALE_GB300_H */

@@ -1,0 +1,225 @@
+/*
+ * bale_oracle.c -- CPU restatement of bale's histo / ig / triangles kernels.
+ *
+ * TEST INFRASTRUCTURE ONLY: the parity checker and the timed CPU baseline.
+ * The shipped GPU library never links, loads or calls this code.
+ * Each routine restates one reference routine at a single processing element
+ * (THREADS == 1, so the cyclic distribution index i -> (i / THREADS, i % THREADS)
+ * is the identity) and cites the reference file:line it follows.  Parity of
+ * this restatement with the reference itself is pinned by tests/golden/.
+ */
+#define _GNU_SOURCE
+#include "bale_oracle.h"
+
+#include <pthread.h>
+#include <stdlib.h>
+#include <string.h>
+#include <unistd.h>
+
+/* apps/histo_src/histo_agi.upc:61-66: lgp_atomic_add(counts, index[i], 1),
+ * which at one PE is shmem_long_add(&counts[index[i]], 1, 0)
+ * (libgetput/libgetput.upc:48-53). */
+void orc_histo_agi(const int64_t *index, int64_t n, int64_t *counts) {
+  for (int64_t i = 0; i < n; i++) counts[index[i]] += 1;
+}
+
+/* apps/histo_src/histo_exstack.upc:64-76: the owner PE (pckindx & 0xffff,
+ * always 0 here) pops col = pckindx >> 16 and does lcounts[col]++. */
+void orc_histo_exstack(const int64_t *pckindx, int64_t n, int64_t *lcounts) {
+  for (int64_t i = 0; i < n; i++) lcounts[pckindx[i] >> 16]++;
+}
+
+/* apps/ig_src/ig_agi.upc:61-64: tgt[i] = lgp_get_int64(table, index[i]). */
+void orc_ig_agi(int64_t *tgt, const int64_t *index, int64_t n, const int64_t *table) {
+  for (int64_t i = 0; i < n; i++) tgt[i] = table[index[i]];
+}
+
+/* apps/ig_src/ig_exstack.upc:69-94: request l_indx = pckindx >> 16 from PE
+ * pckindx & 0xffff, the owner answers ltable[l_indx], the requester retraces
+ * its requests in order.  With one PE the reply for request j is ltable[j's idx]. */
+void orc_ig_exstack(int64_t *tgt, const int64_t *pckindx, int64_t n, const int64_t *ltable) {
+  for (int64_t j = 0; j < n; j++) tgt[j] = ltable[pckindx[j] >> 16];
+}
+
+/* apps/triangle_src/triangle_agi.upc:69-99 (alg 0).  For each nonzero L[i][j]
+ * after the first of row i, walk row j and advance a cursor through row i
+ * (both rows ascending), counting equal columns.  pulled counts 2 offset
+ * reads per (i,j) and one read per row-j element, as the reference does. */
+static int64_t tri_agi_rows(const int64_t *off, const int64_t *col, int64_t r0, int64_t r1,
+                            int64_t *pulled) {
+  int64_t cnt = 0, np = 0;
+  for (int64_t i = r0; i < r1; i++) {
+    for (int64_t k = off[i] + 1; k < off[i + 1]; k++) {
+      int64_t j = col[k];
+      int64_t start = off[i];
+      int64_t kbegin = off[j], kend = off[j + 1];
+      np += 2;
+      for (int64_t kk = kbegin; kk < kend; kk++) {
+        int64_t w = col[kk];
+        np++;
+        for (int64_t ii = start; ii < off[i + 1]; ii++) {
+          if (w == col[ii]) { cnt++; start = ii + 1; break; }
+          if (w < col[ii]) { start = ii; break; }
+        }
+      }
+    }
+  }
+  if (pulled) *pulled += np;
+  return cnt;
+}
+
+int64_t orc_triangle_agi(const int64_t *offset, const int64_t *nonzero, int64_t numrows,
+                         int64_t *pulled) {
+  if (pulled) *pulled = 0;
+  return tri_agi_rows(offset, nonzero, 0, numrows, pulled);
+}
+
+/* apps/triangle_src/triangle_exstack.upc:108-133 (push side, alg 0): for each
+ * nonzero (i,j), every w in row i before the column j itself is pushed to
+ * the owner of row j; :61-82 (pop side): the owner scans row j, which is
+ * ascending, for w and stops at the first column >= w. */
+int64_t orc_triangle_exstack_push(const int64_t *offset, const int64_t *nonzero,
+                                  int64_t numrows, int64_t *pushed) {
+  int64_t cnt = 0, np = 0;
+  for (int64_t i = 0; i < numrows; i++) {
+    for (int64_t k = offset[i]; k < offset[i + 1]; k++) {
+      int64_t j = nonzero[k];
+      for (int64_t kk = offset[i]; kk < offset[i + 1]; kk++) {
+        int64_t w = nonzero[kk];
+        if (w == j) break;
+        np++;
+        for (int64_t t = offset[j]; t < offset[j + 1]; t++) {
+          if (w == nonzero[t]) { cnt++; break; }
+          if (w < nonzero[t]) break;
+        }
+      }
+    }
+  }
+  if (pushed) *pushed = np;
+  return cnt;
+}
+
+/* apps/triangle_src/triangle.upc:325-361: column counts by fetch-and-inc,
+ * then pulls = sum deg(i)*cc(i) and pushes = sum C(deg(i),2) for alg 0. */
+void orc_triangle_work(const int64_t *offset, const int64_t *nonzero, int64_t numrows,
+                       int64_t *pulls, int64_t *pushes) {
+  int64_t *cc = calloc((size_t)(numrows > 0 ? numrows : 1), sizeof(int64_t));
+  for (int64_t k = 0; k < offset[numrows]; k++) cc[nonzero[k]]++;
+  int64_t pl = 0, ps = 0;
+  for (int64_t i = 0; i < numrows; i++) {
+    int64_t deg = offset[i + 1] - offset[i];
+    pl += deg * cc[i];
+    ps += deg * (deg - 1) / 2;
+  }
+  free(cc);
+  *pulls = pl;
+  *pushes = ps;
+}
+
+/* spmat/spmat_utils.upc:377-409 (is_lower_triangular, unit_diagonal = 0)
+ * tightened to STRICTLY lower, plus ascending columns within each row
+ * (the "tidy" property the merge scans need) and consistent offsets. */
+int orc_is_strict_lower_tidy(const int64_t *offset, const int64_t *nonzero, int64_t numrows) {
+  if (offset[0] != 0) return 0;
+  for (int64_t i = 0; i < numrows; i++) {
+    if (offset[i + 1] < offset[i]) return 0;
+    for (int64_t k = offset[i]; k < offset[i + 1]; k++) {
+      if (nonzero[k] < 0 || nonzero[k] >= i) return 0;
+      if (k > offset[i] && nonzero[k] <= nonzero[k - 1]) return 0;
+    }
+  }
+  return 1;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Multi-threaded variants (CPU baseline).                                   */
+/* ------------------------------------------------------------------------ */
+int orc_num_cpus(void) {
+  cpu_set_t set;
+  if (sched_getaffinity(0, sizeof(set), &set) == 0) {
+    int c = CPU_COUNT(&set);
+    if (c > 0) return c;
+  }
+  long n = sysconf(_SC_NPROCESSORS_ONLN);
+  return n > 0 ? (int)n : 1;
+}
+
+typedef struct {
+  int kind;
+  int64_t lo, hi;
+  const int64_t *a;
+  const int64_t *b;
+  int64_t *out;
+  int64_t result;
+  int64_t *next_row; /* shared cursor for dynamic row scheduling */
+  int64_t numrows;
+} orc_job_t;
+
+enum { JOB_HISTO = 0, JOB_IG = 1, JOB_TRI = 2 };
+
+static void *orc_worker(void *p) {
+  orc_job_t *job = (orc_job_t *)p;
+  if (job->kind == JOB_HISTO) {
+    for (int64_t i = job->lo; i < job->hi; i++)
+      __atomic_fetch_add(&job->out[job->a[i]], 1, __ATOMIC_RELAXED);
+  } else if (job->kind == JOB_IG) {
+    for (int64_t i = job->lo; i < job->hi; i++) job->out[i] = job->b[job->a[i]];
+  } else {
+    const int64_t chunk = 256;
+    int64_t cnt = 0;
+    for (;;) {
+      int64_t r0 = __atomic_fetch_add(job->next_row, chunk, __ATOMIC_RELAXED);
+      if (r0 >= job->numrows) break;
+      int64_t r1 = r0 + chunk < job->numrows ? r0 + chunk : job->numrows;
+      cnt += tri_agi_rows(job->a, job->b, r0, r1, NULL);
+    }
+    job->result = cnt;
+  }
+  return NULL;
+}
+
+static int64_t orc_run(int kind, int nthreads, int64_t n, const int64_t *a, const int64_t *b,
+                       int64_t *out) {
+  if (nthreads <= 0) nthreads = orc_num_cpus();
+  if (nthreads > 256) nthreads = 256;
+  pthread_t th[256];
+  orc_job_t jobs[256];
+  int64_t next_row = 0;
+  for (int t = 0; t < nthreads; t++) {
+    jobs[t].kind = kind;
+    jobs[t].lo = n * t / nthreads;
+    jobs[t].hi = n * (t + 1) / nthreads;
+    jobs[t].a = a;
+    jobs[t].b = b;
+    jobs[t].out = out;
+    jobs[t].result = 0;
+    jobs[t].next_row = &next_row;
+    jobs[t].numrows = n;
+  }
+  int started = 0;
+  for (int t = 1; t < nthreads; t++) {
+    if (pthread_create(&th[t], NULL, orc_worker, &jobs[t]) != 0) break;
+    started = t;
+  }
+  /* threads that failed to start: their ranges run on the calling thread */
+  for (int t = started + 1; t < nthreads; t++) orc_worker(&jobs[t]);
+  orc_worker(&jobs[0]);
+  for (int t = 1; t <= started; t++) pthread_join(th[t], NULL);
+  int64_t total = 0;
+  for (int t = 0; t < nthreads; t++) total += jobs[t].result;
+  return total;
+}
+
+void orc_histo_agi_mt(const int64_t *index, int64_t n, int64_t *counts, int nthreads) {
+  orc_run(JOB_HISTO, nthreads, n, index, NULL, counts);
+}
+
+void orc_ig_agi_mt(int64_t *tgt, const int64_t *index, int64_t n, const int64_t *table,
+                   int nthreads) {
+  orc_run(JOB_IG, nthreads, n, index, table, tgt);
+}
+
+int64_t orc_triangle_agi_mt(const int64_t *offset, const int64_t *nonzero, int64_t numrows,
+                            int nthreads) {
+  return orc_run(JOB_TRI, nthreads, numrows, offset, nonzero, NULL);
+}

@@ -1,0 +1,59 @@
+/*
+ * bale_oracle.h -- CPU restatement of bale's histo / ig / triangles kernels.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This is the parity checker for the GPU library
+ * and the source of the timed CPU baseline; nothing in the shipped library
+ * links or calls it.  Every function restates one reference routine at one
+ * processing element (THREADS == 1) and cites the file:line it follows.
+ * The restatement is pinned against the reference itself (oracle/_ref,
+ * compiled from the reference's unmodified sources) through the golden
+ * vectors in tests/golden/.
+ *
+ * The *_mt variants split the same loops over host threads (pthreads) for
+ * the multi-core CPU baseline; their results are identical to the serial
+ * ones (integer sums are order-free).
+ */
+#ifndef BALE_ORACLE_H
+#define BALE_ORACLE_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* histo: counts[index[i]] += 1 (apps/histo_src/histo_agi.upc:61-66). */
+void orc_histo_agi(const int64_t *index, int64_t n, int64_t *counts);
+/* histo, packed indices: lcounts[pckindx[i] >> 16]++ (apps/histo_src/histo_exstack.upc:64-76). */
+void orc_histo_exstack(const int64_t *pckindx, int64_t n, int64_t *lcounts);
+/* ig: tgt[i] = table[index[i]] (apps/ig_src/ig_agi.upc:61-64). */
+void orc_ig_agi(int64_t *tgt, const int64_t *index, int64_t n, const int64_t *table);
+/* ig, packed request/response: tgt[j] = ltable[pckindx[j] >> 16] (apps/ig_src/ig_exstack.upc:69-94). */
+void orc_ig_exstack(int64_t *tgt, const int64_t *pckindx, int64_t n, const int64_t *ltable);
+
+/* triangles alg 0, AGI merge scan (apps/triangle_src/triangle_agi.upc:69-99).
+ * Returns the count; *pulled gets the reference's "shared refs" tally.      */
+int64_t orc_triangle_agi(const int64_t *offset, const int64_t *nonzero, int64_t numrows,
+                         int64_t *pulled);
+/* triangles alg 0, exstack push (apps/triangle_src/triangle_exstack.upc:61-82, :108-133).
+ * *pushed gets the number of wedge packages pushed.                          */
+int64_t orc_triangle_exstack_push(const int64_t *offset, const int64_t *nonzero,
+                                  int64_t numrows, int64_t *pushed);
+/* Work model printed by the reference app (apps/triangle_src/triangle.upc:325-361):
+ * pulls = sum_i deg(i) * colcount(i), pushes = sum_i C(deg(i), 2).            */
+void orc_triangle_work(const int64_t *offset, const int64_t *nonzero, int64_t numrows,
+                       int64_t *pulls, int64_t *pushes);
+/* Structural check of L (spmat/spmat_utils.upc:377-409 with unit_diagonal 0,
+ * plus the tidiness the kernels rely on): 1 if strictly lower and sorted.   */
+int orc_is_strict_lower_tidy(const int64_t *offset, const int64_t *nonzero, int64_t numrows);
+
+/* Multi-threaded variants for the CPU baseline (nthreads <= 0: all cores). */
+void orc_histo_agi_mt(const int64_t *index, int64_t n, int64_t *counts, int nthreads);
+void orc_ig_agi_mt(int64_t *tgt, const int64_t *index, int64_t n, const int64_t *table, int nthreads);
+int64_t orc_triangle_agi_mt(const int64_t *offset, const int64_t *nonzero, int64_t numrows,
+                            int nthreads);
+int orc_num_cpus(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,186 @@
+"""ctypes access to the parity checker -- TEST INFRASTRUCTURE ONLY.
+
+Two libraries, both built by oracle/Makefile:
+
+* ``_build/liboracle.so`` -- the C restatement in bale_oracle.c (always
+  buildable: plain gcc, no reference tree needed).  Used by tests/ as the
+  checker and by bench.py as the timed CPU baseline.
+* ``_ref/libbale_ref.so`` -- the reference's own unmodified SHMEM-mode sources
+  compiled against the single-PE shim.  Only exists where the reference tree
+  is present; it pins the restatement (tests/golden/make_golden.py).
+
+Nothing in the shipped package imports this module.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+PORT_LIB = HERE / "_build" / "liboracle.so"
+REF_LIB = HERE / "_ref" / "libbale_ref.so"
+REF_TREE = Path(os.environ.get("BALE_REFERENCE_TREE", "/root/reference"))
+
+i64 = C.c_int64
+P64 = C.POINTER(C.c_int64)
+
+
+def _p(a: np.ndarray):
+    assert a.dtype == np.int64 and a.flags.c_contiguous
+    return a.ctypes.data_as(P64)
+
+
+def build_port() -> Path:
+    subprocess.run(["make", "-s", "-C", str(HERE), "port"], check=True)
+    return PORT_LIB
+
+
+def build_ref() -> Path | None:
+    """Compile the reference's sources into _ref/ when the tree is present."""
+    if not (REF_TREE / "apps" / "histo_src" / "histo_agi.upc").exists():
+        return None
+    subprocess.run(["make", "-s", "-C", str(HERE), "ref", f"REF={REF_TREE}"], check=True)
+    return REF_LIB
+
+
+class Oracle:
+    """The C restatement (bale_oracle.c)."""
+
+    def __init__(self, path: Path | None = None):
+        if path is None:
+            path = PORT_LIB if PORT_LIB.exists() else build_port()
+        lib = C.CDLL(str(path))
+        sig = {
+            "orc_histo_agi": (None, [P64, i64, P64]),
+            "orc_histo_exstack": (None, [P64, i64, P64]),
+            "orc_ig_agi": (None, [P64, P64, i64, P64]),
+            "orc_ig_exstack": (None, [P64, P64, i64, P64]),
+            "orc_triangle_agi": (i64, [P64, P64, i64, P64]),
+            "orc_triangle_exstack_push": (i64, [P64, P64, i64, P64]),
+            "orc_triangle_work": (None, [P64, P64, i64, P64, P64]),
+            "orc_is_strict_lower_tidy": (C.c_int, [P64, P64, i64]),
+            "orc_histo_agi_mt": (None, [P64, i64, P64, C.c_int]),
+            "orc_ig_agi_mt": (None, [P64, P64, i64, P64, C.c_int]),
+            "orc_triangle_agi_mt": (i64, [P64, P64, i64, C.c_int]),
+            "orc_num_cpus": (C.c_int, []),
+        }
+        for name, (res, args) in sig.items():
+            fn = getattr(lib, name)
+            fn.restype, fn.argtypes = res, args
+        self.lib = lib
+
+    # histo -----------------------------------------------------------------
+    def histo_agi(self, index: np.ndarray, counts: np.ndarray) -> None:
+        self.lib.orc_histo_agi(_p(index), index.size, _p(counts))
+
+    def histo_exstack(self, pckindx: np.ndarray, counts: np.ndarray) -> None:
+        self.lib.orc_histo_exstack(_p(pckindx), pckindx.size, _p(counts))
+
+    def histo_agi_mt(self, index: np.ndarray, counts: np.ndarray, nthreads: int = 0) -> None:
+        self.lib.orc_histo_agi_mt(_p(index), index.size, _p(counts), nthreads)
+
+    # ig --------------------------------------------------------------------
+    def ig_agi(self, index: np.ndarray, table: np.ndarray) -> np.ndarray:
+        tgt = np.empty(index.size, np.int64)
+        self.lib.orc_ig_agi(_p(tgt), _p(index), index.size, _p(table))
+        return tgt
+
+    def ig_exstack(self, pckindx: np.ndarray, table: np.ndarray) -> np.ndarray:
+        tgt = np.empty(pckindx.size, np.int64)
+        self.lib.orc_ig_exstack(_p(tgt), _p(pckindx), pckindx.size, _p(table))
+        return tgt
+
+    def ig_agi_mt(self, tgt: np.ndarray, index: np.ndarray, table: np.ndarray, nthreads: int = 0) -> None:
+        self.lib.orc_ig_agi_mt(_p(tgt), _p(index), index.size, _p(table), nthreads)
+
+    # triangles ---------------------------------------------------------------
+    def triangle_agi(self, offset: np.ndarray, nonzero: np.ndarray) -> tuple[int, int]:
+        pulled = C.c_int64(0)
+        c = self.lib.orc_triangle_agi(_p(offset), _p(nonzero), offset.size - 1, C.byref(pulled))
+        return int(c), int(pulled.value)
+
+    def triangle_exstack_push(self, offset: np.ndarray, nonzero: np.ndarray) -> tuple[int, int]:
+        pushed = C.c_int64(0)
+        c = self.lib.orc_triangle_exstack_push(_p(offset), _p(nonzero), offset.size - 1, C.byref(pushed))
+        return int(c), int(pushed.value)
+
+    def triangle_work(self, offset: np.ndarray, nonzero: np.ndarray) -> tuple[int, int]:
+        pl, ps = C.c_int64(0), C.c_int64(0)
+        self.lib.orc_triangle_work(_p(offset), _p(nonzero), offset.size - 1, C.byref(pl), C.byref(ps))
+        return int(pl.value), int(ps.value)
+
+    def is_strict_lower_tidy(self, offset: np.ndarray, nonzero: np.ndarray) -> bool:
+        return bool(self.lib.orc_is_strict_lower_tidy(_p(offset), _p(nonzero), offset.size - 1))
+
+    def triangle_agi_mt(self, offset: np.ndarray, nonzero: np.ndarray, nthreads: int = 0) -> int:
+        return int(self.lib.orc_triangle_agi_mt(_p(offset), _p(nonzero), offset.size - 1, nthreads))
+
+    def num_cpus(self) -> int:
+        return int(self.lib.orc_num_cpus())
+
+
+class _sparsemat_t(C.Structure):
+    _fields_ = [(n, i64) for n in ("local", "numrows", "lnumrows", "numcols", "nnz", "lnnz")] + [
+        (n, P64) for n in ("offset", "loffset", "nonzero", "lnonzero")]
+
+
+class Reference:
+    """The reference's own functions (oracle/_ref/libbale_ref.so), one PE."""
+
+    def __init__(self, path: Path | None = None):
+        path = path or REF_LIB
+        if not path.exists():
+            raise FileNotFoundError(f"{path} is not built (needs the reference tree)")
+        lib = C.CDLL(str(path))
+        PS = C.POINTER(_sparsemat_t)
+        sig = {
+            "histo_agi": (C.c_double, [P64, i64, P64]),
+            "histo_exstack": (C.c_double, [P64, i64, P64, i64]),
+            "histo_exstack2": (C.c_double, [P64, i64, P64, i64]),
+            "ig_agi": (C.c_double, [P64, P64, i64, P64]),
+            "ig_exstack": (C.c_double, [P64, P64, i64, P64, i64]),
+            "ig_exstack2": (C.c_double, [P64, P64, i64, P64, i64]),
+            "triangle_agi": (C.c_double, [P64, P64, PS, PS, i64]),
+            "triangle_exstack_push": (C.c_double, [P64, P64, PS, PS, i64, i64]),
+            "triangle_exstack2_push": (C.c_double, [P64, P64, PS, PS, i64, i64]),
+            "triangle_agi_iter": (C.c_double, [P64, P64, PS, PS, i64]),
+            "gen_erdos_renyi_graph_dist": (PS, [C.c_int, C.c_double, i64, i64, i64]),
+            "clear_matrix": (None, [PS]),
+        }
+        for name, (res, args) in sig.items():
+            fn = getattr(lib, name)
+            fn.restype, fn.argtypes = res, args
+        self.lib = lib
+        self._PS = PS
+
+    def _mat(self, offset: np.ndarray, nonzero: np.ndarray):
+        n = offset.size - 1
+        po, pn = _p(offset), _p(nonzero)
+        return _sparsemat_t(0, n, n, n, nonzero.size, nonzero.size, po, po, pn, pn)
+
+    def triangles(self, offset: np.ndarray, nonzero: np.ndarray) -> dict[str, tuple[int, int]]:
+        """count and shared-refs/pushes of every variant the oracle build has."""
+        m = self._mat(offset, nonzero)
+        out = {}
+        for name, extra in (("triangle_agi", ()), ("triangle_exstack_push", (1024,)),
+                            ("triangle_exstack2_push", (1024,)), ("triangle_agi_iter", ())):
+            cnt, sr = C.c_int64(0), C.c_int64(0)
+            t = getattr(self.lib, name)(C.byref(cnt), C.byref(sr), C.byref(m), None, 0, *extra)
+            if t < 0:
+                raise RuntimeError(f"reference {name} failed")
+            out[name] = (int(cnt.value), int(sr.value))
+        return out
+
+    def erdos_renyi_lower(self, n: int, p: float, seed: int) -> tuple[np.ndarray, np.ndarray]:
+        """spmat's gen_erdos_renyi_graph_dist(n, p, 0, mode 1 = lower, seed)
+        (spmat/spmat_utils.upc:554-573) at one PE."""
+        m = self.lib.gen_erdos_renyi_graph_dist(n, p, 0, 1, seed)
+        s = m.contents
+        off = np.ctypeslib.as_array(s.loffset, shape=(s.lnumrows + 1,)).copy()
+        col = np.ctypeslib.as_array(s.lnonzero, shape=(s.lnnz,)).copy() if s.lnnz else np.zeros(0, np.int64)
+        self.lib.clear_matrix(m)
+        return off, col

@@ -1,0 +1,135 @@
+"""Regenerate the golden vectors in tests/golden/ from the reference itself.
+
+    python tests/golden/make_golden.py
+
+Compiles the reference's own unmodified histo / ig / triangles / spmat sources
+against the single-PE shim (oracle/Makefile target ``ref``, reads the
+reference tree, writes only oracle/_ref/) and records, for small seeded
+inputs, what the reference returns:
+
+* histo.npz      -- counts after histo_agi, then histo_exstack, then
+                    histo_exstack2 add into the same array (the reference app
+                    accumulates across models, apps/histo_src/histo.upc:161-213);
+* ig.npz         -- tgt from ig_agi, and whether ig_exstack and ig_exstack2
+                    returned the same vector;
+* triangles.npz  -- count and shared-refs/pushes of triangle_agi,
+                    triangle_exstack_push, triangle_exstack2_push and the
+                    alternate triangle_agi_iter on Kronecker graphs (closed-form
+                    answers), the reference's own Erdos-Renyi graph, and R-MAT
+                    graphs from this package's generator.
+
+The inputs are stored next to the outputs, so the fixtures need neither the
+reference nor the generators to be checked.
+"""
+from __future__ import annotations
+
+import sys
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parents[2]
+sys.path.insert(0, str(ROOT))
+
+import bale_old_gb300 as bale  # noqa: E402  (inputs only)
+from oracle.pyoracle import Reference, build_ref  # noqa: E402
+
+OUT = Path(__file__).resolve().parent
+
+
+def _p(a):
+    import ctypes as C
+    return a.ctypes.data_as(C.POINTER(C.c_int64))
+
+
+def make_histo(ref: Reference) -> dict:
+    cases = {}
+    # (name, num updates, table size, generator)
+    specs = [
+        ("uniform", 20_000, 5_000, lambda n, t: bale.gen_uniform(n, t, 11), True),
+        ("zipf_small_table", 20_000, 64, lambda n, t: bale.gen_zipf(n, t, 1.1, 21, 22), True),
+        ("uniform_big_table", 10_000, 100_000, lambda n, t: bale.gen_uniform(n, t, 31), False),
+        ("ragged_odd", 1_001, 997, lambda n, t: bale.gen_uniform(n, t, 41), True),
+    ]
+    for name, n, t, gen, nonzero_start in specs:
+        index = np.ascontiguousarray(gen(n, t))
+        pck = bale.pack_index(index)
+        # a non-zero start checks that the drop-ins ADD into counts
+        counts0 = bale.gen_uniform(t, 1000, 12) if nonzero_start else np.zeros(t, np.int64)
+        c = counts0.copy()
+        assert ref.lib.histo_agi(_p(index), n, _p(c)) >= 0
+        after_agi = c.copy()
+        assert ref.lib.histo_exstack(_p(pck), n, _p(c), 1024) >= 0
+        after_exstack = c.copy()
+        assert ref.lib.histo_exstack2(_p(pck), n, _p(c), 1024) >= 0
+        after_exstack2 = c.copy()
+        cases.update({f"{name}/index": index, f"{name}/counts0": counts0,
+                      f"{name}/after_agi": after_agi, f"{name}/after_exstack": after_exstack,
+                      f"{name}/after_exstack2": after_exstack2})
+    return cases
+
+
+def make_ig(ref: Reference) -> dict:
+    cases = {}
+    specs = [
+        ("uniform", 20_000, 4_096, lambda n, t: bale.gen_uniform(n, t, 14), lambda t: bale.gen_values(t, 13)),
+        ("negative_table", 10_000, 3_000, lambda n, t: bale.gen_uniform(n, t, 15), bale.gen_negative_table),
+        ("zipf", 10_000, 10_000, lambda n, t: bale.gen_zipf(n, t, 1.1, 16, 17), lambda t: bale.gen_values(t, 18)),
+        ("ragged_odd", 999, 1_001, lambda n, t: bale.gen_uniform(n, t, 19), lambda t: bale.gen_values(t, 20)),
+    ]
+    for name, n, t, gidx, gtab in specs:
+        index = np.ascontiguousarray(gidx(n, t))
+        pck = bale.pack_index(index)
+        table = np.ascontiguousarray(gtab(t))
+        outs = {}
+        for fn, arg, extra in (("ig_agi", index, ()), ("ig_exstack", pck, (1024,)), ("ig_exstack2", pck, (1024,))):
+            tgt = np.zeros(n, np.int64)
+            assert getattr(ref.lib, fn)(_p(tgt), _p(arg), n, _p(table), *extra) >= 0
+            outs[fn] = tgt
+        # the three reference variants agree; store one vector and the agreement
+        same = [bool(np.array_equal(outs["ig_agi"], outs[k])) for k in ("ig_exstack", "ig_exstack2")]
+        cases.update({f"{name}/index": index, f"{name}/table": table, f"{name}/tgt": outs["ig_agi"],
+                      f"{name}/exstack_variants_agree": np.array(same)})
+    return cases
+
+
+def make_triangles(ref: Reference) -> dict:
+    cases = {}
+    graphs = []
+    for mode, specs in ((1, [3, 4, 5, 9]), (2, [3, 4, 5, 9, 2]), (0, [3, 4, 5, 9]), (1, [2, 2, 3])):
+        L = bale.gen_kronecker(mode, specs)
+        tag = "kron" + str(mode) + "_" + "_".join(map(str, specs))
+        graphs.append((tag, L.offset, L.nonzero, bale.kronecker_triangles(mode, specs)))
+    off, col = ref.erdos_renyi_lower(3000, 24.0 / 3000, 12345)
+    graphs.append(("ref_erdos_renyi_3000", off, col, -1))
+    for scale, seed in ((9, 6), (10, 1006)):
+        L = bale.gen_rmat(scale, 16, 0.57, 0.19, 0.19, seed)
+        graphs.append((f"rmat{scale}", L.offset, L.nonzero, -1))
+    names = []
+    for tag, off, col, closed in graphs:
+        res = ref.triangles(off, col)
+        names.append(tag)
+        cases[f"{tag}/offset"] = off
+        cases[f"{tag}/nonzero"] = col
+        cases[f"{tag}/closed_form"] = np.array([closed], np.int64)
+        for k, (cnt, sr) in res.items():
+            cases[f"{tag}/{k}"] = np.array([cnt, sr], np.int64)
+    cases["graphs"] = np.array(names)
+    return cases
+
+
+def main() -> int:
+    if build_ref() is None:
+        print("reference tree not found; cannot regenerate golden vectors", file=sys.stderr)
+        return 1
+    ref = Reference()
+    np.savez_compressed(OUT / "histo.npz", **make_histo(ref))
+    np.savez_compressed(OUT / "ig.npz", **make_ig(ref))
+    np.savez_compressed(OUT / "triangles.npz", **make_triangles(ref))
+    for f in ("histo.npz", "ig.npz", "triangles.npz"):
+        print(f, (OUT / f).stat().st_size, "bytes")
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

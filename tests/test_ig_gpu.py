@@ -1,0 +1,98 @@
+"""Index gather on the GPU, through the C ABI, bit-exact against the oracle
+and the reference's golden vectors."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+DROPINS_PACKED = ("ig_exstack", "ig_exstack2", "ig_conveyor")
+
+
+def test_golden_vectors_all_dropins(cuda, bale, golden):
+    d = golden("ig")
+    for name in sorted({k.split("/")[0] for k in d.files}):
+        index, table, want = d[f"{name}/index"], d[f"{name}/table"], d[f"{name}/tgt"]
+        tgt = np.full(index.size, 12345, np.int64)
+        bale.ig_agi(tgt, index, table)
+        np.testing.assert_array_equal(tgt, want, err_msg=name)
+        pck = bale.pack_index(index)
+        for fn in DROPINS_PACKED:
+            tgt[:] = 0
+            getattr(bale, fn)(tgt, pck, table)
+            np.testing.assert_array_equal(tgt, want, err_msg=f"{name}/{fn}")
+
+
+@pytest.mark.parametrize("n,tsize", [(0, 5), (1, 1), (2, 3), (3, 7), (31, 1000), (1000, 1),
+                                     (65_537, 4_096), ((1 << 20) + 3, 1 << 20), (1 << 21, 1 << 24)])
+def test_random_sizes_match_oracle(cuda, bale, oracle, n, tsize):
+    index = bale.gen_uniform(n, tsize, n + tsize) if n else np.zeros(0, np.int64)
+    table = bale.gen_values(tsize, 3 * tsize + 1)
+    tgt = np.zeros(n, np.int64)
+    bale.ig_agi(tgt, index, table)
+    np.testing.assert_array_equal(tgt, oracle.ig_agi(index, table))
+
+
+def test_zipf_and_negative_table_self_check(cuda, bale, oracle):
+    index = bale.gen_zipf(1 << 20, 1 << 22, 1.1, 4, 5)
+    table = bale.gen_negative_table(1 << 22)
+    tgt = np.zeros(index.size, np.int64)
+    bale.ig_agi(tgt, index, table)
+    np.testing.assert_array_equal(tgt, -(index + 1))  # apps/ig_src/ig.upc:96-114
+
+
+def test_unaligned_buffers_take_the_scalar_path(cuda, bale, oracle):
+    base = bale.gen_uniform(10_001, 5_000, 9)
+    index = base[1:]  # 8-byte but not 16-byte aligned
+    table = bale.gen_values(5_000, 10)
+    out = np.zeros(10_001, np.int64)
+    tgt = out[1:]
+    bale.ig_agi(tgt, index, table)
+    np.testing.assert_array_equal(tgt, oracle.ig_agi(np.ascontiguousarray(index), table))
+
+
+def test_out_of_range_index_is_an_error_not_a_fault(cuda, bale):
+    table = bale.gen_values(100, 1)
+    tgt = np.zeros(4, np.int64)
+    with pytest.raises(bale.BaleError):
+        bale.ig_agi(tgt, np.array([1, 2, -3, 4], np.int64), table)
+    # the library stays usable afterwards
+    bale.ig_agi(tgt, np.array([1, 2, 3, 4], np.int64), table)
+    np.testing.assert_array_equal(tgt, table[[1, 2, 3, 4]])
+
+
+def test_device_entry_point_counts_bad_indices(cuda, bale, oracle):
+    import torch
+
+    table_h = bale.gen_values(1000, 4)
+    index_h = bale.gen_uniform(5000, 1200, 5)  # some beyond the 1000-entry table
+    table, index = torch.from_numpy(table_h).to(cuda), torch.from_numpy(index_h).to(cuda)
+    tgt = torch.empty_like(index)
+    bad = torch.zeros(1, dtype=torch.int64, device=cuda)
+    bale.ig_dev(tgt, index, table, bad=bad)
+    torch.cuda.synchronize()
+    ok = index_h < 1000
+    assert int(bad.item()) == int((~ok).sum())
+    got = tgt.cpu().numpy()
+    np.testing.assert_array_equal(got[ok], table_h[index_h[ok]])
+    assert not got[~ok].any()
+
+
+def test_full_size_property_2e28_requests(cuda, bale):
+    """2^26-entry table, 2^28 requests: table[i] = -(i+1) makes every output
+    -(index+1), checked on the device (size-independent self-check)."""
+    import torch
+
+    tsize, n = 1 << 26, 1 << 28
+    table = -(torch.arange(tsize, dtype=torch.int64, device=cuda) + 1)
+    g = torch.Generator(device=cuda).manual_seed(3)
+    index = torch.randint(0, tsize, (n,), dtype=torch.int64, device=cuda, generator=g)
+    tgt = torch.empty_like(index)
+    bad = torch.zeros(1, dtype=torch.int64, device=cuda)
+    bale.ig_dev(tgt, index, table, bad=bad)
+    torch.cuda.synchronize()
+    assert int(bad.item()) == 0
+    assert bool(torch.equal(tgt, -(index + 1)))
+    del table, index, tgt
+    torch.cuda.empty_cache()

@@ -1,0 +1,150 @@
+"""The CPU oracle (oracle/bale_oracle.c) pinned against the reference.
+
+* against the golden vectors recorded from the reference's own compiled
+  sources (tests/golden/make_golden.py);
+* against the reference's built-in self-checks (known answers);
+* directly against oracle/_ref on fresh seeded inputs when that library is
+  present (it is only built where the reference tree exists).
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from oracle.pyoracle import REF_LIB, Reference
+
+
+def _cases(d, suffix):
+    return sorted({k.split("/")[0] for k in d.files if k.endswith(suffix)})
+
+
+def test_histo_matches_reference_golden(oracle, golden):
+    d = golden("histo")
+    for name in _cases(d, "/index"):
+        index = d[f"{name}/index"]
+        pck = (index << 16).astype(np.int64)
+        c = d[f"{name}/counts0"].copy()
+        oracle.histo_agi(index, c)
+        np.testing.assert_array_equal(c, d[f"{name}/after_agi"], err_msg=name)
+        oracle.histo_exstack(pck, c)
+        np.testing.assert_array_equal(c, d[f"{name}/after_exstack"], err_msg=name)
+        oracle.histo_exstack(pck, c)
+        np.testing.assert_array_equal(c, d[f"{name}/after_exstack2"], err_msg=name)
+
+
+def test_ig_matches_reference_golden(oracle, golden):
+    d = golden("ig")
+    for name in _cases(d, "/index"):
+        index, table = d[f"{name}/index"], d[f"{name}/table"]
+        np.testing.assert_array_equal(oracle.ig_agi(index, table), d[f"{name}/tgt"], err_msg=name)
+        pck = (index << 16).astype(np.int64)
+        np.testing.assert_array_equal(oracle.ig_exstack(pck, table), d[f"{name}/tgt"], err_msg=name)
+        assert d[f"{name}/exstack_variants_agree"].all()
+
+
+def test_triangles_match_reference_golden(oracle, golden):
+    d = golden("triangles")
+    for g in d["graphs"]:
+        off, col = d[f"{g}/offset"], d[f"{g}/nonzero"]
+        assert oracle.is_strict_lower_tidy(off, col), g
+        cnt, pulled = oracle.triangle_agi(off, col)
+        ref_cnt, ref_sr = d[f"{g}/triangle_agi"]
+        assert cnt == ref_cnt, g
+        assert pulled == ref_sr, g  # the AGI "shared refs" tally is pinned too
+        pc, pushed = oracle.triangle_exstack_push(off, col)
+        assert pc == d[f"{g}/triangle_exstack_push"][0], g
+        assert pushed == d[f"{g}/triangle_exstack_push"][1], g
+        for k in ("triangle_exstack2_push", "triangle_agi_iter"):
+            assert d[f"{g}/{k}"][0] == cnt, (g, k)
+        closed = int(d[f"{g}/closed_form"][0])
+        if closed >= 0:
+            assert cnt == closed, g
+
+
+def test_histo_self_check_known_answer(oracle, bale):
+    """apps/histo_src/histo.upc:208-227: after every model has added each
+    update once, subtracting num_models per update leaves all counters 0."""
+    index = bale.gen_uniform(50_000, 3_000, 99)
+    counts = np.zeros(3_000, np.int64)
+    num_models = 3
+    for _ in range(num_models):
+        oracle.histo_agi(index, counts)
+    np.subtract.at(counts, index, num_models)
+    assert not counts.any()
+
+
+def test_ig_self_check_known_answer(oracle, bale):
+    """apps/ig_src/ig.upc:96-114, :158-161: table[i] = -(i+1) makes every
+    gathered value -(index+1)."""
+    index = bale.gen_uniform(40_000, 5_000, 98)
+    tgt = oracle.ig_agi(index, bale.gen_negative_table(5_000))
+    np.testing.assert_array_equal(tgt, -(index + 1))
+
+
+@pytest.mark.parametrize("mode,specs", [(0, [3, 4, 5, 9]), (1, [3, 4, 5, 9]), (2, [3, 4, 5, 9, 2]),
+                                        (1, [1, 4, 9, 16]), (2, [2, 3, 4, 5])])
+def test_kronecker_closed_forms(oracle, bale, mode, specs):
+    """apps/triangle_src/triangle.upc:278-295 closed forms."""
+    L = bale.gen_kronecker(mode, specs)
+    cnt, _ = oracle.triangle_agi(L.offset, L.nonzero)
+    assert cnt == bale.kronecker_triangles(mode, specs)
+    assert oracle.triangle_exstack_push(L.offset, L.nonzero)[0] == cnt
+
+
+def test_work_model_matches_pulls(oracle, golden):
+    """triangle.upc:325-361: pulls = sum deg*colcount; the AGI tally adds two
+    offset reads per (i,j) after the first of each row."""
+    d = golden("triangles")
+    for g in d["graphs"]:
+        off, col = d[f"{g}/offset"], d[f"{g}/nonzero"]
+        pulls, pushes = oracle.triangle_work(off, col)
+        deg = np.diff(off)
+        assert pushes == int((deg * (deg - 1) // 2).sum())
+        _, pulled = oracle.triangle_agi(off, col)
+        first_skipped = int((deg > 0).sum())
+        # pulled = sum over (i,j) not first of (2 + deg(j))
+        rowid = np.repeat(np.arange(deg.size), deg)
+        not_first = np.ones(col.size, bool)
+        not_first[off[:-1][deg > 0]] = False
+        assert pulled == int((2 + deg[col[not_first]]).sum())
+        assert pulls == int(deg[col].sum())
+        assert first_skipped == int((deg > 0).sum()) and rowid.size == col.size
+
+
+def test_multithreaded_oracle_equals_serial(oracle, bale):
+    index = bale.gen_uniform(200_000, 10_000, 5)
+    a, b = np.zeros(10_000, np.int64), np.zeros(10_000, np.int64)
+    oracle.histo_agi(index, a)
+    oracle.histo_agi_mt(index, b, 4)
+    np.testing.assert_array_equal(a, b)
+    table = bale.gen_values(10_000, 6)
+    t = np.empty(index.size, np.int64)
+    oracle.ig_agi_mt(t, index, table, 4)
+    np.testing.assert_array_equal(t, oracle.ig_agi(index, table))
+    L = bale.gen_rmat(11, 16, 0.57, 0.19, 0.19, 7)
+    assert oracle.triangle_agi_mt(L.offset, L.nonzero, 4) == oracle.triangle_agi(L.offset, L.nonzero)[0]
+
+
+@pytest.mark.skipif(not REF_LIB.exists(), reason="reference library not built here")
+def test_oracle_equals_reference_on_fresh_inputs(oracle, bale):
+    ref = Reference()
+    import ctypes as C
+
+    P = lambda a: a.ctypes.data_as(C.POINTER(C.c_int64))  # noqa: E731
+    for seed in (101, 202):
+        index = bale.gen_uniform(30_000, 7_777, seed)
+        c1, c2 = np.zeros(7_777, np.int64), np.zeros(7_777, np.int64)
+        ref.lib.histo_agi(P(index), index.size, P(c1))
+        oracle.histo_agi(index, c2)
+        np.testing.assert_array_equal(c1, c2)
+        table = bale.gen_values(7_777, seed + 1)
+        t1 = np.zeros(index.size, np.int64)
+        ref.lib.ig_agi(P(t1), P(index), index.size, P(table))
+        np.testing.assert_array_equal(t1, oracle.ig_agi(index, table))
+    for scale, seed in ((11, 3), (12, 4)):
+        L = bale.gen_rmat(scale, 16, 0.57, 0.19, 0.19, seed)
+        r = ref.triangles(L.offset, L.nonzero)
+        assert oracle.triangle_agi(L.offset, L.nonzero) == r["triangle_agi"]
+        assert oracle.triangle_exstack_push(L.offset, L.nonzero) == r["triangle_exstack_push"]
+    off, col = ref.erdos_renyi_lower(5000, 20.0 / 5000, 777)
+    assert oracle.triangle_agi(off, col) == ref.triangles(off, col)["triangle_agi"]

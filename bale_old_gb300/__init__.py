@@ -30,6 +30,7 @@ __all__ = [
     "splitmix64", "gen_uniform", "gen_values", "gen_negative_table", "gen_zipf",
     "keyed_perm", "gen_rmat", "gen_erdos_renyi", "gen_kronecker", "kronecker_triangles",
     "set_host_threads", "release_buffers", "version", "pack_index",
+    "tune_set", "tune_get", "tune_knobs",
 ]
 
 _lib = load()
@@ -333,6 +334,24 @@ def gen_kronecker(mode: int, specs: Sequence[int]) -> SparseMatrix:
 def kronecker_triangles(mode: int, specs: Iterable[int]) -> int:
     arr = np.ascontiguousarray(np.asarray(list(specs), dtype=np.int64))
     return int(_lib.bale_kronecker_triangles(mode, _p(arr), arr.size))
+
+
+def tune_set(name: str, value: int) -> None:
+    """Pin a launch knob (e.g. "ig.unroll"); -1 returns it to automatic."""
+    if _lib.bale_tune_set(name.encode(), int(value)) != 0:
+        raise BaleError(_last_error())
+
+
+def tune_get(name: str) -> int:
+    v = int(_lib.bale_tune_get(name.encode()))
+    if v == -2:
+        raise BaleError(f"unknown tuning knob {name!r}")
+    return v
+
+
+def tune_knobs() -> dict[str, int]:
+    return {(_lib.bale_tune_name(i)).decode(): tune_get(_lib.bale_tune_name(i).decode())
+            for i in range(_lib.bale_tune_count())}
 
 
 def set_host_threads(n: int) -> None:

@@ -49,6 +49,11 @@ SIGNATURES: dict[str, tuple[object, list[object]]] = {
     "bale_last_error": (C.c_char_p, []),
     "bale_version": (C.c_char_p, []),
     "bale_release_buffers": (None, []),
+    # tuning knobs
+    "bale_tune_set": (C.c_int, [C.c_char_p, i64]),
+    "bale_tune_get": (i64, [C.c_char_p]),
+    "bale_tune_count": (C.c_int, []),
+    "bale_tune_name": (C.c_char_p, [C.c_int]),
     # device-resident
     "bale_histo_dev": (C.c_int, [VP, i64, VP, i64, C.c_int, VP, VP]),
     "bale_ig_dev": (C.c_int, [VP, VP, i64, VP, i64, C.c_int, VP, VP]),
@@ -79,7 +84,7 @@ def load() -> C.CDLL:
         return _lib
     if not LIB_PATH.exists():
         raise ImportError(
-            f"{LIB_PATH} is not built; run `python -m bale_old_gb300.build` "
+            f"{LIB_PATH} is not built; run `python bale_old_gb300/build.py` "
             "(or __graft_entry__.build())")
     lib = C.CDLL(str(LIB_PATH))
     for name, (res, args) in SIGNATURES.items():

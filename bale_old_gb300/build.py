@@ -1,7 +1,9 @@
 """Build recipe for libbale_gb300.so (CUDA for sm_103a + host C), in-tree.
 
-    python -m bale_old_gb300.build          # incremental
-    python -m bale_old_gb300.build --force  # rebuild everything
+    python bale_old_gb300/build.py          # incremental
+    python bale_old_gb300/build.py --force  # rebuild everything
+
+(run as a script: importing the package itself requires the built library)
 
 Every ``csrc/*.cu`` file is compiled by nvcc for sm_103a only, every
 ``csrc/host/*.c`` file by the host C compiler, in parallel, into
@@ -32,7 +34,7 @@ NVCC_FLAGS = ARCH + [
     "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
     "-I", str(INCLUDE), "-I", str(CSRC),
 ]
-CC_FLAGS = ["-O3", "-std=gnu11", "-fPIC", "-Wall", "-Wextra", "-ffp-contract=off",
+CC_FLAGS = ["-O3", "-std=gnu11", "-fPIC", "-fvisibility=hidden", "-Wall", "-Wextra", "-ffp-contract=off",
             "-I", str(INCLUDE)]
 
 
@@ -71,14 +73,11 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     deps = _headers()
     jobs: list[tuple[Path, list[str]]] = []
     objs: list[Path] = []
-    # The exported C ABI must stay visible although -fvisibility=hidden is on.
-    vis = ["-Xcompiler", "-fvisibility=default"]
     for src in sorted(CSRC.glob("*.cu")):
         obj = OBJDIR / (src.stem + ".o")
         objs.append(obj)
-        extra = vis if src.name in ("capi.cu",) or src.stem.startswith("api_") else []
         if force or _stale(obj, src, deps):
-            jobs.append((obj, [nvcc, *NVCC_FLAGS, *extra, "-c", str(src), "-o", str(obj)]))
+            jobs.append((obj, [nvcc, *NVCC_FLAGS, "-c", str(src), "-o", str(obj)]))
     for src in sorted((CSRC / "host").glob("*.c")):
         obj = OBJDIR / (src.stem + "_host.o")
         objs.append(obj)

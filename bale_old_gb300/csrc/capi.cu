@@ -72,6 +72,14 @@ DeviceScratch *device_scratch() {
   return &s;
 }
 
+unsigned long long *next_cursor_word() {
+  static unsigned long long ring = 0;
+  DeviceScratch *ds = device_scratch();
+  if (!ds) return nullptr;
+  const int slot = 8 + static_cast<int>(__atomic_fetch_add(&ring, 1ull, __ATOMIC_RELAXED) % (kScratchWords - 8));
+  return ds->words + slot;
+}
+
 // Scratch word layout used by the synchronous drop-ins (serialised by
 // g_dropin_mu): [0] bad-input count, [1] index max, [2] triangle count,
 // [3] triangle work.  [7] absorbs bad counts the caller does not want.
@@ -111,6 +119,17 @@ struct DropinState {
 
 static std::mutex g_dropin_mu;
 static DropinState g_state[64];
+
+static std::mutex g_ws_mu;
+static DevBuf g_ws[64];
+
+void *device_workspace(size_t bytes) {
+  int d = current_device();
+  if (d < 0 || d >= 64) return nullptr;
+  std::lock_guard<std::mutex> lk(g_ws_mu);
+  if (g_ws[d].ensure(bytes) != BALE_OK) return nullptr;
+  return g_ws[d].p;
+}
 
 static DropinState *dropin_state() {
   int d = current_device();
@@ -342,6 +361,8 @@ void bale_release_buffers(void) {
   std::lock_guard<std::mutex> lk(g_dropin_mu);
   for (int d = 0; d < 64; d++)
     for (auto &b : g_state[d].buf) b.release();
+  std::lock_guard<std::mutex> lk2(g_ws_mu);
+  for (int d = 0; d < 64; d++) g_ws[d].release();
 }
 
 int bale_histo_dev(int64_t *d_counts, int64_t ncounts, const int64_t *d_index, int64_t n, int shift,

@@ -18,6 +18,9 @@ int num_sms();
 // Current device ordinal (cached per call site use).
 int current_device();
 
+// Value of a named tuning knob (tune.cu); -1 means "launcher decides".
+int64_t knob(const char *name);
+
 // Device-wide scratch words owned by the library (per device): the in-kernel
 // bad-input counter and the triangle work cursor.  Allocated once.
 struct DeviceScratch {
@@ -25,6 +28,14 @@ struct DeviceScratch {
 };
 constexpr int kScratchWords = 1024;
 DeviceScratch *device_scratch();
+// A fresh scratch word for a launch's work cursor (ring of kScratchWords - 8
+// words per device; the caller zeroes it on its stream before use).
+unsigned long long *next_cursor_word();
+// Grow-only per-device workspace for kernels that need scratch memory.  The
+// drop-ins and the device entry points share it, so launches that use it
+// must not overlap on different streams.  Returns nullptr (error set) on
+// allocation failure.
+void *device_workspace(size_t bytes);
 
 #define BALE_CUDA_OK(expr)                                                        \
   do {                                                                            \
@@ -44,6 +55,12 @@ int launch_histo(int64_t *counts, int64_t ncounts, const int64_t *index, int64_t
 int launch_triangle(const int64_t *offset, const int64_t *nonzero, int64_t numrows, int64_t nnz,
                     unsigned long long *count, unsigned long long *work,
                     unsigned long long *bad, cudaStream_t stream);
+// Region-partitioned gather for tables larger than L2 (ig_part.cu).
+size_t ig_part_workspace_bytes(int64_t n, int64_t table_len);
+bool ig_part_supported(int64_t n, int64_t table_len);
+int launch_ig_partitioned(int64_t *tgt, const int64_t *index, int64_t n, const int64_t *table,
+                          int64_t table_len, int shift, unsigned long long *bad, void *ws,
+                          unsigned long long *cursor, cudaStream_t stream);
 // max over index[i] >> shift into *out (u64, must start at 0); negatives count as huge.
 int launch_index_max(const int64_t *index, int64_t n, int shift, unsigned long long *out,
                      cudaStream_t stream);
@@ -72,6 +89,54 @@ __device__ __forceinline__ int64_t ld_table(const int64_t *p) {
   asm("ld.global.nc.L1::no_allocate.s64 %0, [%1];" : "=l"(v) : "l"(p));
   return v;
 }
+// L2 cache policies (createpolicy) and loads/stores that carry them.
+__device__ __forceinline__ uint64_t policy_evict_first() {
+  uint64_t pol;
+  asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+  return pol;
+}
+__device__ __forceinline__ uint64_t policy_evict_last() {
+  uint64_t pol;
+  asm("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol));
+  return pol;
+}
+__device__ __forceinline__ uint4 ld_v4_u32_pol(const uint4 *p, uint64_t pol) {
+  uint4 v;
+  asm("ld.global.nc.L1::no_allocate.L2::cache_hint.v4.u32 {%0,%1,%2,%3}, [%4], %5;"
+      : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w) : "l"(p), "l"(pol));
+  return v;
+}
+__device__ __forceinline__ longlong2 ld_v2_s64_pol(const longlong2 *p, uint64_t pol) {
+  longlong2 v;
+  asm("ld.global.nc.L1::no_allocate.L2::cache_hint.v2.s64 {%0,%1}, [%2], %3;"
+      : "=l"(v.x), "=l"(v.y) : "l"(p), "l"(pol));
+  return v;
+}
+__device__ __forceinline__ uint32_t ld_u32_pol(const uint32_t *p, uint64_t pol) {
+  uint32_t v;
+  asm("ld.global.nc.L1::no_allocate.L2::cache_hint.u32 %0, [%1], %2;" : "=r"(v) : "l"(p), "l"(pol));
+  return v;
+}
+__device__ __forceinline__ int64_t ld_s64_pol(const int64_t *p, uint64_t pol) {
+  int64_t v;
+  asm("ld.global.nc.L1::no_allocate.L2::cache_hint.s64 %0, [%1], %2;" : "=l"(v) : "l"(p), "l"(pol));
+  return v;
+}
+__device__ __forceinline__ void st_v4_u32_pol(uint4 *p, uint4 v, uint64_t pol) {
+  asm volatile("st.global.L2::cache_hint.v4.u32 [%0], {%1,%2,%3,%4}, %5;"
+               ::"l"(p), "r"(v.x), "r"(v.y), "r"(v.z), "r"(v.w), "l"(pol) : "memory");
+}
+__device__ __forceinline__ void st_v2_s64_pol(longlong2 *p, longlong2 v, uint64_t pol) {
+  asm volatile("st.global.L2::cache_hint.v2.s64 [%0], {%1,%2}, %3;"
+               ::"l"(p), "l"(v.x), "l"(v.y), "l"(pol) : "memory");
+}
+__device__ __forceinline__ void st_s64_pol(int64_t *p, int64_t v, uint64_t pol) {
+  asm volatile("st.global.L2::cache_hint.s64 [%0], %1, %2;" ::"l"(p), "l"(v), "l"(pol) : "memory");
+}
+__device__ __forceinline__ void st_u32_pol(uint32_t *p, uint32_t v, uint64_t pol) {
+  asm volatile("st.global.L2::cache_hint.u32 [%0], %1, %2;" ::"l"(p), "r"(v), "l"(pol) : "memory");
+}
+
 // Fire-and-forget 64-bit add performed at L2 (no return value).
 __device__ __forceinline__ void red_add_u64(int64_t *p, unsigned long long v) {
   asm volatile("red.global.relaxed.gpu.add.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");

@@ -1,0 +1,255 @@
+// ig_part.cu -- index gather for tables larger than L2, by region partitioning.
+//
+// A random 8-byte read of a table that does not fit in L2 costs far more
+// DRAM traffic than its 8 bytes: the line it lands in is fetched whole and
+// is almost never reused before eviction.  bale's exstack/conveyor variants
+// (apps/ig_src/ig_exstack.upc:69-94) solve the same problem across PEs by
+// sending each request to the PE that owns the table slice and shipping the
+// reply back.  Here the "PEs" are L2-sized regions of the table and the
+// exchange happens through HBM in three coalesced passes:
+//
+//  1. partition: each 1024-request chunk is counting-sorted in shared memory
+//     by region (region = 2^22 entries = 32 MiB).  Each request becomes one
+//     u32 (offset in its region << 10 | position in its chunk), written back
+//     grouped by region, plus the chunk's region boundaries (u16);
+//  2. gather: (region, chunk) segments are processed region-major, so at any
+//     time the whole GPU reads one region, which stays resident in L2; the
+//     table values are written next to their requests;
+//  3. unpermute: each chunk scatters its values to their positions in a
+//     shared-memory tile, which is stored to tgt with 16-byte stores.
+//
+// Per request that is ~46 bytes of streaming traffic (8 index + 4+4+4 entry
+// + 8+8 value + 8 output) and the table is read about once, instead of one
+// mostly wasted DRAM line per request.
+#include "common.cuh"
+
+namespace bale {
+
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kCBits = 10;
+constexpr int kChunk = 1 << kCBits;       // requests per chunk
+constexpr int kRBits = 32 - kCBits;       // log2(entries per region) = 22
+constexpr int kMaxRegions = 1024;         // tables up to 2^32 entries
+constexpr int kDescPerClaim = 8;          // (region, chunk) segments a warp claims at once
+
+// Exclusive scan of a[0,m) in shared memory, in place; a[m] = total.
+// m <= kThreads * 8.  Called by all threads of the block.
+__device__ void block_exclusive_scan(uint32_t *a, int m) {
+  __shared__ uint32_t warp_tot[kThreads / 32];
+  const int per = (m + kThreads - 1) / kThreads;
+  const int lo = threadIdx.x * per;
+  uint32_t sum = 0;
+  for (int i = 0; i < per; i++)
+    if (lo + i < m) sum += a[lo + i];
+  // inclusive warp scan of per-thread sums
+  uint32_t inc = sum;
+  const unsigned lane = lane_id();
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t y = __shfl_up_sync(0xffffffffu, inc, o);
+    if (static_cast<int>(lane) >= o) inc += y;
+  }
+  if (lane == 31) warp_tot[threadIdx.x >> 5] = inc;
+  __syncthreads();
+  uint32_t wbase = 0;
+  for (int w = 0; w < static_cast<int>(threadIdx.x >> 5); w++) wbase += warp_tot[w];
+  uint32_t run = wbase + inc - sum;  // exclusive prefix of this thread's slice
+  for (int i = 0; i < per; i++) {
+    if (lo + i < m) {
+      uint32_t v = a[lo + i];
+      a[lo + i] = run;
+      run += v;
+    }
+  }
+  if (threadIdx.x == kThreads - 1) a[m] = wbase + inc;
+  __syncthreads();
+}
+
+__global__ void __launch_bounds__(kThreads)
+    igp_partition_kernel(const int64_t *__restrict__ index, int64_t n, uint64_t tlen, int shift, int nreg,
+                         uint32_t *__restrict__ entries, uint16_t *__restrict__ starts) {
+  __shared__ uint32_t hist[kMaxRegions + 2];
+  __shared__ __align__(16) uint32_t stage[kChunk];  // read back as uint4
+  const int64_t c = blockIdx.x;
+  const int64_t base = c * kChunk;
+  const int len = static_cast<int>(n - base < kChunk ? n - base : kChunk);
+  const uint64_t pol = policy_evict_first();
+  for (int i = threadIdx.x; i < nreg + 2; i += kThreads) hist[i] = 0;
+  __syncthreads();
+
+  uint32_t key[4], reg[4], rank[4];
+  const longlong2 *src = reinterpret_cast<const longlong2 *>(index + base);
+#pragma unroll
+  for (int h = 0; h < 2; h++) {
+    const int e0 = 2 * (h * kThreads + threadIdx.x);
+    int64_t r[2] = {0, 0};
+    if (e0 + 1 < len) {
+      longlong2 v = ld_v2_s64_pol(src + h * kThreads + threadIdx.x, pol);
+      r[0] = v.x;
+      r[1] = v.y;
+    } else if (e0 < len) {
+      r[0] = index[base + e0];
+    }
+#pragma unroll
+    for (int j = 0; j < 2; j++) {
+      const int e = e0 + j, s = 2 * h + j;
+      if (e < len) {
+        const uint64_t k = static_cast<uint64_t>(r[j] >> shift);
+        const bool ok = k < tlen;
+        reg[s] = ok ? static_cast<uint32_t>(k >> kRBits) : static_cast<uint32_t>(nreg);
+        const uint32_t local = ok ? static_cast<uint32_t>(k & ((1u << kRBits) - 1)) : 0u;
+        key[s] = (local << kCBits) | static_cast<uint32_t>(e);
+        rank[s] = atomicAdd(&hist[reg[s]], 1u);
+      }
+    }
+  }
+  __syncthreads();
+  block_exclusive_scan(hist, nreg + 1);  // hist[b] = start of region b; hist[nreg+1] = len
+  uint16_t *st = starts + c * (nreg + 2);
+  for (int i = threadIdx.x; i < nreg + 2; i += kThreads) st[i] = static_cast<uint16_t>(hist[i]);
+#pragma unroll
+  for (int h = 0; h < 2; h++)
+#pragma unroll
+    for (int j = 0; j < 2; j++) {
+      const int e = 2 * (h * kThreads + threadIdx.x) + j, s = 2 * h + j;
+      if (e < len) stage[hist[reg[s]] + rank[s]] = key[s];
+    }
+  __syncthreads();
+  uint32_t *dst = entries + base;
+  if (len == kChunk) {
+    const uint4 v = reinterpret_cast<const uint4 *>(stage)[threadIdx.x];
+    st_v4_u32_pol(reinterpret_cast<uint4 *>(dst) + threadIdx.x, v, pol);
+  } else {
+    for (int i = threadIdx.x; i < len; i += kThreads) st_u32_pol(dst + i, stage[i], pol);
+  }
+}
+
+// Segment (region b, chunk c): entries[c*kChunk + s .. c*kChunk + e).
+__global__ void __launch_bounds__(kThreads)
+    igp_gather_kernel(const uint32_t *__restrict__ entries, const uint16_t *__restrict__ starts,
+                      int64_t nchunks, int nreg, const int64_t *__restrict__ table,
+                      int64_t *__restrict__ val, unsigned long long *__restrict__ cursor,
+                      unsigned long long *__restrict__ bad) {
+  const unsigned lane = lane_id();
+  const uint64_t ef = policy_evict_first();
+  const uint64_t el = policy_evict_last();
+  const int64_t total = static_cast<int64_t>(nreg + 1) * nchunks;
+  unsigned long long nbad = 0;
+  for (;;) {
+    unsigned long long d0 = 0;
+    if (lane == 0) d0 = atomicAdd(cursor, static_cast<unsigned long long>(kDescPerClaim));
+    d0 = __shfl_sync(0xffffffffu, d0, 0);
+    if (static_cast<int64_t>(d0) >= total) break;
+    for (int g = 0; g < kDescPerClaim; g++) {
+      const int64_t d = static_cast<int64_t>(d0) + g;
+      if (d >= total) break;
+      const int b = static_cast<int>(d / nchunks);
+      const int64_t c = d - static_cast<int64_t>(b) * nchunks;
+      const uint16_t *st = starts + c * (nreg + 2) + b;
+      const int s = st[0], e = st[1];
+      const uint32_t *ent = entries + c * kChunk;
+      int64_t *vo = val + c * kChunk;
+      if (b < nreg) {
+        const int64_t *reg = table + (static_cast<int64_t>(b) << kRBits);
+        for (int k = s + static_cast<int>(lane); k < e; k += 128) {
+          uint32_t kk[4];
+          int64_t v[4];
+#pragma unroll
+          for (int u = 0; u < 4; u++)
+            kk[u] = (k + 32 * u < e) ? ld_u32_pol(ent + k + 32 * u, ef) : 0u;
+#pragma unroll
+          for (int u = 0; u < 4; u++)
+            v[u] = (k + 32 * u < e) ? ld_s64_pol(reg + (kk[u] >> kCBits), el) : 0;
+#pragma unroll
+          for (int u = 0; u < 4; u++)
+            if (k + 32 * u < e) st_s64_pol(vo + k + 32 * u, v[u], ef);
+        }
+      } else {
+        for (int k = s + static_cast<int>(lane); k < e; k += 32) {
+          st_s64_pol(vo + k, 0, ef);  // out-of-range request: value 0, counted
+          nbad++;
+        }
+      }
+    }
+  }
+  nbad = warp_sum_u64(nbad);
+  if (lane == 0 && nbad) atomicAdd(bad, nbad);
+}
+
+__global__ void __launch_bounds__(kThreads)
+    igp_unpermute_kernel(const uint32_t *__restrict__ entries, const int64_t *__restrict__ val,
+                         int64_t *__restrict__ tgt, int64_t n) {
+  __shared__ __align__(16) int64_t tile[kChunk];
+  const int64_t base = static_cast<int64_t>(blockIdx.x) * kChunk;
+  const int len = static_cast<int>(n - base < kChunk ? n - base : kChunk);
+  const uint64_t ef = policy_evict_first();
+  if (len == kChunk) {
+    const uint4 e = ld_v4_u32_pol(reinterpret_cast<const uint4 *>(entries + base) + threadIdx.x, ef);
+    const longlong2 *vp = reinterpret_cast<const longlong2 *>(val + base) + 2 * threadIdx.x;
+    const longlong2 v0 = ld_v2_s64_pol(vp, ef), v1 = ld_v2_s64_pol(vp + 1, ef);
+    tile[e.x & (kChunk - 1)] = v0.x;
+    tile[e.y & (kChunk - 1)] = v0.y;
+    tile[e.z & (kChunk - 1)] = v1.x;
+    tile[e.w & (kChunk - 1)] = v1.y;
+  } else {
+    for (int i = threadIdx.x; i < len; i += kThreads)
+      tile[entries[base + i] & (kChunk - 1)] = val[base + i];
+  }
+  __syncthreads();
+  longlong2 *out = reinterpret_cast<longlong2 *>(tgt + base);
+  for (int p = threadIdx.x; 2 * p < len; p += kThreads) {
+    if (2 * p + 1 < len) st_stream_v2(out + p, make_longlong2(tile[2 * p], tile[2 * p + 1]));
+    else st_stream(tgt + base + 2 * p, tile[2 * p]);
+  }
+}
+
+}  // namespace
+
+size_t ig_part_workspace_bytes(int64_t n, int64_t table_len) {
+  const int64_t nchunks = (n + kChunk - 1) / kChunk;
+  const int64_t nreg = (table_len + (int64_t(1) << kRBits) - 1) >> kRBits;
+  size_t b = 0;
+  b += static_cast<size_t>(nchunks) * kChunk * sizeof(uint32_t);  // entries
+  b += static_cast<size_t>(nchunks) * kChunk * sizeof(int64_t);   // values
+  b += ((static_cast<size_t>(nchunks) * (nreg + 2) * sizeof(uint16_t)) + 255) & ~size_t(255);
+  return b;
+}
+
+bool ig_part_supported(int64_t n, int64_t table_len) {
+  return n > 0 && table_len > 0 && table_len <= (int64_t(kMaxRegions) << kRBits);
+}
+
+int launch_ig_partitioned(int64_t *tgt, const int64_t *index, int64_t n, const int64_t *table,
+                          int64_t table_len, int shift, unsigned long long *bad, void *ws,
+                          unsigned long long *cursor, cudaStream_t stream) {
+  const int64_t nchunks = (n + kChunk - 1) / kChunk;
+  const int nreg = static_cast<int>((table_len + (int64_t(1) << kRBits) - 1) >> kRBits);
+  char *p = static_cast<char *>(ws);
+  uint32_t *entries = reinterpret_cast<uint32_t *>(p);
+  p += static_cast<size_t>(nchunks) * kChunk * sizeof(uint32_t);
+  int64_t *val = reinterpret_cast<int64_t *>(p);
+  p += static_cast<size_t>(nchunks) * kChunk * sizeof(int64_t);
+  uint16_t *starts = reinterpret_cast<uint16_t *>(p);
+
+  BALE_CUDA_OK(cudaMemsetAsync(cursor, 0, sizeof(unsigned long long), stream));
+  igp_partition_kernel<<<static_cast<unsigned>(nchunks), kThreads, 0, stream>>>(
+      index, n, static_cast<uint64_t>(table_len), shift, nreg, entries, starts);
+  BALE_CUDA_OK(cudaGetLastError());
+  int occ = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, igp_gather_kernel, kThreads, 0) != cudaSuccess || occ < 1)
+    occ = 1;
+  int64_t blocks = static_cast<int64_t>(num_sms()) * occ;
+  const int64_t warps_needed = ((nreg + 1) * nchunks + kDescPerClaim - 1) / kDescPerClaim;
+  if (blocks * (kThreads / 32) > warps_needed) blocks = (warps_needed + (kThreads / 32) - 1) / (kThreads / 32);
+  if (blocks < 1) blocks = 1;
+  igp_gather_kernel<<<static_cast<unsigned>(blocks), kThreads, 0, stream>>>(entries, starts, nchunks, nreg,
+                                                                          table, val, cursor, bad);
+  BALE_CUDA_OK(cudaGetLastError());
+  igp_unpermute_kernel<<<static_cast<unsigned>(nchunks), kThreads, 0, stream>>>(entries, val, tgt, n);
+  BALE_CUDA_OK(cudaGetLastError());
+  return BALE_OK;
+}
+
+}  // namespace bale

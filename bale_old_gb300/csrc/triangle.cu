@@ -161,13 +161,10 @@ int launch_triangle(const int64_t *offset, const int64_t *nonzero, int64_t numro
                     unsigned long long *count, unsigned long long *work, unsigned long long *bad,
                     cudaStream_t stream) {
   if (numrows <= 0) return BALE_OK;
-  DeviceScratch *ds = device_scratch();
-  if (!ds) return BALE_ECUDA;
   // Each launch takes its own cursor word from a ring so that launches on
   // different streams do not share one.
-  static unsigned long long ring = 0;
-  const int slot = 8 + static_cast<int>(__atomic_fetch_add(&ring, 1ull, __ATOMIC_RELAXED) % (kScratchWords - 8));
-  unsigned long long *cursor = ds->words + slot;
+  unsigned long long *cursor = next_cursor_word();
+  if (!cursor) return BALE_ECUDA;
   BALE_CUDA_OK(cudaMemsetAsync(cursor, 0, sizeof(unsigned long long), stream));
 
   const bool u32 = numrows <= 0xffffffffll;

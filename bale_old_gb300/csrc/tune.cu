@@ -1,0 +1,76 @@
+// tune.cu -- named launch knobs shared by the kernels' launchers.
+//
+// Every knob defaults to -1 ("automatic": the launcher's own size-class
+// rule).  The autotuner (bale_old_gb300/autotune.py) measures the variants of
+// each kernel per size class and stores the winners; applications may also
+// pin a knob directly.  Knobs only select among variants that compute the
+// same result; none of them changes an output bit.
+#include <cstring>
+#include <mutex>
+
+#include "common.cuh"
+
+namespace bale {
+
+namespace {
+struct Knob {
+  const char *name;
+  int64_t value;
+};
+
+Knob g_knobs[] = {
+    {"ig.mode", -1},            // 0 direct gather, 1 region-partitioned gather
+    {"ig.unroll", -1},          // pairs of requests per thread per trip: 1, 2, 4, 8
+    {"ig.threads", -1},         // threads per block: 128, 256, 512
+    {"ig.blocks_per_sm", -1},   // resident blocks per SM to launch
+    {"ig.table_policy", -1},    // 0 L1::no_allocate, 1 L2 evict_last, 2 L2 evict_first, 3 cached
+    {"ig.l2_fetch", -1},        // cudaLimitMaxL2FetchGranularity in bytes (0..128)
+    {"histo.mode", -1},         // 0 shared-memory private, 1 warp-aggregated L2, 2 plain L2, 3 partitioned
+    {"histo.unroll", -1},       // pairs per thread per trip (L2 modes): 1, 2, 4, 8
+    {"histo.blocks_per_sm", -1},
+    {"histo.smem_updates_per_counter", -1},  // updates per counter per block (shared-memory mode)
+    {"tri.rows_per_fetch", -1}, // rows claimed per cursor increment
+    {"tri.mode", -1},           // 0 warp-per-row merge; further modes added by the kernels
+};
+std::mutex g_mu;
+}  // namespace
+
+int64_t knob(const char *name) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  for (auto &k : g_knobs)
+    if (std::strcmp(k.name, name) == 0) return k.value;
+  return -1;
+}
+
+}  // namespace bale
+
+extern "C" {
+
+int bale_tune_set(const char *name, int64_t value) {
+  if (!name) return BALE_EINVAL;
+  std::lock_guard<std::mutex> lk(bale::g_mu);
+  for (auto &k : bale::g_knobs)
+    if (std::strcmp(k.name, name) == 0) {
+      k.value = value;
+      return BALE_OK;
+    }
+  bale::set_error("unknown tuning knob '%s'", name);
+  return BALE_EINVAL;
+}
+
+int64_t bale_tune_get(const char *name) {
+  if (!name) return -2;
+  std::lock_guard<std::mutex> lk(bale::g_mu);
+  for (auto &k : bale::g_knobs)
+    if (std::strcmp(k.name, name) == 0) return k.value;
+  return -2;
+}
+
+int bale_tune_count(void) { return static_cast<int>(sizeof(bale::g_knobs) / sizeof(bale::g_knobs[0])); }
+
+const char *bale_tune_name(int i) {
+  if (i < 0 || i >= bale_tune_count()) return nullptr;
+  return bale::g_knobs[i].name;
+}
+
+}  // extern "C"

@@ -32,6 +32,12 @@
 #include <stddef.h>
 #include <stdint.h>
 
+#if defined(__GNUC__)
+#define BALE_API __attribute__((visibility("default")))
+#else
+#define BALE_API
+#endif
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -69,25 +75,25 @@ enum {
 
 /* ======================= drop-ins: histogram ============================ */
 /* apps/histo_src/histo.h:47 -- counts[index[i]] += 1 for i < len.          */
-double histo_agi(int64_t *index, int64_t len, int64_t *counts);
+BALE_API double histo_agi(int64_t *index, int64_t len, int64_t *counts);
 /* apps/histo_src/histo.h:48 -- pckindx[i] = (lindex << 16) | pe; with one  */
 /* PE, lcounts[pckindx[i] >> 16] += 1.  buf_cnt (exstack buffer size) is    */
 /* accepted and ignored: there is no message buffering on one GPU.          */
-double histo_exstack(int64_t *pckindx, int64_t len, int64_t *lcounts, int64_t buf_cnt);
+BALE_API double histo_exstack(int64_t *pckindx, int64_t len, int64_t *lcounts, int64_t buf_cnt);
 /* apps/histo_src/histo.h:49 -- same contract as histo_exstack.             */
-double histo_exstack2(int64_t *pckindx, int64_t len, int64_t *lcounts, int64_t buf_cnt);
+BALE_API double histo_exstack2(int64_t *pckindx, int64_t len, int64_t *lcounts, int64_t buf_cnt);
 /* apps/histo_src/histo.h:50 -- same contract, without buf_cnt.             */
-double histo_conveyor(int64_t *pckindx, int64_t len, int64_t *lcounts);
+BALE_API double histo_conveyor(int64_t *pckindx, int64_t len, int64_t *lcounts);
 
 /* ======================= drop-ins: index gather ========================= */
 /* apps/ig_src/ig.h:49 -- tgt[i] = table[index[i]] for i < l_num_req.        */
-double ig_agi(int64_t *tgt, int64_t *index, int64_t l_num_req, int64_t *table);
+BALE_API double ig_agi(int64_t *tgt, int64_t *index, int64_t l_num_req, int64_t *table);
 /* apps/ig_src/ig.h:50 -- tgt[i] = ltable[pckindx[i] >> 16] (one PE).       */
-double ig_exstack(int64_t *tgt, int64_t *pckindx, int64_t l_num_req, int64_t *ltable, int64_t buf_cnt);
+BALE_API double ig_exstack(int64_t *tgt, int64_t *pckindx, int64_t l_num_req, int64_t *ltable, int64_t buf_cnt);
 /* apps/ig_src/ig.h:51 -- same contract as ig_exstack.                     */
-double ig_exstack2(int64_t *tgt, int64_t *pckindx, int64_t l_num_req, int64_t *ltable, int64_t buf_cnt);
+BALE_API double ig_exstack2(int64_t *tgt, int64_t *pckindx, int64_t l_num_req, int64_t *ltable, int64_t buf_cnt);
 /* apps/ig_src/ig.h:52 -- same contract, without buf_cnt.                   */
-double ig_conveyor(int64_t *tgt, int64_t *pckindx, int64_t l_num_req, int64_t *ltable);
+BALE_API double ig_conveyor(int64_t *tgt, int64_t *pckindx, int64_t l_num_req, int64_t *ltable);
 
 /* ======================= drop-ins: triangles ============================ */
 /* apps/triangle_src/triangle.h:50 -- *count = sum over nonzeros L[i][j] of  */
@@ -95,25 +101,36 @@ double ig_conveyor(int64_t *tgt, int64_t *pckindx, int64_t l_num_req, int64_t *l
 /* triangular with ascending columns per row.  alg 0 and alg 1 give the same */
 /* count; both are computed from L (U may be NULL).  *sr receives the number */
 /* of row-j elements examined on the device (not a parity field).            */
-double triangle_agi(int64_t *count, int64_t *sr, sparsemat_t *L, sparsemat_t *U, int64_t alg);
+BALE_API double triangle_agi(int64_t *count, int64_t *sr, sparsemat_t *L, sparsemat_t *U, int64_t alg);
 /* apps/triangle_src/triangle.h:51 -- same contract; bufsiz ignored.        */
-double triangle_exstack_push(int64_t *count, int64_t *sr, sparsemat_t *L, sparsemat_t *U, int64_t alg, int64_t bufsiz);
+BALE_API double triangle_exstack_push(int64_t *count, int64_t *sr, sparsemat_t *L, sparsemat_t *U, int64_t alg, int64_t bufsiz);
 /* apps/triangle_src/triangle.h:53 -- same contract; bufsiz ignored.        */
-double triangle_exstack2_push(int64_t *count, int64_t *sr, sparsemat_t *L, sparsemat_t *U, int64_t alg, int64_t bufsiz);
+BALE_API double triangle_exstack2_push(int64_t *count, int64_t *sr, sparsemat_t *L, sparsemat_t *U, int64_t alg, int64_t bufsiz);
 /* apps/triangle_src/triangle.h:54 -- same contract.                        */
-double triangle_convey_push(int64_t *count, int64_t *sr, sparsemat_t *L, sparsemat_t *U, int64_t alg);
+BALE_API double triangle_convey_push(int64_t *count, int64_t *sr, sparsemat_t *L, sparsemat_t *U, int64_t alg);
 /* apps/triangle_src/triangle.h:61 (the ALTERNATE model) -- same contract.  */
-double triangle_agi_iter(int64_t *count, int64_t *sr, sparsemat_t *L, sparsemat_t *U, int64_t alg);
+BALE_API double triangle_agi_iter(int64_t *count, int64_t *sr, sparsemat_t *L, sparsemat_t *U, int64_t alg);
 
 /* ======================= library state ================================== */
 /* Message describing the most recent failure on the calling thread ("" if */
 /* none).  Replaces the reference's fprintf-and-exit error paths.          */
-const char *bale_last_error(void);
+BALE_API const char *bale_last_error(void);
 /* Library version string. */
-const char *bale_version(void);
+BALE_API const char *bale_version(void);
 /* Release the cached device and pinned buffers the drop-ins keep between  */
 /* calls (they are re-created on demand).                                  */
-void bale_release_buffers(void);
+BALE_API void bale_release_buffers(void);
+
+/* ======================= tuning knobs ==================================== */
+/* Named launch knobs (e.g. "ig.unroll", "histo.mode", "tri.rows_per_fetch")  */
+/* choose among kernel variants that compute identical results; -1 (the     */
+/* default) lets the launcher pick by size class.  The autotuner sets them.  */
+/* bale_tune_set returns BALE_EINVAL for an unknown name; bale_tune_get      */
+/* returns -2 for one.                                                       */
+BALE_API int bale_tune_set(const char *name, int64_t value);
+BALE_API int64_t bale_tune_get(const char *name);
+BALE_API int bale_tune_count(void);
+BALE_API const char *bale_tune_name(int i);
 
 /* ======================= device-resident entry points =================== */
 /* All pointers below are device pointers; stream is a cudaStream_t (NULL  */
@@ -124,14 +141,14 @@ void bale_release_buffers(void);
 
 /* counts[index[i] >> shift] += 1 for i < n (shift is 0, or 16 for packed   */
 /* exstack indices).  Counters are int64, ncounts of them.                  */
-int bale_histo_dev(int64_t *d_counts, int64_t ncounts, const int64_t *d_index, int64_t n,
+BALE_API int bale_histo_dev(int64_t *d_counts, int64_t ncounts, const int64_t *d_index, int64_t n,
                    int shift, int64_t *d_bad, void *stream);
 /* tgt[i] = table[index[i] >> shift] for i < n; out-of-range -> tgt[i] = 0. */
-int bale_ig_dev(int64_t *d_tgt, const int64_t *d_index, int64_t n, const int64_t *d_table,
+BALE_API int bale_ig_dev(int64_t *d_tgt, const int64_t *d_index, int64_t n, const int64_t *d_table,
                 int64_t table_len, int shift, int64_t *d_bad, void *stream);
 /* *d_count += triangle count of the strictly lower CSR (d_offset[n+1],     */
 /* d_nonzero[nnz]); *d_work (may be NULL) += row-j elements examined.       */
-int bale_triangle_dev(const int64_t *d_offset, const int64_t *d_nonzero, int64_t numrows,
+BALE_API int bale_triangle_dev(const int64_t *d_offset, const int64_t *d_nonzero, int64_t numrows,
                       int64_t nnz, int64_t *d_count, int64_t *d_work, int64_t *d_bad,
                       void *stream);
 

@@ -96,3 +96,48 @@ def test_full_size_property_2e28_requests(cuda, bale):
     assert bool(torch.equal(tgt, -(index + 1)))
     del table, index, tgt
     torch.cuda.empty_cache()
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+@pytest.mark.parametrize("n,tsize", [(1, 1), (1000, 7), (1024, 1 << 22), (1025, (1 << 22) + 1),
+                                     (5 * 1024 + 17, 3 * (1 << 22) + 5), (300_001, 1 << 24)])
+def test_both_gather_modes_match_oracle(cuda, bale, oracle, mode, n, tsize):
+    """ig.mode 0 (direct) and 1 (region-partitioned) give identical bits,
+    including partial chunks, partial regions and single-entry tables."""
+    bale.tune_set("ig.mode", mode)
+    try:
+        index = bale.gen_uniform(n, tsize, n ^ tsize)
+        table = bale.gen_values(tsize, tsize + 17)
+        tgt = np.zeros(n, np.int64)
+        bale.ig_agi(tgt, index, table)
+        np.testing.assert_array_equal(tgt, oracle.ig_agi(index, table))
+        pck = bale.pack_index(index)
+        tgt[:] = -1
+        bale.ig_exstack(tgt, pck, table)
+        np.testing.assert_array_equal(tgt, oracle.ig_agi(index, table))
+    finally:
+        bale.tune_set("ig.mode", -1)
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+def test_both_modes_count_bad_indices(cuda, bale, mode):
+    import torch
+
+    bale.tune_set("ig.mode", mode)
+    try:
+        tsize = (1 << 22) + 3
+        table_h = bale.gen_values(tsize, 8)
+        index_h = bale.gen_uniform(70_001, tsize + 5000, 9)
+        index_h[::1000] = -5
+        table, index = torch.from_numpy(table_h).to(cuda), torch.from_numpy(index_h).to(cuda)
+        tgt = torch.empty_like(index)
+        bad = torch.zeros(1, dtype=torch.int64, device=cuda)
+        bale.ig_dev(tgt, index, table, bad=bad)
+        torch.cuda.synchronize()
+        ok = (index_h >= 0) & (index_h < tsize)
+        assert int(bad.item()) == int((~ok).sum())
+        got = tgt.cpu().numpy()
+        np.testing.assert_array_equal(got[ok], table_h[index_h[ok]])
+        assert not got[~ok].any()
+    finally:
+        bale.tune_set("ig.mode", -1)

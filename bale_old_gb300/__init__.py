@@ -26,7 +26,7 @@ __all__ = [
     "ig_agi", "ig_exstack", "ig_exstack2", "ig_conveyor",
     "triangle_agi", "triangle_exstack_push", "triangle_exstack2_push",
     "triangle_convey_push", "triangle_agi_iter",
-    "histo_dev", "ig_dev", "triangle_dev",
+    "histo_dev", "ig_dev", "triangle_dev", "ig_dev_noalloc",
     "splitmix64", "gen_uniform", "gen_values", "gen_negative_table", "gen_zipf",
     "keyed_perm", "gen_rmat", "gen_erdos_renyi", "gen_kronecker", "kronecker_triangles",
     "set_host_threads", "release_buffers", "version", "pack_index",
@@ -263,6 +263,18 @@ def ig_dev(tgt, index, table, shift: int = 0, bad=None, stream=None, n: Optional
     _status(_lib.bale_ig_dev(_dptr(tgt, "tgt"), _dptr(index, "index"), nn, _dptr(table, "table"),
                              table.numel(), shift, _dptr(bad, "bad") if bad is not None else None,
                              _stream(stream)), "bale_ig_dev")
+
+
+def ig_dev_noalloc(tgt, index, table, shift: int = 0, bad=None, stream=None,
+                   n: Optional[int] = None) -> None:
+    """Same result as ig_dev, for callers that cannot allocate device memory:
+    the scratch is a fixed array inside the library (at most 262144 requests
+    per call; tgt and index 16-byte aligned).  Calls share that array, so
+    calls that overlap on the GPU must be serialised by the caller."""
+    nn = index.numel() if n is None else int(n)
+    _status(_lib.bale_ig_dev_noalloc(_dptr(tgt, "tgt"), _dptr(index, "index"), nn, _dptr(table, "table"),
+                                     table.numel(), shift, _dptr(bad, "bad") if bad is not None else None,
+                                     _stream(stream)), "bale_ig_dev_noalloc")
 
 
 def triangle_dev(offset, nonzero, count, work=None, bad=None, stream=None) -> None:

@@ -58,6 +58,7 @@ SIGNATURES: dict[str, tuple[object, list[object]]] = {
     "bale_histo_dev": (C.c_int, [VP, i64, VP, i64, C.c_int, VP, VP]),
     "bale_ig_dev": (C.c_int, [VP, VP, i64, VP, i64, C.c_int, VP, VP]),
     "bale_triangle_dev": (C.c_int, [VP, VP, i64, i64, VP, VP, VP, VP]),
+    "bale_ig_dev_noalloc": (C.c_int, [VP, VP, i64, VP, i64, C.c_int, VP, VP]),
     # inputs
     "bale_splitmix64": (u64, [u64, u64]),
     "bale_gen_uniform": (C.c_int, [P64, i64, i64, u64, C.c_int]),

@@ -152,6 +152,21 @@ BALE_API int bale_triangle_dev(const int64_t *d_offset, const int64_t *d_nonzero
                       int64_t nnz, int64_t *d_count, int64_t *d_work, int64_t *d_bad,
                       void *stream);
 
+/* ======================= no-allocation gather =========================== */
+/* No counterpart in the reference: an addition for callers that cannot      */
+/* allocate device memory when they call (HBM already reserved by another    */
+/* allocator, or a loop that cannot take cudaMalloc/cudaFree's implicit      */
+/* synchronisation).  Same result as bale_ig_dev, computed by the region-    */
+/* partitioned gather with its scratch in a fixed device array inside the    */
+/* library (about 3.6 MiB, held by every GPU that loads the library until    */
+/* exit).  Limits: n <= 262144 requests per call (larger n -> BALE_EINVAL     */
+/* with a message), table_len <= 2^32, d_index and d_tgt 16-byte aligned.    */
+/* The first call on a device looks up the array's address; make it before  */
+/* any stream capture.  All calls share the array: calls that overlap on the */
+/* GPU race and must be serialised by the caller.                            */
+BALE_API int bale_ig_dev_noalloc(int64_t *d_tgt, const int64_t *d_index, int64_t n, const int64_t *d_table,
+                                 int64_t table_len, int shift, int64_t *d_bad, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

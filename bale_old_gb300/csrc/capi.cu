@@ -72,12 +72,18 @@ DeviceScratch *device_scratch() {
   return &s;
 }
 
-unsigned long long *next_cursor_word() {
-  static unsigned long long ring = 0;
+static unsigned long long g_ring = 0;
+
+unsigned long long *next_cursor_word() { return next_cursor_words(1); }
+
+unsigned long long *next_cursor_words(int k) {
+  if (k < 1 || k > 4) return nullptr;
   DeviceScratch *ds = device_scratch();
   if (!ds) return nullptr;
-  const int slot = 8 + static_cast<int>(__atomic_fetch_add(&ring, 1ull, __ATOMIC_RELAXED) % (kScratchWords - 8));
-  return ds->words + slot;
+  // slots of 4 words starting at word 8
+  const int nslots = (kScratchWords - 8) / 4;
+  const int slot = static_cast<int>(__atomic_fetch_add(&g_ring, 1ull, __ATOMIC_RELAXED) % nslots);
+  return ds->words + 8 + 4 * slot;
 }
 
 // Scratch word layout used by the synchronous drop-ins (serialised by

@@ -31,6 +31,8 @@ DeviceScratch *device_scratch();
 // A fresh scratch word for a launch's work cursor (ring of kScratchWords - 8
 // words per device; the caller zeroes it on its stream before use).
 unsigned long long *next_cursor_word();
+// k (<= 4) consecutive fresh scratch words, same ring and rules.
+unsigned long long *next_cursor_words(int k);
 // Grow-only per-device workspace for kernels that need scratch memory.  The
 // drop-ins and the device entry points share it, so launches that use it
 // must not overlap on different streams.  Returns nullptr (error set) on
@@ -61,6 +63,11 @@ bool ig_part_supported(int64_t n, int64_t table_len);
 int launch_ig_partitioned(int64_t *tgt, const int64_t *index, int64_t n, const int64_t *table,
                           int64_t table_len, int shift, unsigned long long *bad, void *ws,
                           unsigned long long *cursor, cudaStream_t stream);
+// Bitmap/search hybrid triangle counting (tri_hybrid.cu); needs numrows < 2^32.
+size_t tri_hybrid_workspace_bytes(int64_t numrows, int64_t nnz);
+int launch_triangle_hybrid(const int64_t *offset, const int64_t *nonzero, int64_t numrows, int64_t nnz,
+                           unsigned long long *count, unsigned long long *work, unsigned long long *bad,
+                           void *ws, unsigned long long *words, int rows_per_fetch, cudaStream_t stream);
 // max over index[i] >> shift into *out (u64, must start at 0); negatives count as huge.
 int launch_index_max(const int64_t *index, int64_t n, int shift, unsigned long long *out,
                      cudaStream_t stream);

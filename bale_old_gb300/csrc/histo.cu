@@ -142,8 +142,15 @@ int launch_histo(int64_t *counts, int64_t ncounts, const int64_t *index, int64_t
   if (n <= 0) return BALE_OK;
   const int sms = num_sms();
   const bool aligned = (reinterpret_cast<uintptr_t>(index) & 15) == 0;
+  // Mode: 0 shared-memory private table, 1 warp-aggregated L2 reductions,
+  // 2 plain L2 reductions.  Automatic: shared memory when the table fits,
+  // aggregation while in-warp collisions are likely, plain above that.
+  int64_t mode = knob("histo.mode");
+  if (mode < 0 || mode > 2) mode = ncounts <= kSmemMaxCounters ? 0 : (ncounts <= (int64_t(1) << 20) ? 1 : 2);
+  if (mode == 0 && ncounts > kSmemMaxCounters) mode = 1;
+  if (!aligned && mode == 0) mode = 1;
 
-  if (ncounts <= kSmemMaxCounters && aligned) {
+  if (mode == 0) {
     const size_t smem = static_cast<size_t>(ncounts) * sizeof(uint32_t);
     const int dev = current_device();
     if (dev >= 0 && dev < 64 && !g_smem_attr_set[dev]) {
@@ -156,7 +163,9 @@ int launch_histo(int64_t *counts, int64_t ncounts, const int64_t *index, int64_t
     int per_sm = smem <= 48 * 1024 ? 4 : (smem <= 96 * 1024 ? 2 : 1);
     // Each block should see several updates per counter so that the flush
     // (ncounts reductions per block) stays a small share of the work.
-    int64_t blocks = n / (4 * (ncounts > 0 ? ncounts : 1));
+    int64_t upc = knob("histo.smem_updates_per_counter");
+    if (upc <= 0) upc = 4;
+    int64_t blocks = n / (upc * (ncounts > 0 ? ncounts : 1));
     int64_t cap = static_cast<int64_t>(sms) * per_sm;
     if (blocks > cap) blocks = cap;
     if (blocks < 1) blocks = 1;
@@ -174,19 +183,24 @@ int launch_histo(int64_t *counts, int64_t ncounts, const int64_t *index, int64_t
   }
 
   int64_t want = (n / 2 + kHistoThreads - 1) / kHistoThreads;
-  int64_t full = static_cast<int64_t>(sms) * 8;
+  int64_t bps = knob("histo.blocks_per_sm");
+  if (bps <= 0) bps = 8;
+  int64_t full = static_cast<int64_t>(sms) * bps;
   int blocks = static_cast<int>(want < full ? (want > 0 ? want : 1) : full);
+  int64_t unroll = knob("histo.unroll");
+  if (unroll != 1 && unroll != 2 && unroll != 4 && unroll != 8) unroll = 4;
+  using HistoKernel = void (*)(int64_t *, uint64_t, const int64_t *, int64_t, int, unsigned long long *);
+  HistoKernel k;
   if (!aligned) {
-    histo_scalar_kernel<<<blocks, kHistoThreads, 0, stream>>>(counts, static_cast<uint64_t>(ncounts),
-                                                             index, n, shift, bad);
-  } else if (ncounts <= (int64_t(1) << 20)) {
-    // Collisions inside a warp are likely enough to aggregate.
-    histo_global_kernel<4, true><<<blocks, kHistoThreads, 0, stream>>>(
-        counts, static_cast<uint64_t>(ncounts), index, n, shift, bad);
+    k = histo_scalar_kernel;
+  } else if (mode == 1) {
+    k = unroll == 1 ? histo_global_kernel<1, true> : unroll == 2 ? histo_global_kernel<2, true>
+      : unroll == 8 ? histo_global_kernel<8, true> : histo_global_kernel<4, true>;
   } else {
-    histo_global_kernel<4, false><<<blocks, kHistoThreads, 0, stream>>>(
-        counts, static_cast<uint64_t>(ncounts), index, n, shift, bad);
+    k = unroll == 1 ? histo_global_kernel<1, false> : unroll == 2 ? histo_global_kernel<2, false>
+      : unroll == 8 ? histo_global_kernel<8, false> : histo_global_kernel<4, false>;
   }
+  k<<<blocks, kHistoThreads, 0, stream>>>(counts, static_cast<uint64_t>(ncounts), index, n, shift, bad);
   BALE_CUDA_OK(cudaGetLastError());
   return BALE_OK;
 }

@@ -28,7 +28,7 @@ namespace {
 constexpr int kTriThreads = 256;
 constexpr int kTriWarps = kTriThreads / 32;
 constexpr int kTriCap = 1024;      // row-i elements cached per warp
-constexpr int kRowsPerFetch = 16;  // rows claimed per cursor increment
+constexpr int kRowsPerFetchDefault = 16;  // rows claimed per cursor increment
 constexpr unsigned kFull = 0xffffffffu;
 
 // Is w in the ascending u32 run rs[0,len) (shared memory)?
@@ -58,7 +58,7 @@ __global__ void __launch_bounds__(kTriThreads)
     tri_rows_kernel(const int64_t *__restrict__ off, const int64_t *__restrict__ col, int64_t n,
                     int64_t nnz, unsigned long long *__restrict__ count,
                     unsigned long long *__restrict__ work, unsigned long long *__restrict__ bad,
-                    unsigned long long *__restrict__ cursor) {
+                    unsigned long long *__restrict__ cursor, int rows_per_fetch) {
   __shared__ uint32_t rowbuf[kTriWarps][kTriCap];
   const unsigned lane = lane_id();
   uint32_t *rb = rowbuf[threadIdx.x >> 5];
@@ -66,10 +66,10 @@ __global__ void __launch_bounds__(kTriThreads)
 
   for (;;) {
     unsigned long long r0 = 0;
-    if (lane == 0) r0 = atomicAdd(cursor, static_cast<unsigned long long>(kRowsPerFetch));
+    if (lane == 0) r0 = atomicAdd(cursor, static_cast<unsigned long long>(rows_per_fetch));
     r0 = __shfl_sync(kFull, r0, 0);
     if (r0 >= static_cast<unsigned long long>(n)) break;
-    const int64_t r1 = static_cast<int64_t>(r0) + kRowsPerFetch < n ? static_cast<int64_t>(r0) + kRowsPerFetch : n;
+    const int64_t r1 = static_cast<int64_t>(r0) + rows_per_fetch < n ? static_cast<int64_t>(r0) + rows_per_fetch : n;
 
     for (int64_t i = static_cast<int64_t>(r0); i < r1; i++) {
       const int64_t b = off[i], e = off[i + 1];
@@ -161,6 +161,18 @@ int launch_triangle(const int64_t *offset, const int64_t *nonzero, int64_t numro
                     unsigned long long *count, unsigned long long *work, unsigned long long *bad,
                     cudaStream_t stream) {
   if (numrows <= 0) return BALE_OK;
+  // Default: the bitmap/search hybrid (tri_hybrid.cu); mode 0 keeps this
+  // file's warp-per-row merge kernel for every row.
+  const int64_t mode = knob("tri.mode");
+  if (mode != 0 && numrows < 0xffffffffll) {
+    int64_t rpf_h = knob("tri.rows_per_fetch");
+    if (rpf_h < 1 || rpf_h > 4096) rpf_h = 8;
+    void *ws = device_workspace(tri_hybrid_workspace_bytes(numrows, nnz));
+    unsigned long long *words = next_cursor_words(3);
+    if (!ws || !words) return BALE_ENOMEM;
+    return launch_triangle_hybrid(offset, nonzero, numrows, nnz, count, work, bad, ws, words,
+                                  static_cast<int>(rpf_h), stream);
+  }
   // Each launch takes its own cursor word from a ring so that launches on
   // different streams do not share one.
   unsigned long long *cursor = next_cursor_word();
@@ -176,15 +188,17 @@ int launch_triangle(const int64_t *offset, const int64_t *nonzero, int64_t numro
     if (e != cudaSuccess || bps < 1) bps = 1;
   }
   int64_t blocks = static_cast<int64_t>(num_sms()) * bps;
-  int64_t need = (numrows + kRowsPerFetch - 1) / kRowsPerFetch;
+  int64_t rpf = knob("tri.rows_per_fetch");
+  if (rpf < 1 || rpf > 4096) rpf = kRowsPerFetchDefault;
+  int64_t need = (numrows + rpf - 1) / rpf;
   need = (need + kTriWarps - 1) / kTriWarps;
   if (blocks > need) blocks = need > 0 ? need : 1;
   if (u32)
     tri_rows_kernel<true><<<static_cast<int>(blocks), kTriThreads, 0, stream>>>(
-        offset, nonzero, numrows, nnz, count, work, bad, cursor);
+        offset, nonzero, numrows, nnz, count, work, bad, cursor, static_cast<int>(rpf));
   else
     tri_rows_kernel<false><<<static_cast<int>(blocks), kTriThreads, 0, stream>>>(
-        offset, nonzero, numrows, nnz, count, work, bad, cursor);
+        offset, nonzero, numrows, nnz, count, work, bad, cursor, static_cast<int>(rpf));
   BALE_CUDA_OK(cudaGetLastError());
   return BALE_OK;
 }

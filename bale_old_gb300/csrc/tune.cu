@@ -30,7 +30,7 @@ Knob g_knobs[] = {
     {"histo.blocks_per_sm", -1},
     {"histo.smem_updates_per_counter", -1},  // updates per counter per block (shared-memory mode)
     {"tri.rows_per_fetch", -1}, // rows claimed per cursor increment
-    {"tri.mode", -1},           // 0 warp-per-row merge; further modes added by the kernels
+    {"tri.mode", -1},           // 0 warp-per-row merge for every row, 1 bitmap/search hybrid
 };
 std::mutex g_mu;
 }  // namespace

@@ -12,7 +12,15 @@ DROPINS = ("triangle_agi", "triangle_exstack_push", "triangle_exstack2_push",
            "triangle_convey_push", "triangle_agi_iter")
 
 
-def test_golden_graphs_all_dropins(cuda, bale, golden):
+@pytest.fixture(params=[0, 1], ids=["merge", "hybrid"])
+def mode(request, bale):
+    """tri.mode 0: warp-per-row merge for every row; 1: bitmap/search hybrid."""
+    bale.tune_set("tri.mode", request.param)
+    yield request.param
+    bale.tune_set("tri.mode", -1)
+
+
+def test_golden_graphs_all_dropins(cuda, bale, golden, mode):
     d = golden("triangles")
     for g in d["graphs"]:
         L = bale.SparseMatrix(d[f"{g}/offset"], d[f"{g}/nonzero"])
@@ -26,29 +34,34 @@ def test_golden_graphs_all_dropins(cuda, bale, golden):
             assert want == closed
 
 
-@pytest.mark.parametrize("mode,specs", [(1, [3, 4, 5, 9]), (2, [3, 4, 5, 9, 2]), (0, [5, 9, 4]),
-                                        (1, [1, 4, 9, 16, 25]), (1, [2000, 2]), (2, [1500, 3])])
-def test_kronecker_closed_forms_including_hub_rows(cuda, bale, mode, specs):
+@pytest.mark.parametrize("kmode,specs", [(1, [3, 4, 5, 9]), (2, [3, 4, 5, 9, 2]), (0, [5, 9, 4]),
+                                         (1, [1, 4, 9, 16, 25]), (1, [2000, 2]), (2, [1500, 3])])
+def test_kronecker_closed_forms_including_hub_rows(cuda, bale, kmode, specs, mode):
     """Star products have hub rows far longer than a warp's shared-memory slot."""
-    L = bale.gen_kronecker(mode, specs)
+    L = bale.gen_kronecker(kmode, specs)
     cnt, _, _ = bale.triangle_agi(L)
-    assert cnt == bale.kronecker_triangles(mode, specs)
+    assert cnt == bale.kronecker_triangles(kmode, specs)
 
 
 @pytest.mark.parametrize("scale", [6, 10, 14, 16])
-def test_rmat_matches_oracle(cuda, bale, oracle, scale):
+def test_rmat_matches_oracle(cuda, bale, oracle, scale, mode):
     L = bale.gen_rmat(scale, 16, 0.57, 0.19, 0.19, 100 + scale)
     cnt, sr, _ = bale.triangle_agi(L)
     assert cnt == oracle.triangle_agi_mt(L.offset, L.nonzero)
-    # the device tally is the number of row-j elements scanned: the pulls of
-    # every (i,j) except the first nonzero of each row
     deg = np.diff(L.offset)
     nf = np.ones(L.nnz, bool)
     nf[L.offset[:-1][deg > 0]] = False
-    assert sr == int(deg[L.nonzero[nf]].sum())
+    pulls = int(deg[L.nonzero[nf]].sum())
+    if mode == 0:
+        # the merge kernel scans every row-j element: the reference's pulls
+        # for every (i,j) except the first nonzero of each row
+        assert sr == pulls
+    else:
+        # the hybrid streams or searches the cheaper side of each (i,j)
+        assert 0 < sr <= pulls + int((deg * (deg - 1) // 2).sum())
 
 
-def test_erdos_renyi_matches_oracle(cuda, bale, oracle):
+def test_erdos_renyi_matches_oracle(cuda, bale, oracle, mode):
     n = 1 << 16
     L = bale.gen_erdos_renyi(n, 32.0 / n, 7)
     assert bale.triangle_agi(L)[0] == oracle.triangle_agi_mt(L.offset, L.nonzero)
@@ -62,13 +75,13 @@ def _clique(m: int):
 
 
 @pytest.mark.parametrize("m", [0, 1, 2, 3, 40, 1025, 1800])
-def test_cliques_long_rows_and_tiny_graphs(cuda, bale, m):
+def test_cliques_long_rows_and_tiny_graphs(cuda, bale, m, mode):
     off, col = _clique(m)
     L = bale.SparseMatrix(off, col)
     assert bale.triangle_agi(L)[0] == m * (m - 1) * (m - 2) // 6
 
 
-def test_malformed_matrices_are_errors_not_faults(cuda, bale):
+def test_malformed_matrices_are_errors_not_faults(cuda, bale, mode):
     good_off, good_col = _clique(6)
     cases = []
     c = good_col.copy(); c[-1] = 5                      # column == row (not strict)
@@ -98,8 +111,45 @@ def test_device_entry_point(cuda, bale, oracle):
     assert int(count.item()) == 2 * oracle.triangle_agi(L.offset, L.nonzero)[0]
 
 
-def test_full_size_rmat_scale22(cuda, bale, oracle):
+def test_full_size_rmat_scale22(cuda, bale, oracle, mode):
     """The R-MAT scale-22 configuration, exact against the multi-threaded oracle."""
     L = bale.gen_rmat(22, 16, 0.57, 0.19, 0.19, 6)
     cnt, _, _ = bale.triangle_agi(L)
     assert cnt == oracle.triangle_agi_mt(L.offset, L.nonzero)
+
+
+def test_heavy_rows_with_malformed_neighbours(cuda, bale, mode):
+    """A heavy row (>= 64 nonzeros, small label) whose neighbour row has bad
+    offsets, and a heavy row that is not ascending: both are errors."""
+    m = 100
+    off, col = _clique(m)
+    o = off.copy()
+    o[70] = o[71] + 5  # row 69 ends after row 70 starts: offsets decrease at 70
+    with pytest.raises(bale.BaleError):
+        bale.triangle_agi(bale.SparseMatrix(o, col))
+    c = col.copy()
+    s = off[90]
+    c[s + 10], c[s + 11] = c[s + 11], c[s + 10]  # row 90 (90 nonzeros) not ascending
+    with pytest.raises(bale.BaleError):
+        bale.triangle_agi(bale.SparseMatrix(off, c))
+    assert bale.triangle_agi(bale.SparseMatrix(off, col))[0] == m * (m - 1) * (m - 2) // 6
+
+
+def test_mixed_heavy_and_light_rows_match_oracle(cuda, bale, oracle, mode):
+    """R-MAT with low edge factor plus a clique grafted on low labels: rows on
+    both sides of the heavy threshold, heavy rows reading light rows."""
+    L = bale.gen_rmat(15, 4, 0.57, 0.19, 0.19, 77)
+    off, col = L.offset, L.nonzero
+    m = 300  # make labels 0..299 a clique: rows 64..299 become heavy
+    rows = []
+    for i in range(L.numrows):
+        r = col[off[i]:off[i + 1]]
+        if i < m:
+            r = np.union1d(r, np.arange(i, dtype=np.int64))
+        rows.append(r)
+    noff = np.zeros(L.numrows + 1, np.int64)
+    noff[1:] = np.cumsum([r.size for r in rows])
+    ncol = np.concatenate(rows).astype(np.int64)
+    M = bale.SparseMatrix(noff, ncol)
+    assert oracle.is_strict_lower_tidy(noff, ncol)
+    assert bale.triangle_agi(M)[0] == oracle.triangle_agi(noff, ncol)[0]

@@ -63,6 +63,11 @@ bool ig_part_supported(int64_t n, int64_t table_len);
 int launch_ig_partitioned(int64_t *tgt, const int64_t *index, int64_t n, const int64_t *table,
                           int64_t table_len, int shift, unsigned long long *bad, void *ws,
                           unsigned long long *cursor, cudaStream_t stream);
+// Histogram over the same region partition (tables beyond L2).
+size_t histo_part_workspace_bytes(int64_t n, int64_t ncounts);
+int launch_histo_partitioned(int64_t *counts, int64_t ncounts, const int64_t *index, int64_t n, int shift,
+                             unsigned long long *bad, void *ws, unsigned long long *cursor,
+                             cudaStream_t stream);
 // Bitmap/search hybrid triangle counting (tri_hybrid.cu); needs numrows < 2^32.
 size_t tri_hybrid_workspace_bytes(int64_t numrows, int64_t nnz);
 int launch_triangle_hybrid(const int64_t *offset, const int64_t *nonzero, int64_t numrows, int64_t nnz,

@@ -143,12 +143,27 @@ int launch_histo(int64_t *counts, int64_t ncounts, const int64_t *index, int64_t
   const int sms = num_sms();
   const bool aligned = (reinterpret_cast<uintptr_t>(index) & 15) == 0;
   // Mode: 0 shared-memory private table, 1 warp-aggregated L2 reductions,
-  // 2 plain L2 reductions.  Automatic: shared memory when the table fits,
-  // aggregation while in-warp collisions are likely, plain above that.
+  // 2 plain L2 reductions, 3 region-partitioned L2 reductions.  Automatic:
+  // shared memory when the table fits; plain L2 reductions while the table
+  // lives in L2 (uniform updates rarely collide inside a warp, so the
+  // aggregation's __match_any_sync costs more than it saves -- it pays only
+  // for skewed updates, which the tuner or the caller can select); the
+  // region partition once the table is well beyond L2.
   int64_t mode = knob("histo.mode");
-  if (mode < 0 || mode > 2) mode = ncounts <= kSmemMaxCounters ? 0 : (ncounts <= (int64_t(1) << 20) ? 1 : 2);
-  if (mode == 0 && ncounts > kSmemMaxCounters) mode = 1;
-  if (!aligned && mode == 0) mode = 1;
+  if (mode < 0 || mode > 3) {
+    if (ncounts <= kSmemMaxCounters) mode = 0;
+    else if (ncounts * 8 > (int64_t(96) << 20) && n >= (int64_t(1) << 20)) mode = 3;
+    else mode = 2;
+  }
+  if (mode == 0 && ncounts > kSmemMaxCounters) mode = 2;
+  if (!aligned && (mode == 0 || mode == 3)) mode = 2;
+  if (mode == 3 && ncounts > (int64_t(1024) << 22)) mode = 2;
+  if (mode == 3) {
+    void *ws = device_workspace(histo_part_workspace_bytes(n, ncounts));
+    unsigned long long *cursor = next_cursor_word();
+    if (!ws || !cursor) return BALE_ENOMEM;
+    return launch_histo_partitioned(counts, ncounts, index, n, shift, bad, ws, cursor, stream);
+  }
 
   if (mode == 0) {
     const size_t smem = static_cast<size_t>(ncounts) * sizeof(uint32_t);

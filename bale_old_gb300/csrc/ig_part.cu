@@ -178,6 +178,41 @@ __global__ void __launch_bounds__(kThreads)
   if (lane == 0 && nbad) atomicAdd(bad, nbad);
 }
 
+// Histogram over the same partition: region-major L2 reductions, so the
+// counters of one region stay in L2 while every chunk's updates to it land.
+__global__ void __launch_bounds__(kThreads)
+    igp_histo_kernel(const uint32_t *__restrict__ entries, const uint16_t *__restrict__ starts,
+                     int64_t nchunks, int nreg, int64_t *__restrict__ counts,
+                     unsigned long long *__restrict__ cursor, unsigned long long *__restrict__ bad) {
+  const unsigned lane = lane_id();
+  const uint64_t ef = policy_evict_first();
+  const int64_t total = static_cast<int64_t>(nreg + 1) * nchunks;
+  unsigned long long nbad = 0;
+  for (;;) {
+    unsigned long long d0 = 0;
+    if (lane == 0) d0 = atomicAdd(cursor, static_cast<unsigned long long>(kDescPerClaim));
+    d0 = __shfl_sync(0xffffffffu, d0, 0);
+    if (static_cast<int64_t>(d0) >= total) break;
+    for (int g = 0; g < kDescPerClaim; g++) {
+      const int64_t d = static_cast<int64_t>(d0) + g;
+      if (d >= total) break;
+      const int b = static_cast<int>(d / nchunks);
+      const int64_t c = d - static_cast<int64_t>(b) * nchunks;
+      const uint16_t *st = starts + c * (nreg + 2) + b;
+      const int s = st[0], e = st[1];
+      if (b == nreg) {  // out-of-range updates: counted, not applied
+        if (lane == 0) nbad += static_cast<unsigned long long>(e - s);
+        continue;
+      }
+      const uint32_t *ent = entries + c * kChunk;
+      int64_t *reg = counts + (static_cast<int64_t>(b) << kRBits);
+      for (int k = s + static_cast<int>(lane); k < e; k += 32)
+        red_add_u64(reg + (ld_u32_pol(ent + k, ef) >> kCBits), 1ull);
+    }
+  }
+  if (lane == 0 && nbad) atomicAdd(bad, nbad);
+}
+
 __global__ void __launch_bounds__(kThreads)
     igp_unpermute_kernel(const uint32_t *__restrict__ entries, const int64_t *__restrict__ val,
                          int64_t *__restrict__ tgt, int64_t n) {
@@ -215,6 +250,39 @@ size_t ig_part_workspace_bytes(int64_t n, int64_t table_len) {
   b += static_cast<size_t>(nchunks) * kChunk * sizeof(int64_t);   // values
   b += ((static_cast<size_t>(nchunks) * (nreg + 2) * sizeof(uint16_t)) + 255) & ~size_t(255);
   return b;
+}
+
+// Entries and region starts only (no values): the histogram's workspace.
+size_t histo_part_workspace_bytes(int64_t n, int64_t ncounts) {
+  const int64_t nchunks = (n + kChunk - 1) / kChunk;
+  const int64_t nreg = (ncounts + (int64_t(1) << kRBits) - 1) >> kRBits;
+  return static_cast<size_t>(nchunks) * kChunk * sizeof(uint32_t) +
+         (((static_cast<size_t>(nchunks) * (nreg + 2) * sizeof(uint16_t)) + 255) & ~size_t(255));
+}
+
+int launch_histo_partitioned(int64_t *counts, int64_t ncounts, const int64_t *index, int64_t n, int shift,
+                             unsigned long long *bad, void *ws, unsigned long long *cursor,
+                             cudaStream_t stream) {
+  const int64_t nchunks = (n + kChunk - 1) / kChunk;
+  const int nreg = static_cast<int>((ncounts + (int64_t(1) << kRBits) - 1) >> kRBits);
+  uint32_t *entries = static_cast<uint32_t *>(ws);
+  uint16_t *starts = reinterpret_cast<uint16_t *>(static_cast<char *>(ws) +
+                                                  static_cast<size_t>(nchunks) * kChunk * sizeof(uint32_t));
+  BALE_CUDA_OK(cudaMemsetAsync(cursor, 0, sizeof(unsigned long long), stream));
+  igp_partition_kernel<<<static_cast<unsigned>(nchunks), kThreads, 0, stream>>>(
+      index, n, static_cast<uint64_t>(ncounts), shift, nreg, entries, starts);
+  BALE_CUDA_OK(cudaGetLastError());
+  int occ = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, igp_histo_kernel, kThreads, 0) != cudaSuccess || occ < 1)
+    occ = 1;
+  int64_t blocks = static_cast<int64_t>(num_sms()) * occ;
+  const int64_t warps_needed = ((nreg + 1) * nchunks + kDescPerClaim - 1) / kDescPerClaim;
+  if (blocks * (kThreads / 32) > warps_needed) blocks = (warps_needed + (kThreads / 32) - 1) / (kThreads / 32);
+  if (blocks < 1) blocks = 1;
+  igp_histo_kernel<<<static_cast<unsigned>(blocks), kThreads, 0, stream>>>(entries, starts, nchunks, nreg,
+                                                                         counts, cursor, bad);
+  BALE_CUDA_OK(cudaGetLastError());
+  return BALE_OK;
 }
 
 bool ig_part_supported(int64_t n, int64_t table_len) {

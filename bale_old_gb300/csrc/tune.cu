@@ -25,7 +25,7 @@ Knob g_knobs[] = {
     {"ig.blocks_per_sm", -1},   // resident blocks per SM to launch
     {"ig.table_policy", -1},    // 0 L1::no_allocate, 1 L2 evict_last, 2 L2 evict_first, 3 cached
     {"ig.l2_fetch", -1},        // cudaLimitMaxL2FetchGranularity in bytes (0..128)
-    {"histo.mode", -1},         // 0 shared-memory private, 1 warp-aggregated L2, 2 plain L2, 3 partitioned
+    {"histo.mode", -1},         // 0 shared-memory private, 1 warp-aggregated L2, 2 plain L2, 3 region-partitioned
     {"histo.unroll", -1},       // pairs per thread per trip (L2 modes): 1, 2, 4, 8
     {"histo.blocks_per_sm", -1},
     {"histo.smem_updates_per_counter", -1},  // updates per counter per block (shared-memory mode)

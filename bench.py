@@ -1,30 +1,34 @@
 """Benchmark of the GB300 irregular-access core.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
-                    [--workload ig|ig_zipf|histo|triangles]
+                    [--workload ig|ig_zipf|histo|triangles] [--only]
 
-One JSON line on stdout (rank 0).  A "step" is one pass of the workload's
-kernel over its whole synthetic input:
+Prints one JSON line (rank 0).  A "step" is one pass of a workload's kernels
+over its whole synthetic input (seeded SplitMix64 streams; R-MAT graph):
 
-* ig        (default, the headline): 2^26-entry int64 table of seeded random
-            values, 2^28 uniform requests -> GUP/s (10^9 requests/s);
-* ig_zipf   : same, requests Zipf(1.1) over a keyed permutation of the table;
+* ig        (headline): 2^26-entry int64 table of random values, 2^28
+            uniform requests -> GUP/s (10^9 requests/s);
+* ig_zipf   : same table, requests Zipf(1.1) over a keyed permutation;
 * histo     : 10^7 uniform updates into 10^6 int64 counters -> GUP/s;
-* triangles : R-MAT scale 22, edge factor 16, (0.57,0.19,0.19,0.05), degree
-            ordered strictly lower L -> edges/s (nnz(L) per second).
+* triangles : R-MAT scale 22, edge factor 16, (0.57,0.19,0.19,0.05),
+            symmetrised, degree-ordered strictly lower L -> edges/s (nnz(L)/s).
 
-``value`` is device-timed with inputs resident in HBM (CUDA events on the
-launching stream, W warm-up steps, K timed steps; the index streams are
-larger than L2 so no flush is needed, except histo whose 80 MB stream is
-followed by a 256 MiB L2 flush write each step, outside the kernel's own
-events).  ``e2e`` is the same metric through the reference-facing C ABI
-(ig_agi / histo_agi / triangle_agi) with pinned host buffers, copies
-included.  ``--impl reference`` times the CPU implementation of the path
-(the oracle restatement of the reference's AGI loop, all host threads) on a
-bounded sample of the same workload.
+The headline workload fills the top-level keys; unless --only is given the
+other three are measured in the same run and reported under "workloads".
 
-Under torchrun every rank runs its own copy of the workload on its own GPU
-(weak scaling); rank 0 reports the job total over the max of the ranks' times.
+``value``: device time from CUDA events on the launching stream, inputs
+resident in HBM, W warm-up steps then K timed steps.  The ig index/output
+streams (2 GiB each) exceed L2; for histo and triangles, whose inputs fit
+in L2, a 256 MiB buffer is rewritten between timed steps (outside the events).
+``e2e``: the same metric through the reference-facing C ABI (ig_agi,
+histo_agi, triangle_agi) with pinned host buffers, copies inside the timed
+region.  ``cpu_baseline``: the oracle restatement of the reference's AGI loop
+on all host threads, on a bounded sample.  ``--impl reference`` times that
+CPU implementation alone.
+
+Under torchrun every rank runs its own copy on its own GPU (weak scaling,
+replicas: no data-path collective); rank 0 reports the job total over the
+max of the ranks' times.
 """
 from __future__ import annotations
 
@@ -44,13 +48,19 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 HBM_FALLBACK_GBS = 6800.0
+IG_TABLE = 1 << 26
+IG_REQUESTS = 1 << 28
+HISTO_COUNTS = 1_000_000
+HISTO_UPDATES = 10_000_000
+TRI_SCALE = 22
+FLUSH_BYTES = 256 << 20
 
 
 # ---------------------------------------------------------------------------
 # distributed plumbing (torchrun sets RANK/WORLD_SIZE/LOCAL_RANK)
 # ---------------------------------------------------------------------------
 class Dist:
-    def __init__(self, want_gpus: int):
+    def __init__(self):
         self.world = int(os.environ.get("WORLD_SIZE", "1"))
         self.rank = int(os.environ.get("RANK", "0"))
         self.local = int(os.environ.get("LOCAL_RANK", "0"))
@@ -70,6 +80,7 @@ class Dist:
             self.pg.barrier()
 
     def max(self, x: float) -> float:
+        """Max of x over ranks (the job's time is its slowest rank's)."""
         if not self.pg:
             return x
         import torch
@@ -84,6 +95,12 @@ class Dist:
             self.pg.destroy_process_group()
 
 
+def job_rate(units_per_rank: int, seconds_max: float, world: int) -> float:
+    """Whole-job throughput: every rank processed units_per_rank in at most
+    seconds_max (the max over ranks)."""
+    return world * units_per_rank / seconds_max
+
+
 def measured_peaks() -> dict:
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -95,7 +112,7 @@ def measured_peaks() -> dict:
 
 
 def committed_traffic() -> dict:
-    """Per-launch DRAM bytes from the committed ncu summaries (profiles/)."""
+    """Per-step DRAM bytes from the committed ncu summaries (profiles/)."""
     p = ROOT / "profiles" / "traffic.json"
     if p.exists():
         try:
@@ -106,12 +123,13 @@ def committed_traffic() -> dict:
 
 
 # ---------------------------------------------------------------------------
-# clocks sampled while the timed region runs
+# clocks sampled while a timed region runs
 # ---------------------------------------------------------------------------
 class ClockSampler:
     QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    NAMES = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
 
     def __init__(self, gpu_index: int):
         self.gpu = gpu_index
@@ -124,8 +142,8 @@ class ClockSampler:
             os.close(fd)
             self.fh = open(self.path, "w")
             self.proc = subprocess.Popen(
-                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
-                 "-lms", "100"], stdout=self.fh, stderr=subprocess.DEVNULL)
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.QUERY}",
+                 "--format=csv,noheader,nounits", "-lms", "100"], stdout=self.fh, stderr=subprocess.DEVNULL)
             time.sleep(0.3)
         except (OSError, ValueError):
             self.proc = None
@@ -144,7 +162,6 @@ class ClockSampler:
         if not self.path or not os.path.exists(self.path):
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
         sm, smax, reasons = [], None, set()
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for line in open(self.path):
             f = [x.strip() for x in line.split(",")]
             if len(f) < 9:
@@ -154,7 +171,7 @@ class ClockSampler:
                 smax = float(f[2])
             except ValueError:
                 continue
-            for name, v in zip(names, f[5:9]):
+            for name, v in zip(self.NAMES, f[5:9]):
                 if v.lower().startswith("active"):
                     reasons.add(name)
         os.unlink(self.path)
@@ -163,34 +180,18 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------------------
-# workloads
+# timing helpers
 # ---------------------------------------------------------------------------
-IG_TABLE = 1 << 26
-IG_REQUESTS = 1 << 28
-HISTO_COUNTS = 1_000_000
-HISTO_UPDATES = 10_000_000
-TRI_SCALE = 22
-
-
-def gen_ig_inputs(bale, zipf: bool):
-    table = bale.gen_values(IG_TABLE, 2)
-    if zipf:
-        index = bale.gen_zipf(IG_REQUESTS, IG_TABLE, 1.1, 4, 5)
-    else:
-        index = bale.gen_uniform(IG_REQUESTS, IG_TABLE, 3)
-    return index, table
-
-
-def time_device(fn, steps: int, warmup: int, stream, between=None):
-    """Average CUDA-event time of fn() per step (ms), on `stream`."""
+def time_device(fn, steps: int, warmup: int, between=None) -> float:
+    """Average CUDA-event time (ms) of fn() per step on the current stream."""
     import torch
 
+    stream = torch.cuda.current_stream()
     for _ in range(warmup):
         if between:
             between()
         fn()
     torch.cuda.synchronize()
-    per = []
     total = 0.0
     for _ in range(steps):
         if between:
@@ -200,108 +201,207 @@ def time_device(fn, steps: int, warmup: int, stream, between=None):
         fn()
         b.record(stream)
         b.synchronize()
-        per.append(a.elapsed_time(b))
-        total += per[-1]
-    return total / steps, per
+        total += a.elapsed_time(b)
+    return total / steps
 
 
-def run_gb300(args, dist: Dist) -> dict | None:
+def time_host(fn, steps: int, warmup: int) -> float:
+    """Average wall seconds of a synchronous call."""
+    for _ in range(warmup):
+        fn()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        fn()
+    return (time.perf_counter() - t0) / steps
+
+
+# ---------------------------------------------------------------------------
+# workloads: each returns a dict with value/roofline/e2e/... for one rank
+# ---------------------------------------------------------------------------
+def ig_inputs(bale, zipf: bool):
+    table = bale.gen_values(IG_TABLE, 2)
+    index = bale.gen_zipf(IG_REQUESTS, IG_TABLE, 1.1, 4, 5) if zipf else bale.gen_uniform(IG_REQUESTS, IG_TABLE, 3)
+    return index, table
+
+
+def run_ig(ctx, zipf: bool) -> dict:
     import torch
 
-    import bale_old_gb300 as bale
-
-    dev = torch.device("cuda", dist.local)
-    torch.cuda.set_device(dev)
-    stream = torch.cuda.current_stream()
-    peaks = measured_peaks()
-    hbm = float(peaks.get("hbm_gbs") or HBM_FALLBACK_GBS)
-    peak_note = "measured" if peaks.get("hbm_gbs") else "fallback"
-    traffic = committed_traffic()
-    wl = args.workload
-    flush = None
-    result: dict = {}
-
-    if wl in ("ig", "ig_zipf"):
-        index_h, table_h = gen_ig_inputs(bale, wl == "ig_zipf")
-        n = index_h.size
-        index = torch.from_numpy(index_h).to(dev)
-        table = torch.from_numpy(table_h).to(dev)
-        tgt = torch.empty_like(index)
-        bad = torch.zeros(1, dtype=torch.int64, device=dev)
-        fn = lambda: bale.ig_dev(tgt, index, table, bad=bad)  # noqa: E731
-        units, unit_name = n, "GUP/s"
-        algo_bytes = 48 * n  # 8 B index + 32 B table sector + 8 B output
-        kernel = "ig_gather_kernel"
-        config = {"workload": f"ig {'zipf(1.1) over a keyed permutation' if wl == 'ig_zipf' else 'uniform'}: "
-                              f"2^26-entry int64 table, 2^28 int64 requests",
-                  "table_entries": IG_TABLE, "requests": n,
-                  "l2": "index and output streams (2 GiB each) exceed L2; no flush"}
-        metric = "GUP/s index gather (10^9 requests/s)"
-
-        def check():
-            torch.cuda.synchronize()
-            s = slice(0, 1 << 20)
-            want = table_h[index_h[s]]
-            return bool(np.array_equal(tgt[s].cpu().numpy(), want)) and int(bad.item()) == 0
-
+    bale, dev, args = ctx["bale"], ctx["dev"], ctx["args"]
+    index_h, table_h = ig_inputs(bale, zipf)
+    n = index_h.size
+    index = torch.from_numpy(index_h).to(dev)
+    table = torch.from_numpy(table_h).to(dev)
+    tgt = torch.empty_like(index)
+    bad = torch.zeros(1, dtype=torch.int64, device=dev)
+    fn = lambda: bale.ig_dev(tgt, index, table, bad=bad)  # noqa: E731
+    with ClockSampler(ctx["gpu"]) as clocks:
+        ctx["dist"].barrier()
+        ms = time_device(fn, args.steps, args.warmup)
+    ms_max = ctx["dist"].max(ms)
+    torch.cuda.synchronize()
+    s = slice(0, 1 << 22)
+    ok = bool(np.array_equal(tgt[s].cpu().numpy(), table_h[index_h[s]])) and int(bad.item()) == 0
+    part = table_h.size * 8 > (96 << 20) and n >= (1 << 20)
+    kernels = 3 if part else 1
+    algo = 48 * n  # 8 B index + 32 B table sector + 8 B output per request
+    wl = "ig_zipf" if zipf else "ig"
+    out = {
+        "metric": "GUP/s index gather (10^9 requests/s)",
+        "value": round(job_rate(n, ms_max / 1e3, ctx["dist"].world) / 1e9, 4), "unit": "GUP/s",
+        "ms_per_step": round(ms_max, 4), "parity_sample_ok": ok,
+        "roofline": roofline(ctx, wl, algo, ms / 1e3,
+                             "ig region-partitioned gather (partition + gather + unpermute)" if part
+                             else "ig_gather_kernel"),
+        "clocks": clocks.summary(),
+        "gpu_launches": kernels * args.steps,
+        "config": {"workload": f"ig {'Zipf(1.1) over a keyed permutation' if zipf else 'uniform'}: "
+                               "2^26-entry int64 table, 2^28 int64 requests",
+                   "table_entries": IG_TABLE, "requests": n,
+                   "l2": "index and output streams (2 GiB each) exceed L2; no flush"},
+    }
+    del index, table, tgt
+    if not zipf:
         pin_idx = torch.from_numpy(index_h).pin_memory()
         pin_tab = torch.from_numpy(table_h).pin_memory()
         pin_tgt = torch.empty(n, dtype=torch.int64).pin_memory()
+        torch.cuda.empty_cache()
+        call = lambda: bale.ig_agi(pin_tgt.numpy(), pin_idx.numpy(), pin_tab.numpy())  # noqa: E731
+        ctx["dist"].barrier()
+        e2e_s = ctx["dist"].max(time_host(call, args.steps, min(args.warmup, 3)))
+        out["e2e"] = {"value": round(job_rate(n, e2e_s, ctx["dist"].world) / 1e9, 4), "unit": "GUP/s",
+                      "ms_per_step": round(e2e_s * 1e3, 3), "h2d_bytes_per_step": 8 * n + 8 * IG_TABLE,
+                      "d2h_bytes_per_step": 8 * n, "path": "ig_agi C ABI, pinned host buffers",
+                      "parity_sample_ok": bool(np.array_equal(pin_tgt.numpy()[s], table_h[index_h[s]]))}
+        if ctx["cpu"]:
+            out["cpu_baseline"] = cpu_ig(index_h, table_h, ctx["budget"])
+    return out
 
-        def e2e_call():
-            t = bale.ig_agi(pin_tgt.numpy(), pin_idx.numpy(), pin_tab.numpy())
-            return t
 
-        h2d, d2h = 8 * n + 8 * IG_TABLE, 8 * n
-        e2e_check = lambda: bool(np.array_equal(pin_tgt.numpy()[: 1 << 20], table_h[index_h[: 1 << 20]]))  # noqa: E731
-    else:
-        raise SystemExit(f"unknown workload {wl}")
+def run_histo(ctx) -> dict:
+    import torch
 
-    # device-timed region (inputs resident)
-    dist.barrier()
-    with ClockSampler(dist.local) as clocks:
-        ms, per = time_device(fn, args.steps, args.warmup, stream, between=flush)
-    ok = check()
-    ms_max = dist.max(ms)
-    value = dist.world * units / (ms_max / 1e3) / 1e9
-    kernel_s = ms / 1e3
-    achieved = algo_bytes / kernel_s / 1e9
-    tr = traffic.get(wl, {}).get("dram_bytes_per_launch")
-    result.update({
-        "metric": metric, "value": round(value, 4), "unit": unit_name,
-        "ms_per_step": round(ms_max, 4), "parity_sample_ok": ok,
-        "roofline": {"bound": "hbm", "kernel": kernel, "achieved": round(achieved, 1), "peak": hbm,
-                     "peak_source": peak_note, "unit": "GB/s", "frac": round(achieved / hbm, 4),
-                     "traffic": tr, "algorithmic_bytes_per_launch": algo_bytes},
-        "clocks": clocks.summary(), "config": config,
-        "gpu_launches": args.steps,
-    })
+    bale, dev, args = ctx["bale"], ctx["dev"], ctx["args"]
+    index_h = bale.gen_uniform(HISTO_UPDATES, HISTO_COUNTS, 1)
+    want = np.bincount(index_h, minlength=HISTO_COUNTS)
+    index = torch.from_numpy(index_h).to(dev)
+    counts = torch.zeros(HISTO_COUNTS, dtype=torch.int64, device=dev)
+    bad = torch.zeros(1, dtype=torch.int64, device=dev)
+    flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.int32, device=dev)
+    fn = lambda: bale.histo_dev(counts, index, bad=bad)  # noqa: E731
+    between = lambda: flush.fill_(1)  # noqa: E731
+    with ClockSampler(ctx["gpu"]) as clocks:
+        ctx["dist"].barrier()
+        ms = time_device(fn, args.steps, args.warmup, between)
+    ms_max = ctx["dist"].max(ms)
+    torch.cuda.synchronize()
+    reps = args.steps + args.warmup
+    ok = bool(np.array_equal(counts.cpu().numpy(), reps * want)) and int(bad.item()) == 0
+    n = HISTO_UPDATES
+    algo = 72 * n  # 8 B index + 32 B sector read + 32 B write-back per update
+    out = {"metric": "GUP/s histogram (10^9 updates/s)",
+           "value": round(job_rate(n, ms_max / 1e3, ctx["dist"].world) / 1e9, 4), "unit": "GUP/s",
+           "ms_per_step": round(ms_max, 4), "parity_ok": ok,
+           "roofline": roofline(ctx, "histo", algo, ms / 1e3, "histo_global_kernel (plain L2 reductions)",
+                                note="the 8 MB table is L2-resident: L2 atomics, not HBM, bound this config"),
+           "clocks": clocks.summary(), "gpu_launches": args.steps,
+           "config": {"workload": "histo: 10^7 uniform updates into 10^6 int64 counters",
+                      "updates": n, "counters": HISTO_COUNTS,
+                      "l2": "inputs fit in L2: a 256 MiB buffer is rewritten between steps"}}
+    del index, counts, flush
+    pin_idx = torch.from_numpy(index_h).pin_memory()
+    pin_cnt = torch.zeros(HISTO_COUNTS, dtype=torch.int64).pin_memory()
+    call = lambda: bale.histo_agi(pin_idx.numpy(), pin_cnt.numpy())  # noqa: E731
+    ctx["dist"].barrier()
+    e2e_s = ctx["dist"].max(time_host(call, args.steps, min(args.warmup, 3)))
+    calls = args.steps + min(args.warmup, 3)
+    out["e2e"] = {"value": round(job_rate(n, e2e_s, ctx["dist"].world) / 1e9, 4), "unit": "GUP/s",
+                  "ms_per_step": round(e2e_s * 1e3, 3), "h2d_bytes_per_step": 8 * n + 8 * HISTO_COUNTS,
+                  "d2h_bytes_per_step": 8 * HISTO_COUNTS, "path": "histo_agi C ABI, pinned host buffers",
+                  "parity_ok": bool(np.array_equal(pin_cnt.numpy(), calls * want))}
+    if ctx["cpu"]:
+        out["cpu_baseline"] = cpu_histo(index_h, ctx["budget"])
+    return out
 
-    # e2e through the C ABI (host pinned buffers, copies inside)
-    for _ in range(max(1, args.warmup)):
-        e2e_call()
-    dist.barrier()
+
+def run_triangles(ctx) -> dict:
+    import torch
+
+    bale, dev, args = ctx["bale"], ctx["dev"], ctx["args"]
     t0 = time.perf_counter()
-    for _ in range(args.steps):
-        e2e_call()
-    e2e_s = dist.max((time.perf_counter() - t0) / args.steps)
-    result["e2e"] = {"value": round(dist.world * units / e2e_s / 1e9, 4), "unit": unit_name,
-                     "ms_per_step": round(e2e_s * 1e3, 3), "h2d_bytes_per_step": h2d,
-                     "d2h_bytes_per_step": d2h, "path": "ig_agi C ABI, pinned host buffers",
-                     "parity_sample_ok": e2e_check()}
+    L = bale.gen_rmat(TRI_SCALE, 16, 0.57, 0.19, 0.19, 6)
+    gen_s = time.perf_counter() - t0
+    n, nnz = L.numrows, L.nnz
+    off = torch.from_numpy(L.offset).to(dev)
+    col = torch.from_numpy(L.nonzero).to(dev)
+    cnt = torch.zeros(1, dtype=torch.int64, device=dev)
+    flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.int32, device=dev)
+    fn = lambda: bale.triangle_dev(off, col, cnt)  # noqa: E731
+    between = lambda: flush.fill_(1)  # noqa: E731
+    with ClockSampler(ctx["gpu"]) as clocks:
+        ctx["dist"].barrier()
+        ms = time_device(fn, args.steps, args.warmup, between)
+    ms_max = ctx["dist"].max(ms)
+    torch.cuda.synchronize()
+    per_step = int(cnt.item()) // (args.steps + args.warmup)
+    deg = np.diff(L.offset)
+    pulls = int(deg[L.nonzero].sum())
+    algo = 8 * (n + 1) + 8 * nnz + 8 * pulls
+    out = {"metric": "edges/s triangle counting (nnz(L) per second)",
+           "value": round(job_rate(nnz, ms_max / 1e3, ctx["dist"].world) / 1e9, 4), "unit": "Gedges/s",
+           "ms_per_step": round(ms_max, 4), "triangles": per_step,
+           "roofline": roofline(ctx, "triangles", algo, ms / 1e3,
+                                "triangle hybrid (convert + classify + heavy bitmap + light search)",
+                                note="algorithmic bytes count every row-j element as an 8 B HBM read "
+                                     "(8(n+1) + 8 nnz + 8 pulls); repeated rows are L2 hits, so the "
+                                     "fraction can exceed 1"),
+           "clocks": clocks.summary(), "gpu_launches": 4 * args.steps,
+           "config": {"workload": "triangles: R-MAT scale 22, edge factor 16, (0.57,0.19,0.19,0.05), "
+                                  "symmetrised, deduplicated, degree-ordered strictly lower L",
+                      "n": n, "nnz": nnz, "pulls": pulls, "generate_s": round(gen_s, 2),
+                      "l2": "the 513 MiB CSR exceeds L2; a 256 MiB buffer is also rewritten between steps"}}
+    del off, col, flush
+    torch.cuda.empty_cache()
+    res = {}
 
-    if dist.rank == 0 and not args.no_cpu_baseline:
-        result["cpu_baseline"] = cpu_baseline(wl, index_h, table_h)
-    return result
+    def call():
+        res["r"] = bale.triangle_agi(L)
+
+    ctx["dist"].barrier()
+    e2e_s = ctx["dist"].max(time_host(call, args.steps, min(args.warmup, 3)))
+    out["e2e"] = {"value": round(job_rate(nnz, e2e_s, ctx["dist"].world) / 1e9, 4), "unit": "Gedges/s",
+                  "ms_per_step": round(e2e_s * 1e3, 3), "h2d_bytes_per_step": 8 * (n + 1) + 8 * nnz,
+                  "d2h_bytes_per_step": 32, "path": "triangle_agi C ABI (numpy host buffers)",
+                  "triangles": res["r"][0]}
+    if ctx["cpu"]:
+        out["cpu_baseline"] = cpu_triangles(L, ctx["budget"])
+        out["parity_ok"] = out["cpu_baseline"].get("triangles") == per_step == res["r"][0]
+    return out
 
 
-def cpu_baseline(wl: str, index_h, table_h, budget_s: float = 10.0) -> dict:
-    """The oracle restatement of ig_agi on all host threads, on a bounded
-    sample: the first 2^25 requests of the same workload, repeated for about
-    budget_s seconds."""
+def roofline(ctx, wl: str, algo_bytes: int, seconds: float, kernel: str, note: str | None = None) -> dict:
+    peak = ctx["peak"]
+    achieved = algo_bytes / seconds / 1e9
+    tr = ctx["traffic"].get(wl, {}).get("dram_bytes_per_step")
+    r = {"bound": "hbm", "kernel": kernel, "achieved": round(achieved, 1), "peak": peak,
+         "peak_source": ctx["peak_src"], "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": tr,
+         "algorithmic_bytes_per_step": algo_bytes}
+    if note:
+        r["note"] = note
+    return r
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline: the oracle restatement of the reference's AGI loops
+# ---------------------------------------------------------------------------
+def _oracle():
     from oracle.pyoracle import Oracle
 
-    orc = Oracle()
+    return Oracle()
+
+
+def cpu_ig(index_h, table_h, budget_s: float) -> dict:
+    orc = _oracle()
     cores = orc.num_cpus()
     sample = np.ascontiguousarray(index_h[: 1 << 25])
     tgt = np.empty(sample.size, np.int64)
@@ -312,38 +412,101 @@ def cpu_baseline(wl: str, index_h, table_h, budget_s: float = 10.0) -> dict:
         if time.perf_counter() - t0 >= budget_s:
             break
     secs = time.perf_counter() - t0
-    return {"value": round(reps * sample.size / secs / 1e9, 5), "unit": "GUP/s", "cores": cores,
-            "kind": "port", "sample": f"{reps} x first 2^25 requests of the {wl} workload against "
-                                       "the full 2^26 table (oracle ig_agi loop, pthreads)"}
+    return {"value": round(reps * sample.size / secs / 1e9, 5), "unit": "GUP/s", "cores": cores, "kind": "port",
+            "sample": f"{reps} x the first 2^25 requests against the full 2^26 table "
+                      "(ig_agi loop, apps/ig_src/ig_agi.upc:61-64, one pthread per core)"}
+
+
+def cpu_histo(index_h, budget_s: float) -> dict:
+    orc = _oracle()
+    cores = orc.num_cpus()
+    counts = np.zeros(HISTO_COUNTS, np.int64)
+    reps, t0 = 0, time.perf_counter()
+    while True:
+        orc.histo_agi_mt(index_h, counts, cores)
+        reps += 1
+        if time.perf_counter() - t0 >= budget_s:
+            break
+    secs = time.perf_counter() - t0
+    return {"value": round(reps * index_h.size / secs / 1e9, 5), "unit": "GUP/s", "cores": cores, "kind": "port",
+            "sample": f"{reps} x all 10^7 updates (histo_agi loop, apps/histo_src/histo_agi.upc:61-66, "
+                      "relaxed atomic adds, one pthread per core)"}
+
+
+def cpu_triangles(L, budget_s: float) -> dict:
+    orc = _oracle()
+    cores = orc.num_cpus()
+    t0 = time.perf_counter()
+    cnt = orc.triangle_agi_mt(L.offset, L.nonzero, cores)
+    secs = time.perf_counter() - t0
+    return {"value": round(L.nnz / secs / 1e9, 5), "unit": "Gedges/s", "cores": cores, "kind": "port",
+            "sample": "1 x the full scale-22 graph (triangle_agi alg 0 loop, "
+                      "apps/triangle_src/triangle_agi.upc:69-99, rows shared dynamically by pthreads)",
+            "seconds": round(secs, 2), "triangles": cnt}
+
+
+# ---------------------------------------------------------------------------
+def run_gb300(args, dist: Dist) -> dict | None:
+    import torch
+
+    import bale_old_gb300 as bale
+
+    dev = torch.device("cuda", dist.local)
+    torch.cuda.set_device(dev)
+    peaks = measured_peaks()
+    ctx = {"bale": bale, "dev": dev, "args": args, "dist": dist, "gpu": dist.local,
+           "peak": float(peaks.get("hbm_gbs") or HBM_FALLBACK_GBS),
+           "peak_src": "measured (MEASURED_PEAKS.json hbm_gbs)" if peaks.get("hbm_gbs") else "fallback",
+           "traffic": committed_traffic(), "cpu": dist.rank == 0 and not args.no_cpu_baseline,
+           "budget": args.cpu_budget}
+    runners = {"ig": lambda: run_ig(ctx, False), "ig_zipf": lambda: run_ig(ctx, True),
+               "histo": lambda: run_histo(ctx), "triangles": lambda: run_triangles(ctx)}
+    head = runners[args.workload]()
+    torch.cuda.empty_cache()
+    if not args.only:
+        others = {}
+        for wl in ("ig_zipf", "histo", "triangles", "ig"):
+            if wl != args.workload:
+                others[wl] = runners[wl]()
+                torch.cuda.empty_cache()
+        head["workloads"] = others
+    return head
 
 
 def run_reference(args, dist: Dist) -> dict | None:
+    """The CPU implementation of the path (the oracle restatement of the
+    reference's AGI loops, all host threads) on a bounded sample per step."""
     if dist.rank != 0:
         return None
     import bale_old_gb300 as bale
-    from oracle.pyoracle import Oracle
 
-    orc = Oracle()
+    orc = _oracle()
     cores = orc.num_cpus()
     wl = args.workload
-    if wl not in ("ig", "ig_zipf"):
-        raise SystemExit(f"unknown workload {wl}")
-    index_h, table_h = gen_ig_inputs(bale, wl == "ig_zipf")
-    sample = np.ascontiguousarray(index_h[: 1 << 26])
-    tgt = np.empty(sample.size, np.int64)
-    for _ in range(args.warmup):
-        orc.ig_agi_mt(tgt, sample, table_h, cores)
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        orc.ig_agi_mt(tgt, sample, table_h, cores)
-    secs = (time.perf_counter() - t0) / args.steps
-    v = sample.size / secs / 1e9
-    return {"metric": "GUP/s index gather (10^9 requests/s)", "value": round(v, 5), "unit": "GUP/s",
-            "impl": "reference", "ms_per_step": round(secs * 1e3, 3),
-            "cpu_baseline": {"value": round(v, 5), "unit": "GUP/s", "cores": cores, "kind": "port",
-                             "sample": "first 2^26 of the 2^28 requests per step, full 2^26 table"},
-            "e2e": {"value": round(v, 5), "unit": "GUP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-            "config": {"workload": f"{wl}: 2^26-entry int64 table, 2^28 requests (2^26-request sample per step)"}}
+    if wl in ("ig", "ig_zipf"):
+        index_h, table_h = ig_inputs(bale, wl == "ig_zipf")
+        sample = np.ascontiguousarray(index_h[: 1 << 26])
+        tgt = np.empty(sample.size, np.int64)
+        secs = time_host(lambda: orc.ig_agi_mt(tgt, sample, table_h, cores), args.steps, args.warmup)
+        v, unit, metric = sample.size / secs / 1e9, "GUP/s", "GUP/s index gather (10^9 requests/s)"
+        desc = "first 2^26 of the 2^28 requests per step against the full 2^26 table"
+    elif wl == "histo":
+        index_h = bale.gen_uniform(HISTO_UPDATES, HISTO_COUNTS, 1)
+        counts = np.zeros(HISTO_COUNTS, np.int64)
+        secs = time_host(lambda: orc.histo_agi_mt(index_h, counts, cores), args.steps, args.warmup)
+        v, unit, metric = HISTO_UPDATES / secs / 1e9, "GUP/s", "GUP/s histogram (10^9 updates/s)"
+        desc = "all 10^7 updates per step"
+    else:
+        L = bale.gen_rmat(TRI_SCALE, 16, 0.57, 0.19, 0.19, 6)
+        secs = time_host(lambda: orc.triangle_agi_mt(L.offset, L.nonzero, cores), args.steps, 0)
+        v, unit, metric = L.nnz / secs / 1e9, "Gedges/s", "edges/s triangle counting (nnz(L) per second)"
+        desc = "the full scale-22 graph per step"
+    return {"metric": metric, "value": round(v, 5), "unit": unit, "impl": "reference",
+            "ms_per_step": round(secs * 1e3, 3),
+            "cpu_baseline": {"value": round(v, 5), "unit": unit, "cores": cores, "kind": "port", "sample": desc},
+            "e2e": {"value": round(v, 5), "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "config": {"workload": wl, "note": "oracle restatement of the reference's AGI loop "
+                                               "(the reference tree is not on this machine)"}}
 
 
 def main(argv=None) -> int:
@@ -353,17 +516,19 @@ def main(argv=None) -> int:
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="ig", choices=["ig", "ig_zipf", "histo", "triangles"])
+    ap.add_argument("--only", action="store_true", help="measure the selected workload only")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-budget", type=float, default=8.0, help="seconds of CPU baseline per workload")
     args = ap.parse_args(argv)
     args.warmup = max(args.warmup, 3)
-    dist = Dist(args.gpus)
+    dist = Dist()
     try:
         res = run_reference(args, dist) if args.impl == "reference" else run_gb300(args, dist)
         if dist.rank == 0 and res is not None:
             line = {"metric": res.pop("metric"), "value": res.pop("value"), "unit": res.pop("unit"),
                     "n_gpus": dist.world, "steps": args.steps, "warmup": args.warmup,
                     "ms_per_step": res.pop("ms_per_step"), "higher_is_better": True, "scaling": "weak",
-                    "vs_baseline": None, "dtype": "int64", "data": "synthetic (seeded SplitMix64)"}
+                    "vs_baseline": None, "dtype": "int64", "data": "synthetic (seeded SplitMix64 / R-MAT)"}
             line.update(res)
             print(json.dumps(line), flush=True)
     finally:

@@ -99,3 +99,32 @@ def test_full_size_config_1e7_updates_1e6_counters(cuda, bale, oracle):
     bale.histo_exstack(bale.pack_index(index), c)
     np.subtract.at(c, index, 2)
     assert not c.any()
+
+
+@pytest.mark.parametrize("hmode", [0, 1, 2, 3])
+@pytest.mark.parametrize("n,tsize", [(1, 1), (3_001, 977), (100_003, 48 * 1024),
+                                     (300_001, (1 << 22) + 5), (2_000_001, 3 * (1 << 22) + 1)])
+def test_every_mode_matches_oracle(cuda, bale, oracle, hmode, n, tsize):
+    """histo.mode 0..3 give identical counts (modes that cannot serve a size
+    fall back to one that can), including invalid updates."""
+    bale.tune_set("histo.mode", hmode)
+    try:
+        index = bale.gen_uniform(n, tsize, n + 3 * tsize)
+        counts = bale.gen_uniform(tsize, 9, 5)
+        want = counts.copy()
+        oracle.histo_agi(index, want)
+        bale.histo_agi(index, counts)
+        np.testing.assert_array_equal(counts, want)
+        import torch
+        idx_h = index.copy()
+        idx_h[::101] = tsize + 7  # out of range
+        idx = torch.from_numpy(idx_h).to(cuda)
+        c = torch.zeros(tsize, dtype=torch.int64, device=cuda)
+        bad = torch.zeros(1, dtype=torch.int64, device=cuda)
+        bale.histo_dev(c, idx, bad=bad)
+        torch.cuda.synchronize()
+        ok = idx_h < tsize
+        assert int(bad.item()) == int((~ok).sum())
+        np.testing.assert_array_equal(c.cpu().numpy(), np.bincount(idx_h[ok], minlength=tsize))
+    finally:
+        bale.tune_set("histo.mode", -1)

@@ -30,7 +30,7 @@ __all__ = [
     "splitmix64", "gen_uniform", "gen_values", "gen_negative_table", "gen_zipf",
     "keyed_perm", "gen_rmat", "gen_erdos_renyi", "gen_kronecker", "kronecker_triangles",
     "set_host_threads", "release_buffers", "version", "pack_index",
-    "tune_set", "tune_get", "tune_knobs",
+    "tune_set", "tune_get", "tune_knobs", "device_caps",
 ]
 
 _lib = load()
@@ -372,6 +372,19 @@ def set_host_threads(n: int) -> None:
 
 def release_buffers() -> None:
     _lib.bale_release_buffers()
+
+
+CAP_NAMES = ("sms", "pageable_memory_access", "pageable_uses_host_page_tables", "concurrent_managed_access",
+             "l2_bytes", "smem_optin_per_block", "host_pointer_for_registered_mem", "copy_engines",
+             "unified_addressing")
+
+
+def device_caps() -> dict[str, int]:
+    """Facts about the current CUDA device (bale_device_caps)."""
+    out = np.zeros(len(CAP_NAMES), np.int64)
+    if _lib.bale_device_caps(_p(out), out.size) != 0:
+        raise BaleError(_last_error())
+    return dict(zip(CAP_NAMES, out.tolist()))
 
 
 def version() -> str:

@@ -48,6 +48,7 @@ SIGNATURES: dict[str, tuple[object, list[object]]] = {
     # library state
     "bale_last_error": (C.c_char_p, []),
     "bale_version": (C.c_char_p, []),
+    "bale_device_caps": (C.c_int, [P64, C.c_int]),
     "bale_release_buffers": (None, []),
     # tuning knobs
     "bale_tune_set": (C.c_int, [C.c_char_p, i64]),

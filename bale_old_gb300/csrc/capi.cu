@@ -360,6 +360,28 @@ double triangle_agi_iter(int64_t *count, int64_t *sr, sparsemat_t *L, sparsemat_
   return triangle_dropin(count, sr, L);
 }
 
+int bale_device_caps(int64_t *out, int n) {
+  if (!out || n <= 0) return BALE_EINVAL;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return BALE_ECUDA;
+  const cudaDeviceAttr attrs[] = {cudaDevAttrMultiProcessorCount,
+                                  cudaDevAttrPageableMemoryAccess,
+                                  cudaDevAttrPageableMemoryAccessUsesHostPageTables,
+                                  cudaDevAttrConcurrentManagedAccess,
+                                  cudaDevAttrL2CacheSize,
+                                  cudaDevAttrMaxSharedMemoryPerBlockOptin,
+                                  cudaDevAttrCanUseHostPointerForRegisteredMem,
+                                  cudaDevAttrAsyncEngineCount,
+                                  cudaDevAttrUnifiedAddressing};
+  const int na = static_cast<int>(sizeof(attrs) / sizeof(attrs[0]));
+  for (int i = 0; i < n; i++) {
+    int v = -1;
+    if (i < na && cudaDeviceGetAttribute(&v, attrs[i], dev) != cudaSuccess) v = -1;
+    out[i] = v;
+  }
+  return BALE_OK;
+}
+
 const char *bale_last_error(void) { return t_err; }
 const char *bale_version(void) { return "bale_gb300 0.1 (sm_103a)"; }
 

@@ -115,6 +115,11 @@ BALE_API double triangle_agi_iter(int64_t *count, int64_t *sr, sparsemat_t *L, s
 /* Message describing the most recent failure on the calling thread ("" if */
 /* none).  Replaces the reference's fprintf-and-exit error paths.          */
 BALE_API const char *bale_last_error(void);
+/* Facts about the current device, out[0..n): SM count, pageable host      */
+/* memory access, ... via host page tables, concurrent managed access, L2   */
+/* bytes, opt-in shared memory per block, host pointers usable for          */
+/* registered memory, copy engines, unified addressing (-1 = unknown).      */
+BALE_API int bale_device_caps(int64_t *out, int n);
 /* Library version string. */
 BALE_API const char *bale_version(void);
 /* Release the cached device and pinned buffers the drop-ins keep between  */

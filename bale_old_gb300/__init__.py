@@ -27,7 +27,7 @@ __all__ = [
     "triangle_agi", "triangle_exstack_push", "triangle_exstack2_push",
     "triangle_convey_push", "triangle_agi_iter",
     "histo_dev", "ig_dev", "triangle_dev", "ig_dev_noalloc",
-    "splitmix64", "gen_uniform", "gen_values", "gen_negative_table", "gen_zipf",
+    "splitmix64", "gen_uniform", "gen_values", "gen_uniform_dev", "gen_values_dev", "gen_negative_table", "gen_zipf",
     "keyed_perm", "gen_rmat", "gen_erdos_renyi", "gen_kronecker", "kronecker_triangles",
     "set_host_threads", "release_buffers", "version", "pack_index",
     "tune_set", "tune_get", "tune_knobs", "device_caps",
@@ -302,6 +302,18 @@ def gen_uniform(n: int, rng: int, seed: int, packed: bool = False) -> np.ndarray
     out = np.empty(n, np.int64)
     _gen_status(_lib.bale_gen_uniform(_p(out), n, rng, seed & (2**64 - 1), int(packed)), "gen_uniform")
     return out
+
+
+def gen_uniform_dev(out, rng: int, seed: int, packed: bool = False, stream=None) -> None:
+    """gen_uniform into a device int64 tensor (same bits as the host one)."""
+    _status(_lib.bale_gen_uniform_dev(_dptr(out, "out"), out.numel(), rng, seed & (2**64 - 1), int(packed),
+                                      _stream(stream)), "bale_gen_uniform_dev")
+
+
+def gen_values_dev(out, seed: int, stream=None) -> None:
+    """gen_values into a device int64 tensor (same bits as the host one)."""
+    _status(_lib.bale_gen_values_dev(_dptr(out, "out"), out.numel(), seed & (2**64 - 1), _stream(stream)),
+            "bale_gen_values_dev")
 
 
 def gen_values(n: int, seed: int) -> np.ndarray:

@@ -27,6 +27,16 @@ class sparsemat_t(C.Structure):
 
 PSM = C.POINTER(sparsemat_t)
 
+
+class bale_instance_t(C.Structure):
+    """One instance of a batch (include/bale_gb300.h)."""
+
+    _fields_ = [("kind", C.c_int32), ("shift", C.c_int32), ("n", i64), ("m", i64),
+                ("out", VP), ("inp", VP), ("aux", VP)]
+
+
+PINST = C.POINTER(bale_instance_t)
+
 # name -> (restype, argtypes)
 SIGNATURES: dict[str, tuple[object, list[object]]] = {
     # drop-ins (apps/histo_src/histo.h:47-50)
@@ -59,11 +69,18 @@ SIGNATURES: dict[str, tuple[object, list[object]]] = {
     "bale_histo_dev": (C.c_int, [VP, i64, VP, i64, C.c_int, VP, VP]),
     "bale_ig_dev": (C.c_int, [VP, VP, i64, VP, i64, C.c_int, VP, VP]),
     "bale_triangle_dev": (C.c_int, [VP, VP, i64, i64, VP, VP, VP, VP]),
+    "bale_batch_create": (VP, [PINST, i64]),
+    "bale_batch_run": (C.c_int, [VP, VP]),
+    "bale_batch_bad": (C.c_int, [VP, P64, i64]),
+    "bale_batch_stats": (C.c_int, [VP, P64, C.c_int]),
+    "bale_batch_destroy": (None, [VP]),
     "bale_ig_dev_noalloc": (C.c_int, [VP, VP, i64, VP, i64, C.c_int, VP, VP]),
     # inputs
     "bale_splitmix64": (u64, [u64, u64]),
     "bale_gen_uniform": (C.c_int, [P64, i64, i64, u64, C.c_int]),
     "bale_gen_values": (C.c_int, [P64, i64, u64]),
+    "bale_gen_uniform_dev": (C.c_int, [VP, i64, i64, u64, C.c_int, VP]),
+    "bale_gen_values_dev": (C.c_int, [VP, i64, u64, VP]),
     "bale_gen_negative_table": (C.c_int, [P64, i64]),
     "bale_gen_zipf": (C.c_int, [P64, i64, i64, C.c_double, u64, u64, C.c_int]),
     "bale_keyed_perm": (i64, [i64, i64, u64]),

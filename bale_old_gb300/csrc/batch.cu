@@ -1,0 +1,481 @@
+// batch.cu -- hundreds of uneven histo / ig / triangle instances in one
+// persistent, CUDA-graph-captured work-queue launch.
+//
+// A plain run launches every instance's kernels separately: small instances
+// leave most of the GPU idle and every launch pays its fixed cost.  Here a
+// host planner cuts every instance into tiles (tasks) sized per kind and size
+// class (the batch.* tuning knobs, set by the autotuner), orders them
+// longest-first, and one persistent kernel -- one 512-thread block per SM,
+// 192 KiB of shared memory -- pulls tasks from a device queue until it is
+// empty:
+//
+//   histo, table <= 48 Ki counters : the task's updates are counted in a
+//                                    shared-memory copy of the table, then
+//                                    flushed with one L2 reduction per counter;
+//   histo, larger table            : plain red.global.add.u64 per update;
+//   ig                             : direct gather, 8 loads in flight/thread;
+//   triangles, light rows          : warps take rows of the task's range
+//                                    (tri_device.cuh light_row);
+//   triangles, heavy rows          : the whole block per heavy row, row i as
+//                                    a shared-memory bitmap (heavy_row).
+//
+// Instances that need the multi-pass region-partitioned algorithms (ig and
+// histo tables well beyond L2 with >= 2^20 elements) are launched as their
+// own kernels on a second captured stream, in parallel with the queue.
+// The whole run -- queue reset, the persistent kernel and those launches --
+// is one CUDA graph, replayed by bale_batch_run.
+//
+// Results match the per-instance entry points bit for bit: histo ADDS into
+// its counts, ig OVERWRITES tgt, triangles ADD their count into out[0].
+// Out-of-range indices and malformed rows are counted per instance.
+#include <algorithm>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "tri_device.cuh"
+
+namespace bale {
+
+namespace {
+
+enum TaskKind : int32_t { kHistoSmem = 0, kHistoL2 = 1, kIgDirect = 2, kTriLight = 3, kTriHeavy = 4 };
+
+struct Inst {
+  int32_t kind, shift;
+  int64_t n, m;
+  int64_t *out;
+  const int64_t *in;
+  const int64_t *aux;
+  int64_t bits;  // triangles: bitmap bits (power of two)
+};
+
+struct Task {
+  int32_t kind, inst;
+  int64_t lo, hi;
+};
+
+constexpr int kThreads = 512;
+constexpr int kWarps = kThreads / 32;
+constexpr int64_t kSmemCounters = 48 * 1024;
+constexpr size_t kSmemBytes = static_cast<size_t>(kSmemCounters) * sizeof(uint32_t);  // 192 KiB
+static_assert(kSmemBytes >= static_cast<size_t>(tri::kHeavyBits / 8), "bitmap must fit");
+static_assert(kSmemBytes >= static_cast<size_t>(kWarps) * tri::kLightCap * sizeof(uint32_t), "row slots must fit");
+
+__device__ __forceinline__ void add_bad(unsigned long long *bad, unsigned long long v) {
+  v = warp_sum_u64(v);
+  if (lane_id() == 0 && v) atomicAdd(bad, v);
+}
+
+__device__ void cta_histo_smem(const Inst &in, int64_t lo, int64_t hi, uint32_t *sm, unsigned long long *bad) {
+  const uint64_t m = static_cast<uint64_t>(in.m);
+  for (uint64_t c = threadIdx.x; c < m; c += kThreads) sm[c] = 0;
+  __syncthreads();
+  unsigned long long nb = 0;
+  for (int64_t i = lo + threadIdx.x; i < hi; i += kThreads) {
+    const uint64_t k = static_cast<uint64_t>(ld_stream(in.in + i) >> in.shift);
+    if (k < m) atomicAdd(&sm[k], 1u); else nb++;
+  }
+  __syncthreads();
+  for (uint64_t c = threadIdx.x; c < m; c += kThreads) {
+    const uint32_t v = sm[c];
+    if (v) red_add_u64(in.out + c, v);
+  }
+  add_bad(bad, nb);
+}
+
+__device__ void cta_histo_l2(const Inst &in, int64_t lo, int64_t hi, unsigned long long *bad) {
+  const uint64_t m = static_cast<uint64_t>(in.m);
+  unsigned long long nb = 0;
+  for (int64_t i = lo + threadIdx.x; i < hi; i += 4 * kThreads) {
+    int64_t r[4];
+#pragma unroll
+    for (int u = 0; u < 4; u++) r[u] = (i + u * kThreads < hi) ? ld_stream(in.in + i + u * kThreads) : -1;
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      if (i + u * kThreads < hi) {
+        const uint64_t k = static_cast<uint64_t>(r[u] >> in.shift);
+        if (k < m) red_add_u64(in.out + k, 1ull); else nb++;
+      }
+    }
+  }
+  add_bad(bad, nb);
+}
+
+__device__ void cta_ig(const Inst &in, int64_t lo, int64_t hi, unsigned long long *bad) {
+  const uint64_t m = static_cast<uint64_t>(in.m);
+  unsigned long long nb = 0;
+  constexpr int U = 8;
+  for (int64_t i = lo + threadIdx.x; i < hi; i += U * kThreads) {
+    int64_t r[U], v[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) r[u] = (i + u * kThreads < hi) ? ld_stream(in.in + i + u * kThreads) : 0;
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const uint64_t k = static_cast<uint64_t>(r[u] >> in.shift);
+      const bool live = i + u * kThreads < hi;
+      v[u] = 0;
+      if (live && k < m) v[u] = ld_table(in.aux + k);
+      else if (live) nb++;
+    }
+#pragma unroll
+    for (int u = 0; u < U; u++)
+      if (i + u * kThreads < hi) st_stream(in.out + i + u * kThreads, v[u]);
+  }
+  add_bad(bad, nb);
+}
+
+__device__ void flush_tri(const tri::Tally &t0, const Inst &in, unsigned long long *bad, unsigned long long *work) {
+  tri::Tally t = t0;
+  t.cnt = warp_sum_u64(t.cnt);
+  t.work = warp_sum_u64(t.work);
+  t.bad = warp_sum_u64(t.bad);
+  if (lane_id() == 0) {
+    if (t.cnt) atomicAdd(reinterpret_cast<unsigned long long *>(in.out), t.cnt);
+    if (t.work) atomicAdd(work, t.work);
+    if (t.bad) atomicAdd(bad, t.bad);
+  }
+}
+
+__device__ void cta_tri_light(const Inst &in, int64_t lo, int64_t hi, uint32_t *sm, unsigned long long *cursor,
+                              unsigned long long *bad, unsigned long long *work) {
+  if (threadIdx.x == 0) *cursor = static_cast<unsigned long long>(lo);
+  __syncthreads();
+  uint32_t *rb = sm + (threadIdx.x >> 5) * tri::kLightCap;
+  tri::Tally t;
+  for (;;) {
+    unsigned long long r = 0;
+    if (lane_id() == 0) r = atomicAdd(cursor, 1ull);
+    r = __shfl_sync(0xffffffffu, r, 0);
+    if (static_cast<int64_t>(r) >= hi) break;
+    tri::light_row(in.in, in.aux, static_cast<int64_t>(r), in.m, in.bits, rb, t);
+  }
+  flush_tri(t, in, bad, work);
+}
+
+__device__ void cta_tri_heavy(const Inst &in, int64_t lo, int64_t hi, uint32_t *sm, unsigned long long *bad,
+                              unsigned long long *work) {
+  const int64_t nwords = in.bits >> 5;
+  for (int64_t w = threadIdx.x; w < nwords; w += kThreads) sm[w] = 0;
+  __syncthreads();
+  tri::Tally t;
+  for (int64_t r = lo; r < hi; r++) {
+    const int64_t b = in.in[r], e = in.in[r + 1];  // the same value in every thread
+    if (!tri::is_heavy(r, b, e, in.bits)) continue;
+    tri::heavy_row<int64_t, kThreads>(in.in, in.aux, r, in.m, sm, static_cast<uint32_t>(nwords - 1), t);
+  }
+  flush_tri(t, in, bad, work);
+}
+
+__global__ void __launch_bounds__(kThreads, 1)
+    batch_kernel(const Task *__restrict__ tasks, int64_t ntasks, const Inst *__restrict__ insts,
+                 unsigned long long *__restrict__ head, unsigned long long *__restrict__ bad,
+                 unsigned long long *__restrict__ work) {
+  extern __shared__ __align__(16) uint32_t sm[];
+  __shared__ long long sel;
+  __shared__ unsigned long long row_cursor;
+  for (;;) {
+    __syncthreads();  // the previous task is finished with shared memory
+    if (threadIdx.x == 0) {
+      const unsigned long long t = atomicAdd(head, 1ull);
+      sel = t < static_cast<unsigned long long>(ntasks) ? static_cast<long long>(t) : -1ll;
+    }
+    __syncthreads();
+    const long long ti = sel;
+    if (ti < 0) break;
+    const Task tk = tasks[ti];
+    const Inst in = insts[tk.inst];
+    unsigned long long *ib = bad + tk.inst;
+    switch (tk.kind) {
+      case kHistoSmem: cta_histo_smem(in, tk.lo, tk.hi, sm, ib); break;
+      case kHistoL2: cta_histo_l2(in, tk.lo, tk.hi, ib); break;
+      case kIgDirect: cta_ig(in, tk.lo, tk.hi, ib); break;
+      case kTriLight: cta_tri_light(in, tk.lo, tk.hi, sm, &row_cursor, ib, work); break;
+      case kTriHeavy: cta_tri_heavy(in, tk.lo, tk.hi, sm, ib, work); break;
+      default: break;
+    }
+  }
+}
+
+bool g_batch_attr[64];
+
+// size class of an instance: 0 small (< 2^18 elements), 1 medium (< 2^23), 2 large
+int size_class(int64_t n) { return n < (int64_t(1) << 18) ? 0 : (n < (int64_t(1) << 23) ? 1 : 2); }
+
+int64_t tuned(const char *base, int cls, int64_t dflt) {
+  static const char *suffix[3] = {".small", ".medium", ".large"};
+  char name[64];
+  snprintf(name, sizeof(name), "%s%s", base, suffix[cls]);
+  const int64_t v = knob(name);
+  return v > 0 ? v : dflt;
+}
+
+}  // namespace
+
+}  // namespace bale
+
+struct bale_batch {
+  int device = 0;
+  int64_t count = 0;
+  std::vector<bale_instance_t> host;
+  bale::Inst *d_inst = nullptr;
+  bale::Task *d_tasks = nullptr;
+  int64_t ntasks = 0;
+  int64_t ntasks_kind[5] = {0, 0, 0, 0, 0};
+  unsigned long long *d_words = nullptr;  // [0] queue head, [1] work, [2..] standalone cursors
+  unsigned long long *d_bad = nullptr;    // per instance
+  void *d_ws = nullptr;                   // shared workspace of the standalone launches
+  std::vector<int64_t> standalone;
+  cudaStream_t s_main = nullptr, s_side = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+};
+
+namespace bale {
+namespace {
+
+void destroy(bale_batch *b) {
+  if (!b) return;
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  if (b->graph) cudaGraphDestroy(b->graph);
+  if (b->ev_fork) cudaEventDestroy(b->ev_fork);
+  if (b->ev_join) cudaEventDestroy(b->ev_join);
+  if (b->s_main) cudaStreamDestroy(b->s_main);
+  if (b->s_side) cudaStreamDestroy(b->s_side);
+  cudaFree(b->d_inst);
+  cudaFree(b->d_tasks);
+  cudaFree(b->d_words);
+  cudaFree(b->d_bad);
+  cudaFree(b->d_ws);
+  delete b;
+}
+
+bool wants_partition(const bale_instance_t &x) {
+  if (knob("batch.standalone") == 0) return false;
+  const int64_t big = int64_t(96) << 20;
+  if (x.kind == BALE_KIND_IG) return x.m * 8 > big && x.n >= (int64_t(1) << 20) && ig_part_supported(x.n, x.m);
+  if (x.kind == BALE_KIND_HISTO) return x.m * 8 > big && x.n >= (int64_t(1) << 20) && x.m <= (int64_t(1024) << 22);
+  return false;
+}
+
+bool aligned16(const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; }
+
+}  // namespace
+}  // namespace bale
+
+using namespace bale;
+
+extern "C" {
+
+bale_batch_t *bale_batch_create(const bale_instance_t *inst, int64_t count) {
+  if (count < 0 || (count > 0 && !inst)) {
+    set_error("bale_batch_create: bad arguments");
+    return nullptr;
+  }
+  bale_batch *b = new (std::nothrow) bale_batch();
+  if (!b) {
+    set_error("bale_batch_create: out of host memory");
+    return nullptr;
+  }
+  b->count = count;
+  b->host.assign(inst, inst + count);
+  if (cudaGetDevice(&b->device) != cudaSuccess) b->device = 0;
+
+  // ---- validate and build the device instance records ----
+  std::vector<Inst> di(static_cast<size_t>(count));
+  for (int64_t k = 0; k < count; k++) {
+    const bale_instance_t &x = inst[k];
+    const bool ok_kind = x.kind == BALE_KIND_HISTO || x.kind == BALE_KIND_IG || x.kind == BALE_KIND_TRIANGLES;
+    const bool ok_shift = x.shift == 0 || x.shift == 16;
+    const bool ok_ptr = x.kind == BALE_KIND_TRIANGLES
+                            ? (x.out && (x.n == 0 || x.in) && (x.m == 0 || x.aux))
+                            : (x.n == 0 || (x.in && x.out && (x.kind != BALE_KIND_IG || x.m == 0 || x.aux)));
+    if (!ok_kind || !ok_shift || x.n < 0 || x.m < 0 || !ok_ptr ||
+        (x.kind == BALE_KIND_TRIANGLES && x.n >= 0xffffffffll)) {
+      set_error("bale_batch_create: instance %lld is invalid", static_cast<long long>(k));
+      destroy(b);
+      return nullptr;
+    }
+    Inst &d = di[static_cast<size_t>(k)];
+    d.kind = x.kind;
+    d.shift = x.shift;
+    d.n = x.n;
+    d.m = x.m;
+    d.out = x.out;
+    d.in = x.in;
+    d.aux = x.aux;
+    d.bits = x.kind == BALE_KIND_TRIANGLES ? tri::bitmap_bits(x.n) : 0;
+  }
+
+  // ---- plan the queue ----
+  struct Planned {
+    Task t;
+    double cost;
+  };
+  std::vector<Planned> plan;
+  size_t ws_need = 256;
+  for (int64_t k = 0; k < count; k++) {
+    const bale_instance_t &x = inst[k];
+    if (x.n == 0) continue;
+    if (wants_partition(x) && aligned16(x.in) && aligned16(x.out)) {
+      b->standalone.push_back(k);
+      const size_t need = x.kind == BALE_KIND_IG ? ig_part_workspace_bytes(x.n, x.m)
+                                                 : histo_part_workspace_bytes(x.n, x.m);
+      ws_need = std::max(ws_need, need);
+      continue;
+    }
+    const int cls = size_class(x.n);
+    if (x.kind == BALE_KIND_HISTO) {
+      if (x.m <= kSmemCounters) {
+        // each task sees several updates per counter so the flush stays cheap
+        int64_t tile = tuned("batch.histo_tile", cls, int64_t(1) << 17);
+        tile = std::max<int64_t>(tile, 4 * x.m);
+        for (int64_t lo = 0; lo < x.n; lo += tile)
+          plan.push_back({{kHistoSmem, static_cast<int32_t>(k), lo, std::min(x.n, lo + tile)},
+                          static_cast<double>(std::min(tile, x.n - lo)) * 0.5 + static_cast<double>(x.m)});
+      } else {
+        const int64_t tile = tuned("batch.histo_l2_tile", cls, int64_t(1) << 17);
+        for (int64_t lo = 0; lo < x.n; lo += tile)
+          plan.push_back({{kHistoL2, static_cast<int32_t>(k), lo, std::min(x.n, lo + tile)},
+                          static_cast<double>(std::min(tile, x.n - lo))});
+      }
+    } else if (x.kind == BALE_KIND_IG) {
+      const int64_t tile = tuned("batch.ig_tile", cls, int64_t(1) << 17);
+      for (int64_t lo = 0; lo < x.n; lo += tile)
+        plan.push_back({{kIgDirect, static_cast<int32_t>(k), lo, std::min(x.n, lo + tile)},
+                        static_cast<double>(std::min(tile, x.n - lo)) * (x.m * 8 > (int64_t(96) << 20) ? 2.0 : 1.0)});
+    } else {
+      const int64_t lim = std::min<int64_t>(x.n, tri::bitmap_bits(x.n));
+      const int64_t hrows = tuned("batch.tri_heavy_rows", cls, 64);
+      const double per_row = static_cast<double>(x.m) / static_cast<double>(x.n > 0 ? x.n : 1);
+      for (int64_t lo = 0; lo < lim; lo += hrows)
+        plan.push_back({{kTriHeavy, static_cast<int32_t>(k), lo, std::min(lim, lo + hrows)},
+                        per_row * per_row * 64.0 * static_cast<double>(hrows)});
+      const int64_t lrows = tuned("batch.tri_light_rows", cls, 2048);
+      for (int64_t lo = 0; lo < x.n; lo += lrows)
+        plan.push_back({{kTriLight, static_cast<int32_t>(k), lo, std::min(x.n, lo + lrows)},
+                        per_row * 8.0 * static_cast<double>(std::min(lrows, x.n - lo))});
+    }
+  }
+  // longest first, keeping each instance's tasks together within a cost tier
+  std::stable_sort(plan.begin(), plan.end(), [](const Planned &a, const Planned &c) { return a.cost > c.cost; });
+  std::vector<Task> tasks;
+  tasks.reserve(plan.size());
+  for (auto &p : plan) {
+    tasks.push_back(p.t);
+    b->ntasks_kind[p.t.kind]++;
+  }
+  b->ntasks = static_cast<int64_t>(tasks.size());
+
+  // ---- device state ----
+  const size_t nw = 2 + b->standalone.size() + 1;
+#define BATCH_CUDA(expr)                                                                  \
+  do {                                                                                    \
+    cudaError_t _e = (expr);                                                              \
+    if (_e != cudaSuccess) {                                                              \
+      set_error("bale_batch_create: %s failed: %s", #expr, cudaGetErrorString(_e));       \
+      cudaGetLastError();                                                                 \
+      destroy(b);                                                                         \
+      return nullptr;                                                                     \
+    }                                                                                     \
+  } while (0)
+  BATCH_CUDA(cudaMalloc(&b->d_inst, sizeof(Inst) * std::max<size_t>(1, di.size())));
+  BATCH_CUDA(cudaMalloc(&b->d_tasks, sizeof(Task) * std::max<size_t>(1, tasks.size())));
+  BATCH_CUDA(cudaMalloc(&b->d_words, sizeof(unsigned long long) * nw));
+  BATCH_CUDA(cudaMalloc(&b->d_bad, sizeof(unsigned long long) * std::max<int64_t>(1, count)));
+  if (!b->standalone.empty()) BATCH_CUDA(cudaMalloc(&b->d_ws, ws_need));
+  if (!di.empty()) BATCH_CUDA(cudaMemcpy(b->d_inst, di.data(), sizeof(Inst) * di.size(), cudaMemcpyHostToDevice));
+  if (!tasks.empty())
+    BATCH_CUDA(cudaMemcpy(b->d_tasks, tasks.data(), sizeof(Task) * tasks.size(), cudaMemcpyHostToDevice));
+  BATCH_CUDA(cudaMemset(b->d_words, 0, sizeof(unsigned long long) * nw));
+  BATCH_CUDA(cudaMemset(b->d_bad, 0, sizeof(unsigned long long) * std::max<int64_t>(1, count)));
+  const int dev = b->device;
+  if (dev >= 0 && dev < 64 && !g_batch_attr[dev]) {
+    BATCH_CUDA(cudaFuncSetAttribute(batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    static_cast<int>(kSmemBytes)));
+    g_batch_attr[dev] = true;
+  }
+  int occ = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, batch_kernel, kThreads, kSmemBytes) != cudaSuccess || occ < 1)
+    occ = 1;
+  int64_t blocks = static_cast<int64_t>(num_sms()) * occ;
+  if (blocks > b->ntasks) blocks = std::max<int64_t>(1, b->ntasks);
+
+  // ---- capture the run as a graph: queue reset, persistent kernel, and the
+  // standalone partitioned launches on a second stream ----
+  BATCH_CUDA(cudaStreamCreateWithFlags(&b->s_main, cudaStreamNonBlocking));
+  BATCH_CUDA(cudaStreamCreateWithFlags(&b->s_side, cudaStreamNonBlocking));
+  BATCH_CUDA(cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming));
+  BATCH_CUDA(cudaEventCreateWithFlags(&b->ev_join, cudaEventDisableTiming));
+  BATCH_CUDA(cudaStreamBeginCapture(b->s_main, cudaStreamCaptureModeThreadLocal));
+  bool cap_ok = true;
+  cap_ok &= cudaMemsetAsync(b->d_words, 0, 2 * sizeof(unsigned long long), b->s_main) == cudaSuccess;
+  cap_ok &= cudaMemsetAsync(b->d_bad, 0, sizeof(unsigned long long) * std::max<int64_t>(1, count), b->s_main) ==
+            cudaSuccess;
+  if (!b->standalone.empty()) {
+    cap_ok &= cudaEventRecord(b->ev_fork, b->s_main) == cudaSuccess;
+    cap_ok &= cudaStreamWaitEvent(b->s_side, b->ev_fork, 0) == cudaSuccess;
+    for (size_t s = 0; s < b->standalone.size() && cap_ok; s++) {
+      const int64_t k = b->standalone[s];
+      const bale_instance_t &x = inst[k];
+      unsigned long long *cur = b->d_words + 2 + s;
+      int rc = x.kind == BALE_KIND_IG
+                   ? launch_ig_partitioned(x.out, x.in, x.n, x.aux, x.m, x.shift, b->d_bad + k, b->d_ws, cur,
+                                           b->s_side)
+                   : launch_histo_partitioned(x.out, x.m, x.in, x.n, x.shift, b->d_bad + k, b->d_ws, cur, b->s_side);
+      cap_ok &= rc == BALE_OK;
+    }
+    cap_ok &= cudaEventRecord(b->ev_join, b->s_side) == cudaSuccess;
+  }
+  if (b->ntasks > 0) {
+    batch_kernel<<<static_cast<unsigned>(blocks), kThreads, kSmemBytes, b->s_main>>>(
+        b->d_tasks, b->ntasks, b->d_inst, b->d_words, b->d_bad, b->d_words + 1);
+    cap_ok &= cudaGetLastError() == cudaSuccess;
+  }
+  if (!b->standalone.empty()) cap_ok &= cudaStreamWaitEvent(b->s_main, b->ev_join, 0) == cudaSuccess;
+  cudaError_t ce = cudaStreamEndCapture(b->s_main, &b->graph);
+  if (!cap_ok || ce != cudaSuccess || !b->graph) {
+    set_error("bale_batch_create: graph capture failed: %s", cudaGetErrorString(ce != cudaSuccess ? ce : cudaGetLastError()));
+    cudaGetLastError();
+    destroy(b);
+    return nullptr;
+  }
+  BATCH_CUDA(cudaGraphInstantiate(&b->exec, b->graph, 0));
+#undef BATCH_CUDA
+  return b;
+}
+
+int bale_batch_run(bale_batch_t *b, void *stream) {
+  if (!b || !b->exec) {
+    set_error("bale_batch_run: no batch");
+    return BALE_EINVAL;
+  }
+  BALE_CUDA_OK(cudaGraphLaunch(b->exec, static_cast<cudaStream_t>(stream)));
+  return BALE_OK;
+}
+
+int bale_batch_bad(bale_batch_t *b, int64_t *bad, int64_t count) {
+  if (!b || !bad || count != b->count) {
+    set_error("bale_batch_bad: bad arguments");
+    return BALE_EINVAL;
+  }
+  if (count == 0) return BALE_OK;
+  BALE_CUDA_OK(cudaMemcpy(bad, b->d_bad, sizeof(int64_t) * static_cast<size_t>(count), cudaMemcpyDeviceToHost));
+  return BALE_OK;
+}
+
+int bale_batch_stats(bale_batch_t *b, int64_t *out, int n) {
+  if (!b || !out || n <= 0) return BALE_EINVAL;
+  const int64_t v[8] = {b->ntasks,          b->ntasks_kind[kHistoSmem], b->ntasks_kind[kHistoL2],
+                        b->ntasks_kind[kIgDirect], b->ntasks_kind[kTriLight], b->ntasks_kind[kTriHeavy],
+                        static_cast<int64_t>(b->standalone.size()), b->count};
+  for (int i = 0; i < n; i++) out[i] = i < 8 ? v[i] : -1;
+  return BALE_OK;
+}
+
+void bale_batch_destroy(bale_batch_t *b) { destroy(b); }
+
+}  // extern "C"

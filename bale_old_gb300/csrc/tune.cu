@@ -30,6 +30,22 @@ Knob g_knobs[] = {
     {"histo.blocks_per_sm", -1},
     {"histo.smem_updates_per_counter", -1},  // updates per counter per block (shared-memory mode)
     {"tri.rows_per_fetch", -1}, // rows claimed per cursor increment
+    {"batch.standalone", -1},   // 0: every instance in the work queue; -1/1: partitioned kernels for big tables
+    {"batch.histo_tile.small", -1},
+    {"batch.histo_tile.medium", -1},
+    {"batch.histo_tile.large", -1},
+    {"batch.histo_l2_tile.small", -1},
+    {"batch.histo_l2_tile.medium", -1},
+    {"batch.histo_l2_tile.large", -1},
+    {"batch.ig_tile.small", -1},
+    {"batch.ig_tile.medium", -1},
+    {"batch.ig_tile.large", -1},
+    {"batch.tri_heavy_rows.small", -1},
+    {"batch.tri_heavy_rows.medium", -1},
+    {"batch.tri_heavy_rows.large", -1},
+    {"batch.tri_light_rows.small", -1},
+    {"batch.tri_light_rows.medium", -1},
+    {"batch.tri_light_rows.large", -1},
     {"tri.mode", -1},           // 0 warp-per-row merge for every row, 1 bitmap/search hybrid
 };
 std::mutex g_mu;

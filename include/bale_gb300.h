@@ -157,6 +157,39 @@ BALE_API int bale_triangle_dev(const int64_t *d_offset, const int64_t *d_nonzero
                       int64_t nnz, int64_t *d_count, int64_t *d_work, int64_t *d_bad,
                       void *stream);
 
+/* ======================= batched execution ============================== */
+/* Many instances of uneven size in one CUDA graph: a persistent work-queue  */
+/* kernel takes tiles of every instance (tile sizes per kind and size class  */
+/* from the batch.* tuning knobs); ig/histo instances big enough for the     */
+/* region-partitioned kernels run beside it on a second captured stream.     */
+/* Create once (plans tasks, allocates the queue, captures the graph), run   */
+/* any number of times, destroy.  Results equal the per-instance entry       */
+/* points: histo ADDS into counts, ig OVERWRITES tgt, triangles ADD their     */
+/* count into out[0].  The instances' device buffers must stay valid while   */
+/* the batch exists.  New entry points; the reference has no batched form.   */
+enum { BALE_KIND_HISTO = 0, BALE_KIND_IG = 1, BALE_KIND_TRIANGLES = 2 };
+typedef struct bale_instance {
+  int32_t kind;        /* BALE_KIND_* */
+  int32_t shift;       /* 0, or 16 for the packed (index << 16) | pe form */
+  int64_t n;           /* histo: updates; ig: requests; triangles: numrows */
+  int64_t m;           /* histo: counters; ig: table entries; triangles: nnz */
+  int64_t *out;        /* histo: counts; ig: tgt; triangles: one int64 */
+  const int64_t *in;   /* histo, ig: index; triangles: row offsets[n+1] */
+  const int64_t *aux;  /* ig: table; triangles: nonzeros[m]; histo: unused */
+} bale_instance_t;
+typedef struct bale_batch bale_batch_t;
+/* NULL on failure (bale_last_error()). */
+BALE_API bale_batch_t *bale_batch_create(const bale_instance_t *inst, int64_t count);
+/* Launch the captured graph on stream (asynchronous). */
+BALE_API int bale_batch_run(bale_batch_t *b, void *stream);
+/* Out-of-range indices / malformed rows of the last run, per instance      */
+/* (synchronous copy; count must equal the batch's instance count).         */
+BALE_API int bale_batch_bad(bale_batch_t *b, int64_t *bad, int64_t count);
+/* out[0..n): tasks, per-kind task counts (histo shared-memory, histo L2,   */
+/* ig, triangle light, triangle heavy), standalone instances, instances.     */
+BALE_API int bale_batch_stats(bale_batch_t *b, int64_t *out, int n);
+BALE_API void bale_batch_destroy(bale_batch_t *b);
+
 /* ======================= no-allocation gather =========================== */
 /* No counterpart in the reference: an addition for callers that cannot      */
 /* allocate device memory when they call (HBM already reserved by another    */

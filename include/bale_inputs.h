@@ -76,6 +76,12 @@ BALE_API int64_t bale_kronecker_triangles(int mode, const int64_t *specs, int64_
 BALE_API sparsemat_t *bale_make_matrix(int64_t numrows, int64_t numcols, int64_t nnz);
 BALE_API void bale_free_matrix(sparsemat_t *m);
 
+/* Device versions (asynchronous on stream; output in device memory), bit-  */
+/* identical to bale_gen_uniform / bale_gen_values.                          */
+BALE_API int bale_gen_uniform_dev(int64_t *d_out, int64_t n, int64_t range, uint64_t seed, int packed,
+                                  void *stream);
+BALE_API int bale_gen_values_dev(int64_t *d_out, int64_t n, uint64_t seed, void *stream);
+
 /* Threads the generators may use (<= 0: all online CPUs).  Default: all. */
 BALE_API void bale_set_host_threads(int nthreads);
 

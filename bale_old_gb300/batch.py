@@ -24,7 +24,7 @@ from ._lib import bale_instance_t
 
 HISTO, IG, TRIANGLES = 0, 1, 2
 STAT_NAMES = ("tasks", "tasks_histo_smem", "tasks_histo_l2", "tasks_ig", "tasks_tri_light", "tasks_tri_heavy",
-              "standalone_instances", "instances")
+              "standalone_instances", "instances", "side_streams")
 
 
 @dataclass

@@ -219,17 +219,18 @@ int64_t tuned(const char *base, int cls, int64_t dflt) {
 struct bale_batch {
   int device = 0;
   int64_t count = 0;
-  std::vector<bale_instance_t> host;
   bale::Inst *d_inst = nullptr;
   bale::Task *d_tasks = nullptr;
   int64_t ntasks = 0;
   int64_t ntasks_kind[5] = {0, 0, 0, 0, 0};
-  unsigned long long *d_words = nullptr;  // [0] queue head, [1] work, [2..] standalone cursors
+  unsigned long long *d_words = nullptr;  // [0] queue head, [1] work, then 4 words per standalone instance
   unsigned long long *d_bad = nullptr;    // per instance
-  void *d_ws = nullptr;                   // shared workspace of the standalone launches
+  void *d_ws = nullptr;                   // workspaces of the standalone instances, one region each
   std::vector<int64_t> standalone;
-  cudaStream_t s_main = nullptr, s_side = nullptr;
-  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  cudaStream_t s_main = nullptr;
+  std::vector<cudaStream_t> s_side;
+  cudaEvent_t ev_fork = nullptr;
+  std::vector<cudaEvent_t> ev_join;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
 };
@@ -242,9 +243,9 @@ void destroy(bale_batch *b) {
   if (b->exec) cudaGraphExecDestroy(b->exec);
   if (b->graph) cudaGraphDestroy(b->graph);
   if (b->ev_fork) cudaEventDestroy(b->ev_fork);
-  if (b->ev_join) cudaEventDestroy(b->ev_join);
+  for (auto e : b->ev_join) cudaEventDestroy(e);
   if (b->s_main) cudaStreamDestroy(b->s_main);
-  if (b->s_side) cudaStreamDestroy(b->s_side);
+  for (auto st : b->s_side) cudaStreamDestroy(st);
   cudaFree(b->d_inst);
   cudaFree(b->d_tasks);
   cudaFree(b->d_words);
@@ -253,15 +254,57 @@ void destroy(bale_batch *b) {
   delete b;
 }
 
-bool wants_partition(const bale_instance_t &x) {
-  if (knob("batch.standalone") == 0) return false;
+bool aligned16(const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; }
+
+// Would this instance use the region-partitioned kernels on its own?
+bool partition_worthy(const bale_instance_t &x) {
   const int64_t big = int64_t(96) << 20;
+  if (!aligned16(x.in) || !aligned16(x.out)) return false;
   if (x.kind == BALE_KIND_IG) return x.m * 8 > big && x.n >= (int64_t(1) << 20) && ig_part_supported(x.n, x.m);
   if (x.kind == BALE_KIND_HISTO) return x.m * 8 > big && x.n >= (int64_t(1) << 20) && x.m <= (int64_t(1024) << 22);
   return false;
 }
 
-bool aligned16(const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; }
+// Instances large enough to fill the GPU by themselves run as their own
+// kernels (the same ones the per-instance entry points use) on side streams
+// of the graph; the work queue takes the rest.
+bool goes_standalone(const bale_instance_t &x) {
+  if (knob("batch.standalone") == 0 || x.n == 0) return false;
+  if (partition_worthy(x)) return true;
+  if (x.kind == BALE_KIND_TRIANGLES) {
+    const int64_t min_e = knob("batch.standalone_min_edges") > 0 ? knob("batch.standalone_min_edges") : int64_t(1) << 21;
+    return x.m >= min_e;
+  }
+  const int64_t min_n = knob("batch.standalone_min") > 0 ? knob("batch.standalone_min") : int64_t(1) << 23;
+  return x.n >= min_n;
+}
+
+size_t standalone_ws(const bale_instance_t &x) {
+  size_t need = 0;
+  if (x.kind == BALE_KIND_IG && partition_worthy(x)) need = ig_part_workspace_bytes(x.n, x.m);
+  else if (x.kind == BALE_KIND_HISTO && partition_worthy(x)) need = histo_part_workspace_bytes(x.n, x.m);
+  else if (x.kind == BALE_KIND_TRIANGLES) need = tri_hybrid_workspace_bytes(x.n, x.m);
+  return (need + 255) & ~size_t(255);
+}
+
+double standalone_cost(const bale_instance_t &x) {
+  if (x.kind == BALE_KIND_TRIANGLES) return 30.0 * static_cast<double>(x.m);
+  return static_cast<double>(x.n) * (x.kind == BALE_KIND_IG ? 1.5 : 1.0);
+}
+
+int launch_standalone(const bale_instance_t &x, unsigned long long *bad, void *ws, unsigned long long *words,
+                      cudaStream_t st) {
+  if (x.kind == BALE_KIND_IG) {
+    if (partition_worthy(x)) return launch_ig_partitioned(x.out, x.in, x.n, x.aux, x.m, x.shift, bad, ws, words, st);
+    return launch_ig(x.out, x.in, x.n, x.aux, x.m, x.shift, bad, st);
+  }
+  if (x.kind == BALE_KIND_HISTO) {
+    if (partition_worthy(x)) return launch_histo_partitioned(x.out, x.m, x.in, x.n, x.shift, bad, ws, words, st);
+    return launch_histo(x.out, x.m, x.in, x.n, x.shift, bad, st);
+  }
+  return launch_triangle_hybrid(x.in, x.aux, x.n, x.m, reinterpret_cast<unsigned long long *>(x.out), nullptr, bad,
+                                ws, words, 8, st);
+}
 
 }  // namespace
 }  // namespace bale
@@ -281,8 +324,17 @@ bale_batch_t *bale_batch_create(const bale_instance_t *inst, int64_t count) {
     return nullptr;
   }
   b->count = count;
-  b->host.assign(inst, inst + count);
   if (cudaGetDevice(&b->device) != cudaSuccess) b->device = 0;
+#define BATCH_CUDA(expr)                                                                  \
+  do {                                                                                    \
+    cudaError_t _e = (expr);                                                              \
+    if (_e != cudaSuccess) {                                                              \
+      set_error("bale_batch_create: %s failed: %s", #expr, cudaGetErrorString(_e));       \
+      cudaGetLastError();                                                                 \
+      destroy(b);                                                                         \
+      return nullptr;                                                                     \
+    }                                                                                     \
+  } while (0)
 
   // ---- validate and build the device instance records ----
   std::vector<Inst> di(static_cast<size_t>(count));
@@ -310,24 +362,25 @@ bale_batch_t *bale_batch_create(const bale_instance_t *inst, int64_t count) {
     d.bits = x.kind == BALE_KIND_TRIANGLES ? tri::bitmap_bits(x.n) : 0;
   }
 
-  // ---- plan the queue ----
+  // ---- plan: standalone instances, then the work queue ----
   struct Planned {
     Task t;
     double cost;
   };
   std::vector<Planned> plan;
-  size_t ws_need = 256;
+  std::vector<size_t> ws_off;
+  size_t ws_total = 256;
+  std::vector<int64_t> host_off;
   for (int64_t k = 0; k < count; k++) {
     const bale_instance_t &x = inst[k];
     if (x.n == 0) continue;
-    if (wants_partition(x) && aligned16(x.in) && aligned16(x.out)) {
+    if (goes_standalone(x)) {
       b->standalone.push_back(k);
-      const size_t need = x.kind == BALE_KIND_IG ? ig_part_workspace_bytes(x.n, x.m)
-                                                 : histo_part_workspace_bytes(x.n, x.m);
-      ws_need = std::max(ws_need, need);
+      ws_off.push_back(ws_total);
+      ws_total += standalone_ws(x);
       continue;
     }
-    const int cls = size_class(x.n);
+    const int cls = size_class(x.kind == BALE_KIND_TRIANGLES ? x.m : x.n);
     if (x.kind == BALE_KIND_HISTO) {
       if (x.m <= kSmemCounters) {
         // each task sees several updates per counter so the flush stays cheap
@@ -348,19 +401,50 @@ bale_batch_t *bale_batch_create(const bale_instance_t *inst, int64_t count) {
         plan.push_back({{kIgDirect, static_cast<int32_t>(k), lo, std::min(x.n, lo + tile)},
                         static_cast<double>(std::min(tile, x.n - lo)) * (x.m * 8 > (int64_t(96) << 20) ? 2.0 : 1.0)});
     } else {
-      const int64_t lim = std::min<int64_t>(x.n, tri::bitmap_bits(x.n));
-      const int64_t hrows = tuned("batch.tri_heavy_rows", cls, 64);
-      const double per_row = static_cast<double>(x.m) / static_cast<double>(x.n > 0 ? x.n : 1);
-      for (int64_t lo = 0; lo < lim; lo += hrows)
-        plan.push_back({{kTriHeavy, static_cast<int32_t>(k), lo, std::min(lim, lo + hrows)},
-                        per_row * per_row * 64.0 * static_cast<double>(hrows)});
-      const int64_t lrows = tuned("batch.tri_light_rows", cls, 2048);
-      for (int64_t lo = 0; lo < x.n; lo += lrows)
-        plan.push_back({{kTriLight, static_cast<int32_t>(k), lo, std::min(x.n, lo + lrows)},
-                        per_row * 8.0 * static_cast<double>(std::min(lrows, x.n - lo))});
+      // Row degrees are known exactly and cheaply: read the offsets once and
+      // give every heavy row its own task; cut the light rows into tasks of
+      // about the same number of nonzeros.
+      host_off.resize(static_cast<size_t>(x.n + 1));
+      BATCH_CUDA(cudaMemcpy(host_off.data(), x.in, sizeof(int64_t) * static_cast<size_t>(x.n + 1),
+                            cudaMemcpyDeviceToHost));
+      const int64_t bits = tri::bitmap_bits(x.n);
+      const int64_t lim = std::min<int64_t>(x.n, bits);
+      const double avg = static_cast<double>(x.m) / static_cast<double>(x.n);
+      const int64_t hrows = tuned("batch.tri_heavy_rows", cls, 1);
+      for (int64_t i = 0; i < lim;) {
+        const int64_t d = host_off[i + 1] - host_off[i];
+        if (i < lim && d >= tri::kHeavyMinDeg) {
+          int64_t j = i, nh = 0;
+          double c = 0;
+          while (j < lim && nh < hrows) {
+            const int64_t dj = host_off[j + 1] - host_off[j];
+            if (dj >= tri::kHeavyMinDeg) {
+              c += static_cast<double>(dj) * 4.0 * avg;
+              nh++;
+            }
+            j++;
+          }
+          plan.push_back({{kTriHeavy, static_cast<int32_t>(k), i, j}, c});
+          i = j;
+        } else {
+          i++;
+        }
+      }
+      const int64_t lnnz = tuned("batch.tri_light_rows", cls, 1 << 15);  // nonzeros per light task
+      int64_t lo = 0;
+      while (lo < x.n) {
+        int64_t hi = lo;
+        int64_t acc = 0;
+        while (hi < x.n && (hi == lo || acc < lnnz)) {
+          acc += host_off[hi + 1] - host_off[hi];
+          hi++;
+        }
+        plan.push_back({{kTriLight, static_cast<int32_t>(k), lo, hi}, static_cast<double>(acc) * 2.0 * avg + 64.0});
+        lo = hi;
+      }
     }
   }
-  // longest first, keeping each instance's tasks together within a cost tier
+  // longest first
   std::stable_sort(plan.begin(), plan.end(), [](const Planned &a, const Planned &c) { return a.cost > c.cost; });
   std::vector<Task> tasks;
   tasks.reserve(plan.size());
@@ -371,22 +455,12 @@ bale_batch_t *bale_batch_create(const bale_instance_t *inst, int64_t count) {
   b->ntasks = static_cast<int64_t>(tasks.size());
 
   // ---- device state ----
-  const size_t nw = 2 + b->standalone.size() + 1;
-#define BATCH_CUDA(expr)                                                                  \
-  do {                                                                                    \
-    cudaError_t _e = (expr);                                                              \
-    if (_e != cudaSuccess) {                                                              \
-      set_error("bale_batch_create: %s failed: %s", #expr, cudaGetErrorString(_e));       \
-      cudaGetLastError();                                                                 \
-      destroy(b);                                                                         \
-      return nullptr;                                                                     \
-    }                                                                                     \
-  } while (0)
+  const size_t nw = 2 + 4 * b->standalone.size();
   BATCH_CUDA(cudaMalloc(&b->d_inst, sizeof(Inst) * std::max<size_t>(1, di.size())));
   BATCH_CUDA(cudaMalloc(&b->d_tasks, sizeof(Task) * std::max<size_t>(1, tasks.size())));
   BATCH_CUDA(cudaMalloc(&b->d_words, sizeof(unsigned long long) * nw));
   BATCH_CUDA(cudaMalloc(&b->d_bad, sizeof(unsigned long long) * std::max<int64_t>(1, count)));
-  if (!b->standalone.empty()) BATCH_CUDA(cudaMalloc(&b->d_ws, ws_need));
+  if (!b->standalone.empty()) BATCH_CUDA(cudaMalloc(&b->d_ws, ws_total));
   if (!di.empty()) BATCH_CUDA(cudaMemcpy(b->d_inst, di.data(), sizeof(Inst) * di.size(), cudaMemcpyHostToDevice));
   if (!tasks.empty())
     BATCH_CUDA(cudaMemcpy(b->d_tasks, tasks.data(), sizeof(Task) * tasks.size(), cudaMemcpyHostToDevice));
@@ -402,43 +476,78 @@ bale_batch_t *bale_batch_create(const bale_instance_t *inst, int64_t count) {
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, batch_kernel, kThreads, kSmemBytes) != cudaSuccess || occ < 1)
     occ = 1;
   int64_t blocks = static_cast<int64_t>(num_sms()) * occ;
+  const int64_t qb = knob("batch.queue_blocks");
+  if (qb > 0 && qb < blocks) blocks = qb;
   if (blocks > b->ntasks) blocks = std::max<int64_t>(1, b->ntasks);
 
-  // ---- capture the run as a graph: queue reset, persistent kernel, and the
-  // standalone partitioned launches on a second stream ----
+  // side streams for the standalone instances, longest first to the least loaded
+  int64_t nside = knob("batch.streams") > 0 ? knob("batch.streams") : 4;
+  nside = std::min<int64_t>(nside, static_cast<int64_t>(b->standalone.size()));
+  std::vector<int> lane(b->standalone.size(), 0);
+  {
+    std::vector<size_t> order(b->standalone.size());
+    for (size_t s = 0; s < order.size(); s++) order[s] = s;
+    std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t c) {
+      return standalone_cost(inst[b->standalone[a]]) > standalone_cost(inst[b->standalone[c]]);
+    });
+    std::vector<double> load(static_cast<size_t>(std::max<int64_t>(1, nside)), 0.0);
+    std::vector<size_t> reordered;
+    for (size_t s : order) {
+      const size_t l = static_cast<size_t>(std::min_element(load.begin(), load.end()) - load.begin());
+      lane[s] = static_cast<int>(l);
+      load[l] += standalone_cost(inst[b->standalone[s]]);
+      reordered.push_back(s);
+    }
+    // launch in longest-first order within each lane
+    std::vector<int64_t> st2;
+    std::vector<size_t> off2;
+    std::vector<int> lane2;
+    for (size_t s : reordered) {
+      st2.push_back(b->standalone[s]);
+      off2.push_back(ws_off[s]);
+      lane2.push_back(lane[s]);
+    }
+    b->standalone.swap(st2);
+    ws_off.swap(off2);
+    lane.swap(lane2);
+  }
+
+  // ---- capture one run as a graph ----
   BATCH_CUDA(cudaStreamCreateWithFlags(&b->s_main, cudaStreamNonBlocking));
-  BATCH_CUDA(cudaStreamCreateWithFlags(&b->s_side, cudaStreamNonBlocking));
   BATCH_CUDA(cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming));
-  BATCH_CUDA(cudaEventCreateWithFlags(&b->ev_join, cudaEventDisableTiming));
+  for (int64_t l = 0; l < nside; l++) {
+    cudaStream_t st = nullptr;
+    cudaEvent_t ev = nullptr;
+    BATCH_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    b->s_side.push_back(st);
+    BATCH_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    b->ev_join.push_back(ev);
+  }
   BATCH_CUDA(cudaStreamBeginCapture(b->s_main, cudaStreamCaptureModeThreadLocal));
   bool cap_ok = true;
   cap_ok &= cudaMemsetAsync(b->d_words, 0, 2 * sizeof(unsigned long long), b->s_main) == cudaSuccess;
   cap_ok &= cudaMemsetAsync(b->d_bad, 0, sizeof(unsigned long long) * std::max<int64_t>(1, count), b->s_main) ==
             cudaSuccess;
-  if (!b->standalone.empty()) {
+  if (nside > 0) {
     cap_ok &= cudaEventRecord(b->ev_fork, b->s_main) == cudaSuccess;
-    cap_ok &= cudaStreamWaitEvent(b->s_side, b->ev_fork, 0) == cudaSuccess;
+    for (int64_t l = 0; l < nside; l++) cap_ok &= cudaStreamWaitEvent(b->s_side[l], b->ev_fork, 0) == cudaSuccess;
     for (size_t s = 0; s < b->standalone.size() && cap_ok; s++) {
       const int64_t k = b->standalone[s];
-      const bale_instance_t &x = inst[k];
-      unsigned long long *cur = b->d_words + 2 + s;
-      int rc = x.kind == BALE_KIND_IG
-                   ? launch_ig_partitioned(x.out, x.in, x.n, x.aux, x.m, x.shift, b->d_bad + k, b->d_ws, cur,
-                                           b->s_side)
-                   : launch_histo_partitioned(x.out, x.m, x.in, x.n, x.shift, b->d_bad + k, b->d_ws, cur, b->s_side);
-      cap_ok &= rc == BALE_OK;
+      void *ws = static_cast<char *>(b->d_ws) + ws_off[s];
+      cap_ok &= launch_standalone(inst[k], b->d_bad + k, ws, b->d_words + 2 + 4 * s, b->s_side[lane[s]]) == BALE_OK;
     }
-    cap_ok &= cudaEventRecord(b->ev_join, b->s_side) == cudaSuccess;
+    for (int64_t l = 0; l < nside; l++) cap_ok &= cudaEventRecord(b->ev_join[l], b->s_side[l]) == cudaSuccess;
   }
   if (b->ntasks > 0) {
     batch_kernel<<<static_cast<unsigned>(blocks), kThreads, kSmemBytes, b->s_main>>>(
         b->d_tasks, b->ntasks, b->d_inst, b->d_words, b->d_bad, b->d_words + 1);
     cap_ok &= cudaGetLastError() == cudaSuccess;
   }
-  if (!b->standalone.empty()) cap_ok &= cudaStreamWaitEvent(b->s_main, b->ev_join, 0) == cudaSuccess;
+  for (int64_t l = 0; l < nside; l++) cap_ok &= cudaStreamWaitEvent(b->s_main, b->ev_join[l], 0) == cudaSuccess;
   cudaError_t ce = cudaStreamEndCapture(b->s_main, &b->graph);
   if (!cap_ok || ce != cudaSuccess || !b->graph) {
-    set_error("bale_batch_create: graph capture failed: %s", cudaGetErrorString(ce != cudaSuccess ? ce : cudaGetLastError()));
+    set_error("bale_batch_create: graph capture failed: %s",
+              cudaGetErrorString(ce != cudaSuccess ? ce : cudaGetLastError()));
     cudaGetLastError();
     destroy(b);
     return nullptr;
@@ -469,10 +578,16 @@ int bale_batch_bad(bale_batch_t *b, int64_t *bad, int64_t count) {
 
 int bale_batch_stats(bale_batch_t *b, int64_t *out, int n) {
   if (!b || !out || n <= 0) return BALE_EINVAL;
-  const int64_t v[8] = {b->ntasks,          b->ntasks_kind[kHistoSmem], b->ntasks_kind[kHistoL2],
-                        b->ntasks_kind[kIgDirect], b->ntasks_kind[kTriLight], b->ntasks_kind[kTriHeavy],
-                        static_cast<int64_t>(b->standalone.size()), b->count};
-  for (int i = 0; i < n; i++) out[i] = i < 8 ? v[i] : -1;
+  const int64_t v[9] = {b->ntasks,
+                        b->ntasks_kind[kHistoSmem],
+                        b->ntasks_kind[kHistoL2],
+                        b->ntasks_kind[kIgDirect],
+                        b->ntasks_kind[kTriLight],
+                        b->ntasks_kind[kTriHeavy],
+                        static_cast<int64_t>(b->standalone.size()),
+                        b->count,
+                        static_cast<int64_t>(b->s_side.size())};
+  for (int i = 0; i < n; i++) out[i] = i < 9 ? v[i] : -1;
   return BALE_OK;
 }
 

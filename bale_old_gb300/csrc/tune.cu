@@ -30,7 +30,11 @@ Knob g_knobs[] = {
     {"histo.blocks_per_sm", -1},
     {"histo.smem_updates_per_counter", -1},  // updates per counter per block (shared-memory mode)
     {"tri.rows_per_fetch", -1}, // rows claimed per cursor increment
-    {"batch.standalone", -1},   // 0: every instance in the work queue; -1/1: partitioned kernels for big tables
+    {"batch.standalone", -1},   // 0: every instance in the work queue; -1/1: large instances run their own kernels
+    {"batch.standalone_min", -1},        // histo/ig elements from which an instance runs standalone (2^23)
+    {"batch.standalone_min_edges", -1},  // triangle nonzeros from which a graph runs standalone (2^21)
+    {"batch.streams", -1},               // side streams for standalone instances (4)
+    {"batch.queue_blocks", -1},          // blocks of the persistent queue kernel (one per SM)
     {"batch.histo_tile.small", -1},
     {"batch.histo_tile.medium", -1},
     {"batch.histo_tile.large", -1},

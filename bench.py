@@ -11,7 +11,10 @@ over its whole synthetic input (seeded SplitMix64 streams; R-MAT graph):
 * ig_zipf   : same table, requests Zipf(1.1) over a keyed permutation;
 * histo     : 10^7 uniform updates into 10^6 int64 counters -> GUP/s;
 * triangles : R-MAT scale 22, edge factor 16, (0.57,0.19,0.19,0.05),
-            symmetrised, degree-ordered strictly lower L -> edges/s (nnz(L)/s).
+            symmetrised, degree-ordered strictly lower L -> edges/s (nnz(L)/s);
+* batch     : the uneven 512-instance mix (256 histo, 192 ig, 64 R-MAT
+            triangle instances) in one CUDA graph, against the same instances
+            launched one by one -> G items/s (updates + requests + edges).
 
 The headline workload fills the top-level keys; unless --only is given the
 other three are measured in the same run and reported under "workloads".
@@ -379,6 +382,118 @@ def run_triangles(ctx) -> dict:
     return out
 
 
+MIX_FULL = {"histo_t": (1_000, 16 << 20), "histo_n": (10_000, 64 << 20), "ig_t": (1_000, 64 << 20),
+            "ig_n": (10_000, 128 << 20), "scales": (10, 20)}
+MIX_SMALL = {"histo_t": (1_000, 1 << 20), "histo_n": (10_000, 1 << 20), "ig_t": (1_000, 4 << 20),
+             "ig_n": (10_000, 1 << 20), "scales": (8, 14)}
+
+
+def build_mix(bale, dev, spec=None, seed: int = 1000, counts=(256, 192, 64)):
+    """The uneven 512-instance mix: 256 histograms (tables log-uniform in
+    [1K, 16M] counters, updates log-uniform in [10K, 64M]), 192 gathers (tables
+    [1K, 64M], requests [10K, 128M]) and 64 R-MAT triangle counts (scales
+    scale_min..scale_max, edge factor 16).  Instance k uses seed 1000+k; index
+    arrays are generated on the device (same bits as the host generator)."""
+    import torch
+
+    rng = np.random.default_rng(seed)
+    logu = lambda lo, hi: int(round(np.exp(rng.uniform(np.log(lo), np.log(hi)))))  # noqa: E731
+    inst = []
+    k = 0
+    spec = spec or MIX_FULL
+    for _ in range(counts[0]):
+        t, n = logu(*spec["histo_t"]), logu(*spec["histo_n"])
+        idx = torch.empty(n, dtype=torch.int64, device=dev)
+        bale.gen_uniform_dev(idx, t, seed + k)
+        inst.append(("histo", torch.zeros(t, dtype=torch.int64, device=dev), idx, None, n))
+        k += 1
+    for _ in range(counts[1]):
+        t, n = logu(*spec["ig_t"]), logu(*spec["ig_n"])
+        idx = torch.empty(n, dtype=torch.int64, device=dev)
+        tab = torch.empty(t, dtype=torch.int64, device=dev)
+        bale.gen_uniform_dev(idx, t, seed + k)
+        bale.gen_values_dev(tab, seed + k + 1_000_000)
+        inst.append(("ig", torch.empty(n, dtype=torch.int64, device=dev), idx, tab, n))
+        k += 1
+    for _ in range(counts[2]):
+        sc = int(rng.integers(spec["scales"][0], spec["scales"][1] + 1))
+        L = bale.gen_rmat(sc, 16, 0.57, 0.19, 0.19, seed + k)
+        inst.append(("tri", torch.zeros(1, dtype=torch.int64, device=dev), torch.from_numpy(L.offset).to(dev),
+                     torch.from_numpy(L.nonzero).to(dev), L.nnz))
+        k += 1
+    torch.cuda.synchronize()
+    return inst
+
+
+def run_plain(bale, inst):
+    """Every instance through its own device entry point, back to back on one stream."""
+    for kind, out, a, b, _ in inst:
+        if kind == "histo":
+            bale.histo_dev(out, a)
+        elif kind == "ig":
+            bale.ig_dev(out, a, b)
+        else:
+            bale.triangle_dev(a, b, out)
+
+
+def run_batch(ctx, small: bool = False) -> dict:
+    import torch
+
+    from bale_old_gb300 import batch as bb
+
+    bale, dev, args = ctx["bale"], ctx["dev"], ctx["args"]
+    t0 = time.perf_counter()
+    spec = MIX_SMALL if small else MIX_FULL
+    inst = build_mix(bale, dev, spec)
+    gen_s = time.perf_counter() - t0
+    items = sum(x[4] for x in inst)
+    kinds = {"histo": 0, "ig": 0, "tri": 0}
+    for x in inst:
+        kinds[x[0]] += x[4]
+    # plain per-instance launches
+    with ClockSampler(ctx["gpu"]) as clocks:
+        ctx["dist"].barrier()
+        plain_ms = time_device(lambda: run_plain(bale, inst), args.steps, args.warmup)
+    plain_out = [x[1].clone() for x in inst]
+    for x in inst:
+        if x[0] != "ig":
+            x[1].zero_()
+    # batched: one graph launch per step
+    b = bb.Batch([bb.histo(x[1], x[2]) if x[0] == "histo" else bb.ig(x[1], x[2], x[3]) if x[0] == "ig"
+                  else bb.triangles(x[2], x[3], x[1]) for x in inst])
+    ctx["dist"].barrier()
+    batch_ms = time_device(b.run, args.steps, args.warmup)
+    torch.cuda.synchronize()
+    ok = all(torch.equal(o, x[1]) for o, x in zip(plain_out, inst)) and not b.bad().any()
+    stats = b.stats()
+    b.close()
+    plain_ms, batch_ms = ctx["dist"].max(plain_ms), ctx["dist"].max(batch_ms)
+    w = ctx["dist"].world
+    # per-instance launches, synchronised after each one (a drop-in caller's pattern)
+    def plain_sync():
+        for x in inst:
+            run_plain(bale, [x])
+            torch.cuda.synchronize()
+    sync_s = ctx["dist"].max(time_host(plain_sync, max(1, args.steps // 3), 1))
+    name = "small-instance 512 mix" if small else "uneven 512-instance mix"
+    return {"metric": f"G items/s on the {name} (updates + requests + edges), batched",
+            "value": round(job_rate(items, batch_ms / 1e3, w) / 1e9, 4), "unit": "G items/s",
+            "ms_per_step": round(batch_ms, 3),
+            "plain": {"value": round(job_rate(items, plain_ms / 1e3, w) / 1e9, 4), "unit": "G items/s",
+                      "ms_per_step": round(plain_ms, 3),
+                      "how": "each instance's device entry point, back to back on one stream"},
+            "plain_sync": {"value": round(job_rate(items, sync_s, w) / 1e9, 4), "unit": "G items/s",
+                           "ms_per_step": round(sync_s * 1e3, 3),
+                           "how": "each instance's device entry point, synchronised after each instance"},
+            "batched_vs_plain": round(plain_ms / batch_ms, 3), "batched_vs_plain_sync": round(sync_s * 1e3 / batch_ms, 3),
+            "parity_ok": bool(ok), "batch_stats": stats, "clocks": clocks.summary(),
+            "gpu_launches": args.steps,
+            "config": {"workload": f"batched {name}: 256 histo + 192 ig + 64 R-MAT triangle instances, "
+                                   f"log-uniform sizes {spec}",
+                       "items_per_step": items, "items_by_kind": kinds, "generate_s": round(gen_s, 1),
+                       "l2": "the mix's working set (~60 GB) exceeds L2; no flush"}}
+
+
 def roofline(ctx, wl: str, algo_bytes: int, seconds: float, kernel: str, note: str | None = None) -> dict:
     peak = ctx["peak"]
     achieved = algo_bytes / seconds / 1e9
@@ -460,12 +575,13 @@ def run_gb300(args, dist: Dist) -> dict | None:
            "traffic": committed_traffic(), "cpu": dist.rank == 0 and not args.no_cpu_baseline,
            "budget": args.cpu_budget}
     runners = {"ig": lambda: run_ig(ctx, False), "ig_zipf": lambda: run_ig(ctx, True),
-               "histo": lambda: run_histo(ctx), "triangles": lambda: run_triangles(ctx)}
+               "histo": lambda: run_histo(ctx), "triangles": lambda: run_triangles(ctx),
+               "batch": lambda: run_batch(ctx), "batch_small": lambda: run_batch(ctx, small=True)}
     head = runners[args.workload]()
     torch.cuda.empty_cache()
     if not args.only:
         others = {}
-        for wl in ("ig_zipf", "histo", "triangles", "ig"):
+        for wl in ("ig_zipf", "histo", "triangles", "batch", "batch_small", "ig"):
             if wl != args.workload:
                 others[wl] = runners[wl]()
                 torch.cuda.empty_cache()
@@ -515,7 +631,7 @@ def main(argv=None) -> int:
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="ig", choices=["ig", "ig_zipf", "histo", "triangles"])
+    ap.add_argument("--workload", default="ig", choices=["ig", "ig_zipf", "histo", "triangles", "batch", "batch_small"])
     ap.add_argument("--only", action="store_true", help="measure the selected workload only")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=8.0, help="seconds of CPU baseline per workload")

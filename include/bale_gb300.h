@@ -186,7 +186,8 @@ BALE_API int bale_batch_run(bale_batch_t *b, void *stream);
 /* (synchronous copy; count must equal the batch's instance count).         */
 BALE_API int bale_batch_bad(bale_batch_t *b, int64_t *bad, int64_t count);
 /* out[0..n): tasks, per-kind task counts (histo shared-memory, histo L2,   */
-/* ig, triangle light, triangle heavy), standalone instances, instances.     */
+/* ig, triangle light, triangle heavy), standalone instances, instances,    */
+/* side streams.                                                             */
 BALE_API int bale_batch_stats(bale_batch_t *b, int64_t *out, int n);
 BALE_API void bale_batch_destroy(bale_batch_t *b);
 

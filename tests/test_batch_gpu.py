@@ -57,6 +57,10 @@ def _mix(bale, oracle, cuda, seed: int, big: bool):
         d_cnt = torch.zeros(1 << 24, dtype=torch.int64, device=cuda)
         insts.append(batch.histo(d_cnt, torch.from_numpy(idx).to(cuda)))
         checks.append(("histo", d_cnt, np.bincount(idx, minlength=1 << 24), 0))
+        L = bale.gen_rmat(18, 16, 0.57, 0.19, 0.19, 14 + seed)  # > 2^21 nonzeros: its own kernels
+        d_cnt = torch.zeros(1, dtype=torch.int64, device=cuda)
+        insts.append(batch.triangles(torch.from_numpy(L.offset).to(cuda), torch.from_numpy(L.nonzero).to(cuda), d_cnt))
+        checks.append(("tri", d_cnt, oracle.triangle_agi_mt(L.offset, L.nonzero), 0))
     return insts, checks
 
 
@@ -76,7 +80,7 @@ def test_mixed_batch_matches_per_instance_results(cuda, bale, oracle, standalone
             if standalone == 0:
                 assert st["standalone_instances"] == 0
             else:
-                assert st["standalone_instances"] == 2
+                assert st["standalone_instances"] == 3
             b.run()
             b.run()  # replaying the graph: histo/triangles accumulate, ig overwrites
             torch.cuda.synchronize()
@@ -93,6 +97,38 @@ def test_mixed_batch_matches_per_instance_results(cuda, bale, oracle, standalone
             assert bad[k] == nbad, (k, kind, int(bad[k]), nbad)
     finally:
         bale.tune_set("batch.standalone", -1)
+
+
+def test_many_standalone_instances_on_several_streams(cuda, bale, oracle):
+    """Low standalone thresholds: most instances run their own kernels,
+    spread over the side streams of the graph, concurrently with the queue."""
+    import torch
+
+    from bale_old_gb300 import batch
+
+    knobs = {"batch.standalone_min": 1000, "batch.standalone_min_edges": 1000, "batch.streams": 3}
+    for k, v in knobs.items():
+        bale.tune_set(k, v)
+    try:
+        insts, checks = _mix(bale, oracle, cuda, seed=3, big=True)
+        starts = [c[1].clone() for c in checks]
+        with batch.Batch(insts) as b:
+            st = b.stats()
+            assert st["standalone_instances"] > 40 and st["side_streams"] == 3
+            b.run()
+            torch.cuda.synchronize()
+            bad = b.bad()
+        for k, (kind, dev, want, nbad) in enumerate(checks):
+            got = dev.cpu().numpy()
+            if kind == "tri":
+                assert int(got[0]) == want
+            else:
+                np.testing.assert_array_equal(got, want, err_msg=f"{kind} {k}")
+            assert bad[k] == nbad, (k, kind)
+        del starts
+    finally:
+        for k in knobs:
+            bale.tune_set(k, -1)
 
 
 def test_tiny_tiles_and_knobs_do_not_change_results(cuda, bale, oracle):

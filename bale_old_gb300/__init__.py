@@ -401,3 +401,15 @@ def device_caps() -> dict[str, int]:
 
 def version() -> str:
     return _lib.bale_version().decode()
+
+
+def _apply_committed_tuning() -> None:
+    """Apply bale_old_gb300/tuning/gb300.tune (autotuner output) if present."""
+    from pathlib import Path
+
+    p = Path(__file__).resolve().parent / "tuning" / "gb300.tune"
+    if p.exists():
+        _lib.bale_tune_load(str(p).encode())
+
+
+_apply_committed_tuning()

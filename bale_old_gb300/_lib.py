@@ -64,6 +64,7 @@ SIGNATURES: dict[str, tuple[object, list[object]]] = {
     "bale_tune_set": (C.c_int, [C.c_char_p, i64]),
     "bale_tune_get": (i64, [C.c_char_p]),
     "bale_tune_count": (C.c_int, []),
+    "bale_tune_load": (C.c_int, [C.c_char_p]),
     "bale_tune_name": (C.c_char_p, [C.c_int]),
     # device-resident
     "bale_histo_dev": (C.c_int, [VP, i64, VP, i64, C.c_int, VP, VP]),

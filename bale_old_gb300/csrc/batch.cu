@@ -258,10 +258,9 @@ bool aligned16(const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 
 
 // Would this instance use the region-partitioned kernels on its own?
 bool partition_worthy(const bale_instance_t &x) {
-  const int64_t big = int64_t(96) << 20;
   if (!aligned16(x.in) || !aligned16(x.out)) return false;
-  if (x.kind == BALE_KIND_IG) return x.m * 8 > big && x.n >= (int64_t(1) << 20) && ig_part_supported(x.n, x.m);
-  if (x.kind == BALE_KIND_HISTO) return x.m * 8 > big && x.n >= (int64_t(1) << 20) && x.m <= (int64_t(1024) << 22);
+  if (x.kind == BALE_KIND_IG) return ig_auto_partition(x.n, x.m) && ig_part_supported(x.n, x.m);
+  if (x.kind == BALE_KIND_HISTO) return histo_auto_partition(x.n, x.m) && x.m <= (int64_t(1024) << 22);
   return false;
 }
 

@@ -20,6 +20,11 @@ int current_device();
 
 // Value of a named tuning knob (tune.cu); -1 means "launcher decides".
 int64_t knob(const char *name);
+int64_t knob_or(const char *name, int64_t dflt);
+// Automatic choice of the region-partitioned kernels (tables beyond L2 with
+// enough elements to amortise the passes); thresholds are tuning knobs.
+bool ig_auto_partition(int64_t n, int64_t table_len);
+bool histo_auto_partition(int64_t n, int64_t ncounts);
 
 // Device-wide scratch words owned by the library (per device): the in-kernel
 // bad-input counter and the triangle work cursor.  Allocated once.

@@ -152,7 +152,7 @@ int launch_histo(int64_t *counts, int64_t ncounts, const int64_t *index, int64_t
   int64_t mode = knob("histo.mode");
   if (mode < 0 || mode > 3) {
     if (ncounts <= kSmemMaxCounters) mode = 0;
-    else if (ncounts * 8 > (int64_t(96) << 20) && n >= (int64_t(1) << 20)) mode = 3;
+    else if (histo_auto_partition(n, ncounts)) mode = 3;
     else mode = 2;
   }
   if (mode == 0 && ncounts > kSmemMaxCounters) mode = 2;

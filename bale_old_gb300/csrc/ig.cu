@@ -171,7 +171,7 @@ int launch_ig(int64_t *tgt, const int64_t *index, int64_t n, const int64_t *tabl
   // gather (ig_part.cu) when there are enough requests to amortise its passes.
   const int64_t mode = knob("ig.mode");
   const bool part = aligned && ig_part_supported(n, table_len) &&
-                    (mode == 1 || (mode < 0 && table_len * 8 > (int64_t(96) << 20) && n >= (int64_t(1) << 20)));
+                    (mode == 1 || (mode < 0 && ig_auto_partition(n, table_len)));
   if (part) {
     void *ws = device_workspace(ig_part_workspace_bytes(n, table_len));
     unsigned long long *cursor = next_cursor_word();

@@ -5,6 +5,7 @@
 // each kernel per size class and stores the winners; applications may also
 // pin a knob directly.  Knobs only select among variants that compute the
 // same result; none of them changes an output bit.
+#include <cstdio>
 #include <cstring>
 #include <mutex>
 
@@ -20,11 +21,15 @@ struct Knob {
 
 Knob g_knobs[] = {
     {"ig.mode", -1},            // 0 direct gather, 1 region-partitioned gather
+    {"ig.part_min_table_bytes", -1},   // automatic partitioning above this table size (96 MiB)
+    {"ig.part_min_requests", -1},      // ... with at least this many requests (2^20)
     {"ig.unroll", -1},          // pairs of requests per thread per trip: 1, 2, 4, 8
     {"ig.threads", -1},         // threads per block: 128, 256, 512
     {"ig.blocks_per_sm", -1},   // resident blocks per SM to launch
     {"ig.table_policy", -1},    // 0 L1::no_allocate, 1 L2 evict_last, 2 L2 evict_first, 3 cached
     {"ig.l2_fetch", -1},        // cudaLimitMaxL2FetchGranularity in bytes (0..128)
+    {"histo.part_min_table_bytes", -1},  // automatic partitioning above this table size (96 MiB)
+    {"histo.part_min_updates", -1},      // ... with at least this many updates (2^20)
     {"histo.mode", -1},         // 0 shared-memory private, 1 warp-aggregated L2, 2 plain L2, 3 region-partitioned
     {"histo.unroll", -1},       // pairs per thread per trip (L2 modes): 1, 2, 4, 8
     {"histo.blocks_per_sm", -1},
@@ -62,6 +67,23 @@ int64_t knob(const char *name) {
   return -1;
 }
 
+int64_t knob_or(const char *name, int64_t dflt) {
+  const int64_t v = knob(name);
+  return v >= 0 ? v : dflt;
+}
+
+bool ig_auto_partition(int64_t n, int64_t table_len) {
+  return table_len * 8 > knob_or("ig.part_min_table_bytes", int64_t(96) << 20) &&
+         n >= knob_or("ig.part_min_requests", int64_t(1) << 20);
+}
+
+bool histo_auto_partition(int64_t n, int64_t ncounts) {
+  return ncounts * 8 > knob_or("histo.part_min_table_bytes", int64_t(96) << 20) &&
+         n >= knob_or("histo.part_min_updates", int64_t(1) << 20);
+}
+
+
+
 }  // namespace bale
 
 extern "C" {
@@ -84,6 +106,25 @@ int64_t bale_tune_get(const char *name) {
   for (auto &k : bale::g_knobs)
     if (std::strcmp(k.name, name) == 0) return k.value;
   return -2;
+}
+
+int bale_tune_load(const char *path) {
+  if (!path) return -1;
+  FILE *f = std::fopen(path, "r");
+  if (!f) {
+    bale::set_error("bale_tune_load: cannot open %s", path);
+    return -1;
+  }
+  char line[256];
+  int applied = 0;
+  while (std::fgets(line, sizeof(line), f)) {
+    char name[128];
+    long long value = 0;
+    if (line[0] == '#' || std::sscanf(line, "%127s %lld", name, &value) != 2) continue;
+    if (bale_tune_set(name, static_cast<int64_t>(value)) == BALE_OK) applied++;
+  }
+  std::fclose(f);
+  return applied;
 }
 
 int bale_tune_count(void) { return static_cast<int>(sizeof(bale::g_knobs) / sizeof(bale::g_knobs[0])); }

@@ -382,69 +382,15 @@ def run_triangles(ctx) -> dict:
     return out
 
 
-MIX_FULL = {"histo_t": (1_000, 16 << 20), "histo_n": (10_000, 64 << 20), "ig_t": (1_000, 64 << 20),
-            "ig_n": (10_000, 128 << 20), "scales": (10, 20)}
-MIX_SMALL = {"histo_t": (1_000, 1 << 20), "histo_n": (10_000, 1 << 20), "ig_t": (1_000, 4 << 20),
-             "ig_n": (10_000, 1 << 20), "scales": (8, 14)}
-
-
-def build_mix(bale, dev, spec=None, seed: int = 1000, counts=(256, 192, 64)):
-    """The uneven 512-instance mix: 256 histograms (tables log-uniform in
-    [1K, 16M] counters, updates log-uniform in [10K, 64M]), 192 gathers (tables
-    [1K, 64M], requests [10K, 128M]) and 64 R-MAT triangle counts (scales
-    scale_min..scale_max, edge factor 16).  Instance k uses seed 1000+k; index
-    arrays are generated on the device (same bits as the host generator)."""
-    import torch
-
-    rng = np.random.default_rng(seed)
-    logu = lambda lo, hi: int(round(np.exp(rng.uniform(np.log(lo), np.log(hi)))))  # noqa: E731
-    inst = []
-    k = 0
-    spec = spec or MIX_FULL
-    for _ in range(counts[0]):
-        t, n = logu(*spec["histo_t"]), logu(*spec["histo_n"])
-        idx = torch.empty(n, dtype=torch.int64, device=dev)
-        bale.gen_uniform_dev(idx, t, seed + k)
-        inst.append(("histo", torch.zeros(t, dtype=torch.int64, device=dev), idx, None, n))
-        k += 1
-    for _ in range(counts[1]):
-        t, n = logu(*spec["ig_t"]), logu(*spec["ig_n"])
-        idx = torch.empty(n, dtype=torch.int64, device=dev)
-        tab = torch.empty(t, dtype=torch.int64, device=dev)
-        bale.gen_uniform_dev(idx, t, seed + k)
-        bale.gen_values_dev(tab, seed + k + 1_000_000)
-        inst.append(("ig", torch.empty(n, dtype=torch.int64, device=dev), idx, tab, n))
-        k += 1
-    for _ in range(counts[2]):
-        sc = int(rng.integers(spec["scales"][0], spec["scales"][1] + 1))
-        L = bale.gen_rmat(sc, 16, 0.57, 0.19, 0.19, seed + k)
-        inst.append(("tri", torch.zeros(1, dtype=torch.int64, device=dev), torch.from_numpy(L.offset).to(dev),
-                     torch.from_numpy(L.nonzero).to(dev), L.nnz))
-        k += 1
-    torch.cuda.synchronize()
-    return inst
-
-
-def run_plain(bale, inst):
-    """Every instance through its own device entry point, back to back on one stream."""
-    for kind, out, a, b, _ in inst:
-        if kind == "histo":
-            bale.histo_dev(out, a)
-        elif kind == "ig":
-            bale.ig_dev(out, a, b)
-        else:
-            bale.triangle_dev(a, b, out)
-
-
 def run_batch(ctx, small: bool = False) -> dict:
     import torch
 
-    from bale_old_gb300 import batch as bb
+    from bale_old_gb300.mix import MIX_FULL, MIX_SMALL, as_batch, build_mix, run_plain
 
     bale, dev, args = ctx["bale"], ctx["dev"], ctx["args"]
     t0 = time.perf_counter()
     spec = MIX_SMALL if small else MIX_FULL
-    inst = build_mix(bale, dev, spec)
+    inst = build_mix(dev, spec)
     gen_s = time.perf_counter() - t0
     items = sum(x[4] for x in inst)
     kinds = {"histo": 0, "ig": 0, "tri": 0}
@@ -453,14 +399,13 @@ def run_batch(ctx, small: bool = False) -> dict:
     # plain per-instance launches
     with ClockSampler(ctx["gpu"]) as clocks:
         ctx["dist"].barrier()
-        plain_ms = time_device(lambda: run_plain(bale, inst), args.steps, args.warmup)
+        plain_ms = time_device(lambda: run_plain(inst), args.steps, args.warmup)
     plain_out = [x[1].clone() for x in inst]
     for x in inst:
         if x[0] != "ig":
             x[1].zero_()
     # batched: one graph launch per step
-    b = bb.Batch([bb.histo(x[1], x[2]) if x[0] == "histo" else bb.ig(x[1], x[2], x[3]) if x[0] == "ig"
-                  else bb.triangles(x[2], x[3], x[1]) for x in inst])
+    b = as_batch(inst)
     ctx["dist"].barrier()
     batch_ms = time_device(b.run, args.steps, args.warmup)
     torch.cuda.synchronize()
@@ -472,7 +417,7 @@ def run_batch(ctx, small: bool = False) -> dict:
     # per-instance launches, synchronised after each one (a drop-in caller's pattern)
     def plain_sync():
         for x in inst:
-            run_plain(bale, [x])
+            run_plain([x])
             torch.cuda.synchronize()
     sync_s = ctx["dist"].max(time_host(plain_sync, max(1, args.steps // 3), 1))
     name = "small-instance 512 mix" if small else "uneven 512-instance mix"

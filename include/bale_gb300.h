@@ -134,6 +134,9 @@ BALE_API void bale_release_buffers(void);
 /* returns -2 for one.                                                       */
 BALE_API int bale_tune_set(const char *name, int64_t value);
 BALE_API int64_t bale_tune_get(const char *name);
+/* Apply a tuning file: one "name value" pair per line, '#' comments.        */
+/* Returns the number of knobs applied, -1 if the file cannot be read.      */
+BALE_API int bale_tune_load(const char *path);
 BALE_API int bale_tune_count(void);
 BALE_API const char *bale_tune_name(int i);
 

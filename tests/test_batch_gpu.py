@@ -64,14 +64,35 @@ def _mix(bale, oracle, cuda, seed: int, big: bool):
     return insts, checks
 
 
+class pinned:
+    """Set tuning knobs for a block and restore their previous values."""
+
+    def __init__(self, bale, **knobs):
+        self.bale, self.knobs = bale, {k.replace("__", "."): v for k, v in knobs.items()}
+
+    def __enter__(self):
+        self.old = {k: self.bale.tune_get(k) for k in self.knobs}
+        for k, v in self.knobs.items():
+            self.bale.tune_set(k, v)
+
+    def __exit__(self, *exc):
+        for k, v in self.old.items():
+            self.bale.tune_set(k, v)
+
+
+# the standalone thresholds the assertions below count against
+DEFAULT_RULES = dict(ig__part_min_table_bytes=96 << 20, ig__part_min_requests=1 << 20,
+                     histo__part_min_table_bytes=96 << 20, histo__part_min_updates=1 << 20,
+                     batch__standalone_min=1 << 23, batch__standalone_min_edges=1 << 21)
+
+
 @pytest.mark.parametrize("standalone", [-1, 0])
 def test_mixed_batch_matches_per_instance_results(cuda, bale, oracle, standalone):
     import torch
 
     from bale_old_gb300 import batch
 
-    bale.tune_set("batch.standalone", standalone)
-    try:
+    with pinned(bale, batch__standalone=standalone, **DEFAULT_RULES):
         insts, checks = _mix(bale, oracle, cuda, seed=1, big=True)
         starts = [c[1].clone() for c in checks]
         with batch.Batch(insts) as b:
@@ -95,8 +116,6 @@ def test_mixed_batch_matches_per_instance_results(cuda, bale, oracle, standalone
             else:
                 assert int(got[0]) == 2 * want, (k, int(got[0]), want)
             assert bad[k] == nbad, (k, kind, int(bad[k]), nbad)
-    finally:
-        bale.tune_set("batch.standalone", -1)
 
 
 def test_many_standalone_instances_on_several_streams(cuda, bale, oracle):
@@ -106,10 +125,7 @@ def test_many_standalone_instances_on_several_streams(cuda, bale, oracle):
 
     from bale_old_gb300 import batch
 
-    knobs = {"batch.standalone_min": 1000, "batch.standalone_min_edges": 1000, "batch.streams": 3}
-    for k, v in knobs.items():
-        bale.tune_set(k, v)
-    try:
+    with pinned(bale, batch__standalone_min=1000, batch__standalone_min_edges=1000, batch__streams=3):
         insts, checks = _mix(bale, oracle, cuda, seed=3, big=True)
         starts = [c[1].clone() for c in checks]
         with batch.Batch(insts) as b:
@@ -126,9 +142,6 @@ def test_many_standalone_instances_on_several_streams(cuda, bale, oracle):
                 np.testing.assert_array_equal(got, want, err_msg=f"{kind} {k}")
             assert bad[k] == nbad, (k, kind)
         del starts
-    finally:
-        for k in knobs:
-            bale.tune_set(k, -1)
 
 
 def test_tiny_tiles_and_knobs_do_not_change_results(cuda, bale, oracle):
@@ -136,11 +149,10 @@ def test_tiny_tiles_and_knobs_do_not_change_results(cuda, bale, oracle):
 
     from bale_old_gb300 import batch
 
-    names = [f"batch.{b}.{c}" for b in ("histo_tile", "histo_l2_tile", "ig_tile", "tri_heavy_rows", "tri_light_rows")
-             for c in ("small", "medium", "large")]
-    for name in names:
-        bale.tune_set(name, 1 if "rows" in name else 1000)
-    try:
+    names = {f"batch__{b}__{c}": (1 if "rows" in b else 1000)
+             for b in ("histo_tile", "histo_l2_tile", "ig_tile", "tri_heavy_rows", "tri_light_rows")
+             for c in ("small", "medium", "large")}
+    with pinned(bale, **names):
         insts, checks = _mix(bale, oracle, cuda, seed=2, big=False)
         starts = [c[1].clone() for c in checks]
         with batch.Batch(insts) as b:
@@ -155,9 +167,6 @@ def test_tiny_tiles_and_knobs_do_not_change_results(cuda, bale, oracle):
             else:
                 assert int(got[0]) == want
         del starts
-    finally:
-        for name in names:
-            bale.tune_set(name, -1)
 
 
 def test_empty_and_degenerate_batches(cuda, bale):

@@ -37,6 +37,18 @@ class bale_instance_t(C.Structure):
 
 PINST = C.POINTER(bale_instance_t)
 
+
+class bale_request_t(C.Structure):
+    """One request of a serving trace (include/bale_gb300.h)."""
+
+    _fields_ = [("kind", C.c_int32), ("object", C.c_int32), ("shift", C.c_int32), ("reserved", C.c_int32),
+                ("n", i64), ("index", VP), ("out", VP), ("arrival", C.c_double)]
+
+
+class bale_serve_stats_t(C.Structure):
+    _fields_ = [(f, C.c_double) for f in ("makespan_s", "p50_s", "p99_s", "mean_s", "items_per_s", "gpu_busy_s")] + \
+               [(f, i64) for f in ("ticks", "tasks", "max_active", "admission_waits", "bad", "loop_iters")]
+
 # name -> (restype, argtypes)
 SIGNATURES: dict[str, tuple[object, list[object]]] = {
     # drop-ins (apps/histo_src/histo.h:47-50)
@@ -75,6 +87,14 @@ SIGNATURES: dict[str, tuple[object, list[object]]] = {
     "bale_batch_bad": (C.c_int, [VP, P64, i64]),
     "bale_batch_stats": (C.c_int, [VP, P64, C.c_int]),
     "bale_batch_destroy": (None, [VP]),
+    "bale_server_create": (VP, [i64, C.c_int]),
+    "bale_server_add_table": (C.c_int, [VP, P64, i64]),
+    "bale_server_add_counts": (C.c_int, [VP, i64]),
+    "bale_server_add_graph": (C.c_int, [VP, P64, P64, i64, i64]),
+    "bale_server_read_counts": (C.c_int, [VP, C.c_int, P64, i64]),
+    "bale_server_run": (C.c_int, [VP, C.POINTER(bale_request_t), i64, C.POINTER(C.c_double),
+                                  C.POINTER(bale_serve_stats_t)]),
+    "bale_server_destroy": (None, [VP]),
     "bale_ig_dev_noalloc": (C.c_int, [VP, VP, i64, VP, i64, C.c_int, VP, VP]),
     # inputs
     "bale_splitmix64": (u64, [u64, u64]),

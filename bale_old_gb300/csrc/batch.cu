@@ -35,34 +35,13 @@
 #include <new>
 #include <vector>
 
-#include "tri_device.cuh"
+#include "batch.cuh"
 
 namespace bale {
+namespace q {
 
 namespace {
 
-enum TaskKind : int32_t { kHistoSmem = 0, kHistoL2 = 1, kIgDirect = 2, kTriLight = 3, kTriHeavy = 4 };
-
-struct Inst {
-  int32_t kind, shift;
-  int64_t n, m;
-  int64_t *out;
-  const int64_t *in;
-  const int64_t *aux;
-  int64_t bits;  // triangles: bitmap bits (power of two)
-};
-
-struct Task {
-  int32_t kind, inst;
-  int64_t lo, hi;
-};
-
-constexpr int kThreads = 512;
-constexpr int kWarps = kThreads / 32;
-constexpr int64_t kSmemCounters = 48 * 1024;
-constexpr size_t kSmemBytes = static_cast<size_t>(kSmemCounters) * sizeof(uint32_t);  // 192 KiB
-static_assert(kSmemBytes >= static_cast<size_t>(tri::kHeavyBits / 8), "bitmap must fit");
-static_assert(kSmemBytes >= static_cast<size_t>(kWarps) * tri::kLightCap * sizeof(uint32_t), "row slots must fit");
 
 __device__ __forceinline__ void add_bad(unsigned long long *bad, unsigned long long v) {
   v = warp_sum_u64(v);
@@ -214,13 +193,113 @@ int64_t tuned(const char *base, int cls, int64_t dflt) {
 
 }  // namespace
 
+Inst make_inst(const bale_instance_t &x) {
+  Inst d;
+  d.kind = x.kind;
+  d.shift = x.shift;
+  d.n = x.n;
+  d.m = x.m;
+  d.out = x.out;
+  d.in = x.in;
+  d.aux = x.aux;
+  d.bits = x.kind == BALE_KIND_TRIANGLES ? tri::bitmap_bits(x.n) : 0;
+  return d;
+}
+
+void plan_tasks(const bale_instance_t &x, int32_t k, const int64_t *host_off, std::vector<Planned> &plan) {
+  if (x.n == 0) return;
+  const int cls = size_class(x.kind == BALE_KIND_TRIANGLES ? x.m : x.n);
+  if (x.kind == BALE_KIND_HISTO) {
+    if (x.m <= kSmemCounters) {
+      // each task sees several updates per counter so the flush stays cheap
+      int64_t tile = tuned("batch.histo_tile", cls, int64_t(1) << 17);
+      tile = std::max<int64_t>(tile, 4 * x.m);
+      for (int64_t lo = 0; lo < x.n; lo += tile)
+        plan.push_back({{kHistoSmem, k, lo, std::min(x.n, lo + tile)},
+                        static_cast<double>(std::min(tile, x.n - lo)) * 0.5 + static_cast<double>(x.m)});
+    } else {
+      const int64_t tile = tuned("batch.histo_l2_tile", cls, int64_t(1) << 17);
+      for (int64_t lo = 0; lo < x.n; lo += tile)
+        plan.push_back({{kHistoL2, k, lo, std::min(x.n, lo + tile)}, static_cast<double>(std::min(tile, x.n - lo))});
+    }
+  } else if (x.kind == BALE_KIND_IG) {
+    const int64_t tile = tuned("batch.ig_tile", cls, int64_t(1) << 17);
+    for (int64_t lo = 0; lo < x.n; lo += tile)
+      plan.push_back({{kIgDirect, k, lo, std::min(x.n, lo + tile)},
+                      static_cast<double>(std::min(tile, x.n - lo)) * (x.m * 8 > (int64_t(96) << 20) ? 2.0 : 1.0)});
+  } else {
+    // Row degrees are known exactly and cheaply: every heavy row gets its own
+    // task (or a few per task); light rows are cut into tasks of about the
+    // same number of nonzeros.
+    const int64_t bits = tri::bitmap_bits(x.n);
+    const int64_t lim = std::min<int64_t>(x.n, bits);
+    const double avg = static_cast<double>(x.m) / static_cast<double>(x.n);
+    const int64_t hrows = tuned("batch.tri_heavy_rows", cls, 1);
+    for (int64_t i = 0; i < lim;) {
+      if (host_off[i + 1] - host_off[i] >= tri::kHeavyMinDeg) {
+        int64_t j = i, nh = 0;
+        double c = 0;
+        while (j < lim && nh < hrows) {
+          const int64_t dj = host_off[j + 1] - host_off[j];
+          if (dj >= tri::kHeavyMinDeg) {
+            c += static_cast<double>(dj) * 4.0 * avg;
+            nh++;
+          }
+          j++;
+        }
+        plan.push_back({{kTriHeavy, k, i, j}, c});
+        i = j;
+      } else {
+        i++;
+      }
+    }
+    const int64_t lnnz = tuned("batch.tri_light_rows", cls, 1 << 15);  // nonzeros per light task
+    int64_t lo = 0;
+    while (lo < x.n) {
+      int64_t hi = lo, acc = 0;
+      while (hi < x.n && (hi == lo || acc < lnnz)) {
+        acc += host_off[hi + 1] - host_off[hi];
+        hi++;
+      }
+      plan.push_back({{kTriLight, k, lo, hi}, static_cast<double>(acc) * 2.0 * avg + 64.0});
+      lo = hi;
+    }
+  }
+}
+
+int64_t queue_blocks() {
+  const int dev = current_device();
+  if (dev >= 0 && dev < 64 && !g_batch_attr[dev]) {
+    if (cudaFuncSetAttribute(batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             static_cast<int>(kSmemBytes)) != cudaSuccess)
+      return 0;
+    g_batch_attr[dev] = true;
+  }
+  int occ = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, batch_kernel, kThreads, kSmemBytes) != cudaSuccess || occ < 1)
+    occ = 1;
+  return static_cast<int64_t>(num_sms()) * occ;
+}
+
+int launch_queue(const Task *d_tasks, int64_t ntasks, const Inst *d_inst, unsigned long long *words,
+                 unsigned long long *bad, int64_t blocks, cudaStream_t stream) {
+  if (ntasks <= 0) return BALE_OK;
+  if (blocks > ntasks) blocks = ntasks;
+  if (blocks < 1) blocks = 1;
+  batch_kernel<<<static_cast<unsigned>(blocks), kThreads, kSmemBytes, stream>>>(d_tasks, ntasks, d_inst, words, bad,
+                                                                                  words + 1);
+  BALE_CUDA_OK(cudaGetLastError());
+  return BALE_OK;
+}
+
+}  // namespace q
 }  // namespace bale
 
 struct bale_batch {
   int device = 0;
   int64_t count = 0;
-  bale::Inst *d_inst = nullptr;
-  bale::Task *d_tasks = nullptr;
+  bale::q::Inst *d_inst = nullptr;
+  bale::q::Task *d_tasks = nullptr;
   int64_t ntasks = 0;
   int64_t ntasks_kind[5] = {0, 0, 0, 0, 0};
   unsigned long long *d_words = nullptr;  // [0] queue head, [1] work, then 4 words per standalone instance
@@ -270,12 +349,8 @@ bool partition_worthy(const bale_instance_t &x) {
 bool goes_standalone(const bale_instance_t &x) {
   if (knob("batch.standalone") == 0 || x.n == 0) return false;
   if (partition_worthy(x)) return true;
-  if (x.kind == BALE_KIND_TRIANGLES) {
-    const int64_t min_e = knob("batch.standalone_min_edges") > 0 ? knob("batch.standalone_min_edges") : int64_t(1) << 21;
-    return x.m >= min_e;
-  }
-  const int64_t min_n = knob("batch.standalone_min") > 0 ? knob("batch.standalone_min") : int64_t(1) << 23;
-  return x.n >= min_n;
+  if (x.kind == BALE_KIND_TRIANGLES) return x.m >= knob_or("batch.standalone_min_edges", int64_t(1) << 21);
+  return x.n >= knob_or("batch.standalone_min", int64_t(1) << 23);
 }
 
 size_t standalone_ws(const bale_instance_t &x) {
@@ -306,9 +381,21 @@ int launch_standalone(const bale_instance_t &x, unsigned long long *bad, void *w
 }
 
 }  // namespace
+
+bool instance_valid(const bale_instance_t &x) {
+  const bool ok_kind = x.kind == BALE_KIND_HISTO || x.kind == BALE_KIND_IG || x.kind == BALE_KIND_TRIANGLES;
+  const bool ok_shift = x.shift == 0 || x.shift == 16;
+  const bool ok_ptr = x.kind == BALE_KIND_TRIANGLES
+                          ? (x.out && (x.n == 0 || x.in) && (x.m == 0 || x.aux))
+                          : (x.n == 0 || (x.in && x.out && (x.kind != BALE_KIND_IG || x.m == 0 || x.aux)));
+  return ok_kind && ok_shift && x.n >= 0 && x.m >= 0 && ok_ptr &&
+         !(x.kind == BALE_KIND_TRIANGLES && x.n >= 0xffffffffll);
+}
+
 }  // namespace bale
 
 using namespace bale;
+using namespace bale::q;
 
 extern "C" {
 
@@ -335,37 +422,17 @@ bale_batch_t *bale_batch_create(const bale_instance_t *inst, int64_t count) {
     }                                                                                     \
   } while (0)
 
-  // ---- validate and build the device instance records ----
   std::vector<Inst> di(static_cast<size_t>(count));
   for (int64_t k = 0; k < count; k++) {
-    const bale_instance_t &x = inst[k];
-    const bool ok_kind = x.kind == BALE_KIND_HISTO || x.kind == BALE_KIND_IG || x.kind == BALE_KIND_TRIANGLES;
-    const bool ok_shift = x.shift == 0 || x.shift == 16;
-    const bool ok_ptr = x.kind == BALE_KIND_TRIANGLES
-                            ? (x.out && (x.n == 0 || x.in) && (x.m == 0 || x.aux))
-                            : (x.n == 0 || (x.in && x.out && (x.kind != BALE_KIND_IG || x.m == 0 || x.aux)));
-    if (!ok_kind || !ok_shift || x.n < 0 || x.m < 0 || !ok_ptr ||
-        (x.kind == BALE_KIND_TRIANGLES && x.n >= 0xffffffffll)) {
+    if (!instance_valid(inst[k])) {
       set_error("bale_batch_create: instance %lld is invalid", static_cast<long long>(k));
       destroy(b);
       return nullptr;
     }
-    Inst &d = di[static_cast<size_t>(k)];
-    d.kind = x.kind;
-    d.shift = x.shift;
-    d.n = x.n;
-    d.m = x.m;
-    d.out = x.out;
-    d.in = x.in;
-    d.aux = x.aux;
-    d.bits = x.kind == BALE_KIND_TRIANGLES ? tri::bitmap_bits(x.n) : 0;
+    di[static_cast<size_t>(k)] = make_inst(inst[k]);
   }
 
   // ---- plan: standalone instances, then the work queue ----
-  struct Planned {
-    Task t;
-    double cost;
-  };
   std::vector<Planned> plan;
   std::vector<size_t> ws_off;
   size_t ws_total = 256;
@@ -379,69 +446,12 @@ bale_batch_t *bale_batch_create(const bale_instance_t *inst, int64_t count) {
       ws_total += standalone_ws(x);
       continue;
     }
-    const int cls = size_class(x.kind == BALE_KIND_TRIANGLES ? x.m : x.n);
-    if (x.kind == BALE_KIND_HISTO) {
-      if (x.m <= kSmemCounters) {
-        // each task sees several updates per counter so the flush stays cheap
-        int64_t tile = tuned("batch.histo_tile", cls, int64_t(1) << 17);
-        tile = std::max<int64_t>(tile, 4 * x.m);
-        for (int64_t lo = 0; lo < x.n; lo += tile)
-          plan.push_back({{kHistoSmem, static_cast<int32_t>(k), lo, std::min(x.n, lo + tile)},
-                          static_cast<double>(std::min(tile, x.n - lo)) * 0.5 + static_cast<double>(x.m)});
-      } else {
-        const int64_t tile = tuned("batch.histo_l2_tile", cls, int64_t(1) << 17);
-        for (int64_t lo = 0; lo < x.n; lo += tile)
-          plan.push_back({{kHistoL2, static_cast<int32_t>(k), lo, std::min(x.n, lo + tile)},
-                          static_cast<double>(std::min(tile, x.n - lo))});
-      }
-    } else if (x.kind == BALE_KIND_IG) {
-      const int64_t tile = tuned("batch.ig_tile", cls, int64_t(1) << 17);
-      for (int64_t lo = 0; lo < x.n; lo += tile)
-        plan.push_back({{kIgDirect, static_cast<int32_t>(k), lo, std::min(x.n, lo + tile)},
-                        static_cast<double>(std::min(tile, x.n - lo)) * (x.m * 8 > (int64_t(96) << 20) ? 2.0 : 1.0)});
-    } else {
-      // Row degrees are known exactly and cheaply: read the offsets once and
-      // give every heavy row its own task; cut the light rows into tasks of
-      // about the same number of nonzeros.
+    if (x.kind == BALE_KIND_TRIANGLES) {
       host_off.resize(static_cast<size_t>(x.n + 1));
       BATCH_CUDA(cudaMemcpy(host_off.data(), x.in, sizeof(int64_t) * static_cast<size_t>(x.n + 1),
                             cudaMemcpyDeviceToHost));
-      const int64_t bits = tri::bitmap_bits(x.n);
-      const int64_t lim = std::min<int64_t>(x.n, bits);
-      const double avg = static_cast<double>(x.m) / static_cast<double>(x.n);
-      const int64_t hrows = tuned("batch.tri_heavy_rows", cls, 1);
-      for (int64_t i = 0; i < lim;) {
-        const int64_t d = host_off[i + 1] - host_off[i];
-        if (i < lim && d >= tri::kHeavyMinDeg) {
-          int64_t j = i, nh = 0;
-          double c = 0;
-          while (j < lim && nh < hrows) {
-            const int64_t dj = host_off[j + 1] - host_off[j];
-            if (dj >= tri::kHeavyMinDeg) {
-              c += static_cast<double>(dj) * 4.0 * avg;
-              nh++;
-            }
-            j++;
-          }
-          plan.push_back({{kTriHeavy, static_cast<int32_t>(k), i, j}, c});
-          i = j;
-        } else {
-          i++;
-        }
-      }
-      const int64_t lnnz = tuned("batch.tri_light_rows", cls, 1 << 15);  // nonzeros per light task
-      int64_t lo = 0;
-      while (lo < x.n) {
-        int64_t hi = lo;
-        int64_t acc = 0;
-        while (hi < x.n && (hi == lo || acc < lnnz)) {
-          acc += host_off[hi + 1] - host_off[hi];
-          hi++;
-        }
-        plan.push_back({{kTriLight, static_cast<int32_t>(k), lo, hi}, static_cast<double>(acc) * 2.0 * avg + 64.0});
-        lo = hi;
-      }
     }
+    plan_tasks(x, static_cast<int32_t>(k), host_off.data(), plan);
   }
   // longest first
   std::stable_sort(plan.begin(), plan.end(), [](const Planned &a, const Planned &c) { return a.cost > c.cost; });
@@ -465,22 +475,18 @@ bale_batch_t *bale_batch_create(const bale_instance_t *inst, int64_t count) {
     BATCH_CUDA(cudaMemcpy(b->d_tasks, tasks.data(), sizeof(Task) * tasks.size(), cudaMemcpyHostToDevice));
   BATCH_CUDA(cudaMemset(b->d_words, 0, sizeof(unsigned long long) * nw));
   BATCH_CUDA(cudaMemset(b->d_bad, 0, sizeof(unsigned long long) * std::max<int64_t>(1, count)));
-  const int dev = b->device;
-  if (dev >= 0 && dev < 64 && !g_batch_attr[dev]) {
-    BATCH_CUDA(cudaFuncSetAttribute(batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    static_cast<int>(kSmemBytes)));
-    g_batch_attr[dev] = true;
+  int64_t blocks = queue_blocks();
+  if (blocks < 1) {
+    set_error("bale_batch_create: the queue kernel cannot be configured");
+    destroy(b);
+    return nullptr;
   }
-  int occ = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, batch_kernel, kThreads, kSmemBytes) != cudaSuccess || occ < 1)
-    occ = 1;
-  int64_t blocks = static_cast<int64_t>(num_sms()) * occ;
   const int64_t qb = knob("batch.queue_blocks");
   if (qb > 0 && qb < blocks) blocks = qb;
-  if (blocks > b->ntasks) blocks = std::max<int64_t>(1, b->ntasks);
 
   // side streams for the standalone instances, longest first to the least loaded
-  int64_t nside = knob("batch.streams") > 0 ? knob("batch.streams") : 4;
+  int64_t nside = knob_or("batch.streams", 4);
+  if (nside < 1) nside = 1;
   nside = std::min<int64_t>(nside, static_cast<int64_t>(b->standalone.size()));
   std::vector<int> lane(b->standalone.size(), 0);
   {
@@ -490,21 +496,15 @@ bale_batch_t *bale_batch_create(const bale_instance_t *inst, int64_t count) {
       return standalone_cost(inst[b->standalone[a]]) > standalone_cost(inst[b->standalone[c]]);
     });
     std::vector<double> load(static_cast<size_t>(std::max<int64_t>(1, nside)), 0.0);
-    std::vector<size_t> reordered;
-    for (size_t s : order) {
-      const size_t l = static_cast<size_t>(std::min_element(load.begin(), load.end()) - load.begin());
-      lane[s] = static_cast<int>(l);
-      load[l] += standalone_cost(inst[b->standalone[s]]);
-      reordered.push_back(s);
-    }
-    // launch in longest-first order within each lane
     std::vector<int64_t> st2;
     std::vector<size_t> off2;
     std::vector<int> lane2;
-    for (size_t s : reordered) {
+    for (size_t s : order) {
+      const size_t l = static_cast<size_t>(std::min_element(load.begin(), load.end()) - load.begin());
+      load[l] += standalone_cost(inst[b->standalone[s]]);
       st2.push_back(b->standalone[s]);
       off2.push_back(ws_off[s]);
-      lane2.push_back(lane[s]);
+      lane2.push_back(static_cast<int>(l));
     }
     b->standalone.swap(st2);
     ws_off.swap(off2);
@@ -537,11 +537,7 @@ bale_batch_t *bale_batch_create(const bale_instance_t *inst, int64_t count) {
     }
     for (int64_t l = 0; l < nside; l++) cap_ok &= cudaEventRecord(b->ev_join[l], b->s_side[l]) == cudaSuccess;
   }
-  if (b->ntasks > 0) {
-    batch_kernel<<<static_cast<unsigned>(blocks), kThreads, kSmemBytes, b->s_main>>>(
-        b->d_tasks, b->ntasks, b->d_inst, b->d_words, b->d_bad, b->d_words + 1);
-    cap_ok &= cudaGetLastError() == cudaSuccess;
-  }
+  cap_ok &= launch_queue(b->d_tasks, b->ntasks, b->d_inst, b->d_words, b->d_bad, blocks, b->s_main) == BALE_OK;
   for (int64_t l = 0; l < nside; l++) cap_ok &= cudaStreamWaitEvent(b->s_main, b->ev_join[l], 0) == cudaSuccess;
   cudaError_t ce = cudaStreamEndCapture(b->s_main, &b->graph);
   if (!cap_ok || ce != cudaSuccess || !b->graph) {

@@ -78,6 +78,16 @@ size_t tri_hybrid_workspace_bytes(int64_t numrows, int64_t nnz);
 int launch_triangle_hybrid(const int64_t *offset, const int64_t *nonzero, int64_t numrows, int64_t nnz,
                            unsigned long long *count, unsigned long long *work, unsigned long long *bad,
                            void *ws, unsigned long long *words, int rows_per_fetch, cudaStream_t stream);
+// A public batch instance is well formed (kind, shift, sizes, pointers).
+bool instance_valid(const bale_instance_t &x);
+// The two halves of the hybrid: prepare (u32 column copy + heavy-row list,
+// once per graph) and run (heavy and light kernels; cursors[0..1] zeroed here).
+int tri_hybrid_prepare(const int64_t *offset, const int64_t *nonzero, int64_t numrows, int64_t nnz,
+                       uint32_t *col32, uint32_t *heavy, unsigned long long *nheavy, cudaStream_t stream);
+int tri_hybrid_run(const int64_t *offset, const uint32_t *col32, const uint32_t *heavy,
+                   const unsigned long long *nheavy, int64_t numrows, int64_t nnz, unsigned long long *count,
+                   unsigned long long *work, unsigned long long *bad, unsigned long long *cursors,
+                   int rows_per_fetch, cudaStream_t stream);
 // max over index[i] >> shift into *out (u64, must start at 0); negatives count as huge.
 int launch_index_max(const int64_t *index, int64_t n, int shift, unsigned long long *out,
                      cudaStream_t stream);

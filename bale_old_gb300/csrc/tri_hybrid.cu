@@ -126,31 +126,32 @@ size_t tri_hybrid_workspace_bytes(int64_t numrows, int64_t nnz) {
          static_cast<size_t>(lim > 0 ? lim : 1) * sizeof(uint32_t);
 }
 
-int launch_triangle_hybrid(const int64_t *offset, const int64_t *nonzero, int64_t numrows, int64_t nnz,
-                           unsigned long long *count, unsigned long long *work, unsigned long long *bad,
-                           void *ws, unsigned long long *words, int rows_per_fetch, cudaStream_t stream) {
-  // words: [0] heavy-list length, [1] heavy cursor, [2] light cursor (zeroed here)
+int tri_hybrid_prepare(const int64_t *offset, const int64_t *nonzero, int64_t numrows, int64_t nnz,
+                       uint32_t *col32, uint32_t *heavy, unsigned long long *nheavy, cudaStream_t stream) {
   const int sms = num_sms();
-  char *p = static_cast<char *>(ws);
-  uint32_t *col32 = reinterpret_cast<uint32_t *>(p);
-  p += (static_cast<size_t>(nnz > 0 ? nnz : 1) * sizeof(uint32_t) + 255) & ~size_t(255);
-  uint32_t *heavy = reinterpret_cast<uint32_t *>(p);
   const int64_t bits = tri::bitmap_bits(numrows);
-
-  BALE_CUDA_OK(cudaMemsetAsync(words, 0, 3 * sizeof(unsigned long long), stream));
+  BALE_CUDA_OK(cudaMemsetAsync(nheavy, 0, sizeof(unsigned long long), stream));
   if (nnz > 0) {
     int64_t blocks = (nnz + 255) / 256, cap = static_cast<int64_t>(sms) * 8;
     tri_convert_kernel<<<static_cast<unsigned>(blocks < cap ? blocks : cap), 256, 0, stream>>>(nonzero, nnz, col32);
     BALE_CUDA_OK(cudaGetLastError());
   }
-  {
-    const int64_t lim = numrows < bits ? numrows : bits;
-    int64_t blocks = (lim + 255) / 256, cap = static_cast<int64_t>(sms) * 8;
-    if (blocks < 1) blocks = 1;
-    tri_classify_kernel<<<static_cast<unsigned>(blocks < cap ? blocks : cap), 256, 0, stream>>>(
-        offset, numrows, bits, heavy, words);
-    BALE_CUDA_OK(cudaGetLastError());
-  }
+  const int64_t lim = numrows < bits ? numrows : bits;
+  int64_t blocks = (lim + 255) / 256, cap = static_cast<int64_t>(sms) * 8;
+  if (blocks < 1) blocks = 1;
+  tri_classify_kernel<<<static_cast<unsigned>(blocks < cap ? blocks : cap), 256, 0, stream>>>(
+      offset, numrows, bits, heavy, nheavy);
+  BALE_CUDA_OK(cudaGetLastError());
+  return BALE_OK;
+}
+
+int tri_hybrid_run(const int64_t *offset, const uint32_t *col32, const uint32_t *heavy,
+                   const unsigned long long *nheavy, int64_t numrows, int64_t nnz, unsigned long long *count,
+                   unsigned long long *work, unsigned long long *bad, unsigned long long *cursors,
+                   int rows_per_fetch, cudaStream_t stream) {
+  const int sms = num_sms();
+  const int64_t bits = tri::bitmap_bits(numrows);
+  BALE_CUDA_OK(cudaMemsetAsync(cursors, 0, 2 * sizeof(unsigned long long), stream));
   {
     const size_t smem = static_cast<size_t>(bits / 32) * sizeof(uint32_t);
     const int dev = current_device();
@@ -164,7 +165,7 @@ int launch_triangle_hybrid(const int64_t *offset, const int64_t *nonzero, int64_
         occ < 1)
       occ = 1;
     tri_heavy_kernel<<<static_cast<unsigned>(sms * occ), kHeavyThreads, smem, stream>>>(
-        offset, col32, nnz, heavy, words, bits, count, work, bad, words + 1);
+        offset, col32, nnz, heavy, nheavy, bits, count, work, bad, cursors);
     BALE_CUDA_OK(cudaGetLastError());
   }
   {
@@ -176,10 +177,24 @@ int launch_triangle_hybrid(const int64_t *offset, const int64_t *nonzero, int64_
     const int64_t need = ((numrows + rows_per_fetch - 1) / rows_per_fetch + kLightWarps - 1) / kLightWarps;
     if (blocks > need) blocks = need > 0 ? need : 1;
     tri_light_kernel<<<static_cast<unsigned>(blocks), kLightThreads, 0, stream>>>(
-        offset, col32, numrows, nnz, bits, count, work, bad, words + 2, rows_per_fetch);
+        offset, col32, numrows, nnz, bits, count, work, bad, cursors + 1, rows_per_fetch);
     BALE_CUDA_OK(cudaGetLastError());
   }
   return BALE_OK;
+}
+
+int launch_triangle_hybrid(const int64_t *offset, const int64_t *nonzero, int64_t numrows, int64_t nnz,
+                           unsigned long long *count, unsigned long long *work, unsigned long long *bad,
+                           void *ws, unsigned long long *words, int rows_per_fetch, cudaStream_t stream) {
+  // words: [0] heavy-list length, [1] heavy cursor, [2] light cursor
+  char *p = static_cast<char *>(ws);
+  uint32_t *col32 = reinterpret_cast<uint32_t *>(p);
+  p += (static_cast<size_t>(nnz > 0 ? nnz : 1) * sizeof(uint32_t) + 255) & ~size_t(255);
+  uint32_t *heavy = reinterpret_cast<uint32_t *>(p);
+  int rc = tri_hybrid_prepare(offset, nonzero, numrows, nnz, col32, heavy, words, stream);
+  if (rc != BALE_OK) return rc;
+  return tri_hybrid_run(offset, col32, heavy, words, numrows, nnz, count, work, bad, words + 1, rows_per_fetch,
+                        stream);
 }
 
 }  // namespace bale

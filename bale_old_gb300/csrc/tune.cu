@@ -55,6 +55,10 @@ Knob g_knobs[] = {
     {"batch.tri_light_rows.small", -1},
     {"batch.tri_light_rows.medium", -1},
     {"batch.tri_light_rows.large", -1},
+    {"serve.tick_cost", -1},      // work per tick (element-cost units, 2^24)
+    {"serve.request_cost", -1},   // work one request may add to a tick (2^22)
+    {"serve.tick_tasks", -1},     // tasks per tick (4096)
+    {"serve.reserve_bytes", -1},  // free HBM a registration must leave (1 GiB)
     {"tri.mode", -1},           // 0 warp-per-row merge for every row, 1 bitmap/search hybrid
 };
 std::mutex g_mu;

@@ -439,6 +439,109 @@ def run_batch(ctx, small: bool = False) -> dict:
                        "l2": "the mix's working set (~60 GB) exceeds L2; no flush"}}
 
 
+def run_serve(ctx) -> dict:
+    """Serving: Poisson arrivals of 60% ig / 30% histo / 10% triangle requests
+    (sizes log-uniform as in the batched mix; graphs R-MAT scales 12-20)
+    against resident tables, counters and graphs; rates swept from light load
+    to saturation; p50/p99 latency and throughput per rate."""
+    import torch
+
+    from bale_old_gb300 import serve as sv
+
+    bale, args = ctx["bale"], ctx["args"]
+    rng = np.random.default_rng(4242)
+    logu = lambda lo, hi: int(round(np.exp(rng.uniform(np.log(lo), np.log(hi)))))  # noqa: E731
+    nreq = 200
+    t0 = time.perf_counter()
+    s = sv.Server(arena_bytes=48 << 30, max_active=64)
+    # resident objects
+    tables = [logu(1_000, 64 << 20) for _ in range(8)]
+    tids = [s.add_table(bale.gen_values(t, 50 + i)) for i, t in enumerate(tables)]
+    counters = [logu(1_000, 16 << 20) for _ in range(8)]
+    cids = [s.add_counts(c) for c in counters]
+    graphs = [bale.gen_rmat(sc, 16, 0.57, 0.19, 0.19, 70 + sc) for sc in (12, 14, 16, 18, 19, 20)]
+    gids = [s.add_graph(L) for L in graphs]
+    # requests: each ig/histo request reads a prefix of its object's pinned index pool
+    kinds, objs, sizes = [], [], []
+    for _ in range(nreq):
+        u = rng.random()
+        if u < 0.6:
+            kinds.append("ig"); objs.append(int(rng.integers(8))); sizes.append(logu(10_000, 128 << 20))
+        elif u < 0.9:
+            kinds.append("histo"); objs.append(int(rng.integers(8))); sizes.append(logu(10_000, 64 << 20))
+        else:
+            kinds.append("tri"); objs.append(int(rng.integers(len(graphs)))); sizes.append(0)
+    pools = {}
+    for kind, o, n in zip(kinds, objs, sizes):
+        if kind != "tri":
+            key = (kind, o)
+            pools[key] = max(pools.get(key, 0), n)
+    pinned = {}
+    for (kind, o), n in pools.items():
+        rngmax = tables[o] if kind == "ig" else counters[o]
+        pinned[(kind, o)] = torch.from_numpy(bale.gen_uniform(n, rngmax, 90 + o + (0 if kind == "ig" else 100))).pin_memory()
+    out_total = sum(n for k, n in zip(kinds, sizes) if k == "ig")
+    out_pool = torch.empty(out_total, dtype=torch.int64).pin_memory()
+    tri_out = np.zeros((nreq, 1), np.int64)
+    items = sum(sizes) + sum(graphs[o].nnz for k, o in zip(kinds, objs) if k == "tri")
+    gen_s = time.perf_counter() - t0
+
+    def trace(arrivals):
+        reqs, off = [], 0
+        for k, (kind, o, n) in enumerate(zip(kinds, objs, sizes)):
+            if kind == "ig":
+                reqs.append(sv.ig(tids[o], pinned[(kind, o)].numpy()[:n], out_pool.numpy()[off:off + n], arrivals[k]))
+                off += n
+            elif kind == "histo":
+                reqs.append(sv.histo(cids[o], pinned[(kind, o)].numpy()[:n], arrivals[k]))
+            else:
+                reqs.append(sv.triangles(gids[o], tri_out[k], arrivals[k]))
+        return reqs
+
+    # capacity: everything arrives at once
+    s.run(trace(np.zeros(nreq)))  # warm-up
+    _, cap = s.run(trace(np.zeros(nreq)))
+    cap_rate = nreq / cap["makespan_s"]
+    rates = []
+    for frac in (0.25, 0.5, 0.75, 1.0, 1.5):
+        lat, st = s.run(trace(sv.poisson_arrivals(nreq, frac * cap_rate, 17)))
+        rates.append({"offered_requests_per_s": round(frac * cap_rate, 2), "load": frac,
+                      "p50_ms": round(st["p50_s"] * 1e3, 3), "p99_ms": round(st["p99_s"] * 1e3, 3),
+                      "mean_ms": round(st["mean_s"] * 1e3, 3), "items_per_s": round(st["items_per_s"], 1),
+                      "makespan_s": round(st["makespan_s"], 4), "ticks": st["ticks"],
+                      "max_active": st["max_active"], "admission_waits": st["admission_waits"]})
+    # exactness of the last run: triangle counts and a sample of ig values
+    ok = True
+    tri_want = {}
+    for k, (kind, o) in enumerate(zip(kinds, objs)):
+        if kind == "tri":
+            if o not in tri_want:
+                L = graphs[o]
+                c = torch.zeros(1, dtype=torch.int64, device=ctx["dev"])
+                bale.triangle_dev(torch.from_numpy(L.offset).to(ctx["dev"]), torch.from_numpy(L.nonzero).to(ctx["dev"]), c)
+                tri_want[o] = int(c.item())
+            ok &= int(tri_out[k][0]) == tri_want[o]
+    k0 = kinds.index("ig")
+    t = bale.gen_values(tables[objs[k0]], 50 + objs[k0])
+    ok &= bool(np.array_equal(out_pool.numpy()[: min(sizes[k0], 1 << 20)],
+                              t[pinned[("ig", objs[k0])].numpy()[: min(sizes[k0], 1 << 20)]]))
+    s.close()
+    return {"metric": "served G items/s at saturation (updates + requests + edges), p50/p99 per offered rate",
+            "value": round(cap["items_per_s"] / 1e9, 4), "unit": "G items/s",
+            "ms_per_step": round(cap["makespan_s"] * 1e3, 3), "parity_ok": bool(ok),
+            "capacity_requests_per_s": round(cap_rate, 2),
+            "saturation": {"p50_ms": round(cap["p50_s"] * 1e3, 3), "p99_ms": round(cap["p99_s"] * 1e3, 3),
+                           "ticks": cap["ticks"], "max_active": cap["max_active"],
+                           "gpu_busy_s": round(cap["gpu_busy_s"], 4), "loop_iters": cap["loop_iters"],
+                           "tasks": cap["tasks"]},
+            "rates": rates, "gpu_launches": cap["ticks"],
+            "config": {"workload": "serving: Poisson arrivals, 60% ig / 30% histo / 10% triangles, 200 requests, "
+                                   "8 resident tables (1K-64M entries), 8 counter arrays (1K-16M), "
+                                   "6 resident R-MAT graphs (scales 12-20); request sizes log-uniform "
+                                   "(ig 10K-128M, histo 10K-64M); pinned host index and output buffers",
+                       "items_per_trace": items, "setup_s": round(gen_s, 1)}}
+
+
 def roofline(ctx, wl: str, algo_bytes: int, seconds: float, kernel: str, note: str | None = None) -> dict:
     peak = ctx["peak"]
     achieved = algo_bytes / seconds / 1e9
@@ -521,12 +624,13 @@ def run_gb300(args, dist: Dist) -> dict | None:
            "budget": args.cpu_budget}
     runners = {"ig": lambda: run_ig(ctx, False), "ig_zipf": lambda: run_ig(ctx, True),
                "histo": lambda: run_histo(ctx), "triangles": lambda: run_triangles(ctx),
-               "batch": lambda: run_batch(ctx), "batch_small": lambda: run_batch(ctx, small=True)}
+               "batch": lambda: run_batch(ctx), "batch_small": lambda: run_batch(ctx, small=True),
+               "serve": lambda: run_serve(ctx)}
     head = runners[args.workload]()
     torch.cuda.empty_cache()
     if not args.only:
         others = {}
-        for wl in ("ig_zipf", "histo", "triangles", "batch", "batch_small", "ig"):
+        for wl in ("ig_zipf", "histo", "triangles", "batch", "batch_small", "serve", "ig"):
             if wl != args.workload:
                 others[wl] = runners[wl]()
                 torch.cuda.empty_cache()
@@ -576,7 +680,7 @@ def main(argv=None) -> int:
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="ig", choices=["ig", "ig_zipf", "histo", "triangles", "batch", "batch_small"])
+    ap.add_argument("--workload", default="ig", choices=["ig", "ig_zipf", "histo", "triangles", "batch", "batch_small", "serve"])
     ap.add_argument("--only", action="store_true", help="measure the selected workload only")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=8.0, help="seconds of CPU baseline per workload")

@@ -194,6 +194,48 @@ BALE_API int bale_batch_bad(bale_batch_t *b, int64_t *bad, int64_t count);
 BALE_API int bale_batch_stats(bale_batch_t *b, int64_t *out, int n);
 BALE_API void bale_batch_destroy(bale_batch_t *b);
 
+/* ======================= serving loop =================================== */
+/* Continuous batching of arriving requests against objects kept resident    */
+/* in HBM (ig tables, histo counters, CSR graphs).  Registration and request */
+/* admission are by free device memory.  bale_server_run replays a trace in  */
+/* real time: requests are admitted as slots and arena space free up, cut    */
+/* into the batched kernel's tasks, and run in "ticks" over a slice of every */
+/* active request, so new requests join while long ones are running; results */
+/* are copied back as each request finishes.  New entry points; the         */
+/* reference has no serving form.                                           */
+typedef struct bale_server bale_server_t;
+typedef struct bale_request {
+  int32_t kind;          /* BALE_KIND_* */
+  int32_t object;        /* resident object id of the same kind */
+  int32_t shift;         /* 0, or 16 for packed indices */
+  int32_t reserved;
+  int64_t n;             /* ig: requests; histo: updates; triangles: 0 */
+  const int64_t *index;  /* host index array (ig, histo); pinned memory overlaps best */
+  int64_t *out;          /* host: ig values[n]; triangles one int64; histo NULL */
+  double arrival;        /* seconds after the start of bale_server_run */
+} bale_request_t;
+typedef struct bale_serve_stats {
+  double makespan_s, p50_s, p99_s, mean_s, items_per_s;
+  double gpu_busy_s;     /* sum of the ticks' device time (events) */
+  int64_t ticks, tasks, max_active, admission_waits, bad;
+  int64_t loop_iters;    /* host scheduling iterations */
+} bale_serve_stats_t;
+/* arena_bytes for per-request buffers (<= 0: a quarter of free HBM);       */
+/* max_active requests in flight (<= 0: 64).  NULL on failure.               */
+BALE_API bale_server_t *bale_server_create(int64_t arena_bytes, int max_active);
+/* Register resident objects; return the object id (>= 0) or -status        */
+/* (-BALE_EBUSY when free HBM would drop below the reserve).                */
+BALE_API int bale_server_add_table(bale_server_t *s, const int64_t *host_table, int64_t n);
+BALE_API int bale_server_add_counts(bale_server_t *s, int64_t ncounts);
+BALE_API int bale_server_add_graph(bale_server_t *s, const int64_t *offset, const int64_t *nonzero,
+                                   int64_t numrows, int64_t nnz);
+BALE_API int bale_server_read_counts(bale_server_t *s, int object, int64_t *host_counts, int64_t ncounts);
+/* Run the trace; latency[r] receives request r's seconds from arrival to   */
+/* completion; stats may be NULL.  Histo requests add into their counters.  */
+BALE_API int bale_server_run(bale_server_t *s, const bale_request_t *req, int64_t nreq, double *latency,
+                             bale_serve_stats_t *stats);
+BALE_API void bale_server_destroy(bale_server_t *s);
+
 /* ======================= no-allocation gather =========================== */
 /* No counterpart in the reference: an addition for callers that cannot      */
 /* allocate device memory when they call (HBM already reserved by another    */

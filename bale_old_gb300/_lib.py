@@ -47,7 +47,7 @@ class bale_request_t(C.Structure):
 
 class bale_serve_stats_t(C.Structure):
     _fields_ = [(f, C.c_double) for f in ("makespan_s", "p50_s", "p99_s", "mean_s", "items_per_s", "gpu_busy_s")] + \
-               [(f, i64) for f in ("ticks", "tasks", "max_active", "admission_waits", "bad", "loop_iters")]
+               [(f, i64) for f in ("ticks", "tasks", "max_active", "admission_waits", "bad", "loop_iters", "express")]
 
 # name -> (restype, argtypes)
 SIGNATURES: dict[str, tuple[object, list[object]]] = {

@@ -333,13 +333,14 @@ void destroy(bale_batch *b) {
   delete b;
 }
 
-bool aligned16(const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; }
+
+}  // namespace
+namespace q {
 
 // Would this instance use the region-partitioned kernels on its own?
 bool partition_worthy(const bale_instance_t &x) {
-  if (!aligned16(x.in) || !aligned16(x.out)) return false;
-  if (x.kind == BALE_KIND_IG) return ig_auto_partition(x.n, x.m) && ig_part_supported(x.n, x.m);
-  if (x.kind == BALE_KIND_HISTO) return histo_auto_partition(x.n, x.m) && x.m <= (int64_t(1024) << 22);
+  if (x.kind == BALE_KIND_IG) return ig_partition_for(x.n, x.m, x.out, x.in);
+  if (x.kind == BALE_KIND_HISTO) return histo_mode_for(x.n, x.m, x.in) == 3;
   return false;
 }
 
@@ -380,7 +381,7 @@ int launch_standalone(const bale_instance_t &x, unsigned long long *bad, void *w
                                 ws, words, 8, st);
 }
 
-}  // namespace
+}  // namespace q
 
 bool instance_valid(const bale_instance_t &x) {
   const bool ok_kind = x.kind == BALE_KIND_HISTO || x.kind == BALE_KIND_IG || x.kind == BALE_KIND_TRIANGLES;

@@ -50,5 +50,16 @@ int64_t queue_blocks();
 int launch_queue(const Task *d_tasks, int64_t ntasks, const Inst *d_inst, unsigned long long *words,
                  unsigned long long *bad, int64_t blocks, cudaStream_t stream);
 
+// Large instances run as their own specialised kernels instead of queue
+// tasks: the rule (batch.standalone* knobs and the partition thresholds),
+// their workspace, a relative cost for stream balancing, and the launch
+// (words: 4 zero-initialised device words of cursors).
+bool partition_worthy(const bale_instance_t &x);
+bool goes_standalone(const bale_instance_t &x);
+size_t standalone_ws(const bale_instance_t &x);
+double standalone_cost(const bale_instance_t &x);
+int launch_standalone(const bale_instance_t &x, unsigned long long *bad, void *ws, unsigned long long *words,
+                      cudaStream_t st);
+
 }  // namespace q
 }  // namespace bale

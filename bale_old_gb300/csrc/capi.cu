@@ -12,6 +12,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <mutex>
 
 #include "common.cuh"
@@ -126,15 +127,20 @@ struct DropinState {
 static std::mutex g_dropin_mu;
 static DropinState g_state[64];
 
+// One grow-only workspace per (device, stream): work on one stream runs in
+// order, so launches on the same stream may share it, while launches on
+// different streams (the batched graph's side streams, the serving loop's
+// express streams, callers' own streams) never see each other's data.
 static std::mutex g_ws_mu;
-static DevBuf g_ws[64];
+static std::map<std::pair<int, cudaStream_t>, DevBuf> g_ws;
 
-void *device_workspace(size_t bytes) {
+void *device_workspace(size_t bytes, cudaStream_t stream) {
   int d = current_device();
-  if (d < 0 || d >= 64) return nullptr;
+  if (d < 0) return nullptr;
   std::lock_guard<std::mutex> lk(g_ws_mu);
-  if (g_ws[d].ensure(bytes) != BALE_OK) return nullptr;
-  return g_ws[d].p;
+  DevBuf &b = g_ws[{d, stream}];
+  if (b.ensure(bytes) != BALE_OK) return nullptr;
+  return b.p;
 }
 
 static DropinState *dropin_state() {
@@ -390,7 +396,8 @@ void bale_release_buffers(void) {
   for (int d = 0; d < 64; d++)
     for (auto &b : g_state[d].buf) b.release();
   std::lock_guard<std::mutex> lk2(g_ws_mu);
-  for (int d = 0; d < 64; d++) g_ws[d].release();
+  for (auto &kv : g_ws) kv.second.release();
+  g_ws.clear();
 }
 
 int bale_histo_dev(int64_t *d_counts, int64_t ncounts, const int64_t *d_index, int64_t n, int shift,

@@ -38,11 +38,17 @@ DeviceScratch *device_scratch();
 unsigned long long *next_cursor_word();
 // k (<= 4) consecutive fresh scratch words, same ring and rules.
 unsigned long long *next_cursor_words(int k);
-// Grow-only per-device workspace for kernels that need scratch memory.  The
-// drop-ins and the device entry points share it, so launches that use it
-// must not overlap on different streams.  Returns nullptr (error set) on
-// allocation failure.
-void *device_workspace(size_t bytes);
+// Grow-only workspace for kernels that need scratch memory, one per (device,
+// stream): launches on one stream share it in stream order, launches on
+// different streams get their own.  Growing it frees the old buffer, which
+// waits for the device.  Returns nullptr (error set) on allocation failure.
+void *device_workspace(size_t bytes, cudaStream_t stream);
+// The launchers' choices, shared with the batched and serving planners so a
+// planner that supplies its own workspace takes the same path:
+// launch_histo's mode (0 shared memory, 1 aggregated, 2 plain, 3 partitioned)
+// and whether launch_ig uses the region partition.
+int histo_mode_for(int64_t n, int64_t ncounts, const int64_t *index);
+bool ig_partition_for(int64_t n, int64_t table_len, const int64_t *tgt, const int64_t *index);
 
 #define BALE_CUDA_OK(expr)                                                        \
   do {                                                                            \

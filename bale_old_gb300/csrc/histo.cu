@@ -137,18 +137,15 @@ bool g_smem_attr_set[64] = {false};
 
 }  // namespace
 
-int launch_histo(int64_t *counts, int64_t ncounts, const int64_t *index, int64_t n, int shift,
-                 unsigned long long *bad, cudaStream_t stream) {
-  if (n <= 0) return BALE_OK;
-  const int sms = num_sms();
+// Mode: 0 shared-memory private table, 1 warp-aggregated L2 reductions,
+// 2 plain L2 reductions, 3 region-partitioned L2 reductions.  Automatic:
+// shared memory when the table fits; plain L2 reductions while the table
+// lives in L2 (uniform updates rarely collide inside a warp, so the
+// aggregation's __match_any_sync costs more than it saves -- it pays only
+// for skewed updates, which the tuner or the caller can select); the
+// region partition once the table is well beyond L2.
+int histo_mode_for(int64_t n, int64_t ncounts, const int64_t *index) {
   const bool aligned = (reinterpret_cast<uintptr_t>(index) & 15) == 0;
-  // Mode: 0 shared-memory private table, 1 warp-aggregated L2 reductions,
-  // 2 plain L2 reductions, 3 region-partitioned L2 reductions.  Automatic:
-  // shared memory when the table fits; plain L2 reductions while the table
-  // lives in L2 (uniform updates rarely collide inside a warp, so the
-  // aggregation's __match_any_sync costs more than it saves -- it pays only
-  // for skewed updates, which the tuner or the caller can select); the
-  // region partition once the table is well beyond L2.
   int64_t mode = knob("histo.mode");
   if (mode < 0 || mode > 3) {
     if (ncounts <= kSmemMaxCounters) mode = 0;
@@ -158,8 +155,17 @@ int launch_histo(int64_t *counts, int64_t ncounts, const int64_t *index, int64_t
   if (mode == 0 && ncounts > kSmemMaxCounters) mode = 2;
   if (!aligned && (mode == 0 || mode == 3)) mode = 2;
   if (mode == 3 && ncounts > (int64_t(1024) << 22)) mode = 2;
+  return static_cast<int>(mode);
+}
+
+int launch_histo(int64_t *counts, int64_t ncounts, const int64_t *index, int64_t n, int shift,
+                 unsigned long long *bad, cudaStream_t stream) {
+  if (n <= 0) return BALE_OK;
+  const int sms = num_sms();
+  const bool aligned = (reinterpret_cast<uintptr_t>(index) & 15) == 0;
+  const int64_t mode = histo_mode_for(n, ncounts, index);
   if (mode == 3) {
-    void *ws = device_workspace(histo_part_workspace_bytes(n, ncounts));
+    void *ws = device_workspace(histo_part_workspace_bytes(n, ncounts), stream);
     unsigned long long *cursor = next_cursor_word();
     if (!ws || !cursor) return BALE_ENOMEM;
     return launch_histo_partitioned(counts, ncounts, index, n, shift, bad, ws, cursor, stream);

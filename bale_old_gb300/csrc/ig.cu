@@ -153,6 +153,14 @@ int g_l2_fetch_set[64];
 
 }  // namespace
 
+// Tables well beyond what L2 can hold go through the region-partitioned
+// gather (ig_part.cu) when there are enough requests to amortise its passes.
+bool ig_partition_for(int64_t n, int64_t table_len, const int64_t *tgt, const int64_t *index) {
+  const bool aligned = ((reinterpret_cast<uintptr_t>(tgt) | reinterpret_cast<uintptr_t>(index)) & 15) == 0;
+  const int64_t mode = knob("ig.mode");
+  return aligned && ig_part_supported(n, table_len) && (mode == 1 || (mode < 0 && ig_auto_partition(n, table_len)));
+}
+
 int launch_ig(int64_t *tgt, const int64_t *index, int64_t n, const int64_t *table,
               int64_t table_len, int shift, unsigned long long *bad, cudaStream_t stream) {
   if (n <= 0) return BALE_OK;
@@ -167,13 +175,8 @@ int launch_ig(int64_t *tgt, const int64_t *index, int64_t n, const int64_t *tabl
       g_l2_fetch_set[dev] = static_cast<int>(fetch + 1);
     }
   }
-  // Tables well beyond what L2 can hold go through the region-partitioned
-  // gather (ig_part.cu) when there are enough requests to amortise its passes.
-  const int64_t mode = knob("ig.mode");
-  const bool part = aligned && ig_part_supported(n, table_len) &&
-                    (mode == 1 || (mode < 0 && ig_auto_partition(n, table_len)));
-  if (part) {
-    void *ws = device_workspace(ig_part_workspace_bytes(n, table_len));
+  if (ig_partition_for(n, table_len, tgt, index)) {
+    void *ws = device_workspace(ig_part_workspace_bytes(n, table_len), stream);
     unsigned long long *cursor = next_cursor_word();
     if (!ws || !cursor) return BALE_ENOMEM;
     return launch_ig_partitioned(tgt, index, n, table, table_len, shift, bad, ws, cursor, stream);

@@ -14,6 +14,11 @@
 //    over a bounded slice of every active request's remaining tasks, so a
 //    request that arrives while a long one is running joins at the next tick
 //    instead of waiting for it to finish;
+//  * a request large enough to fill the GPU by itself (the batched form's
+//    standalone rule) skips the queue: it runs as its own specialised kernels
+//    (region-partitioned ig / histo, the heavy/light triangle kernels over the
+//    graph's resident 32-bit column copy) on one of a few express streams,
+//    concurrently with the ticks;
 //  * when a request's last task has run, its result is copied back on a copy
 //    stream (ig values, the triangle count) and its arena space is freed.
 //
@@ -45,6 +50,9 @@ struct Object {
   int64_t n = 0, m = 0;
   int64_t *d_a = nullptr;             // table / counts / row offsets
   int64_t *d_b = nullptr;             // graph nonzeros
+  char *d_c = nullptr;                // graphs: the triangle kernels' prepared form
+  uint32_t *col32 = nullptr, *heavy = nullptr;
+  unsigned long long *nheavy = nullptr;
   std::vector<int64_t> host_offsets;  // graphs: for the planner
 };
 
@@ -110,6 +118,8 @@ struct bale_server {
   int max_active = 64;
   int64_t reserve_bytes = int64_t(1) << 30;
   cudaStream_t s_compute = nullptr, s_up = nullptr, s_down = nullptr;
+  static constexpr int kExpress = 4;
+  cudaStream_t s_express[kExpress] = {};
 };
 
 namespace {
@@ -118,6 +128,8 @@ struct Active {
   ~Active() {
     if (uploaded) cudaEventDestroy(uploaded);
     if (downloaded) cudaEventDestroy(downloaded);
+    if (xstart) cudaEventDestroy(xstart);
+    if (xdone) cudaEventDestroy(xdone);
   }
   int64_t id = 0;
   char *buf = nullptr;
@@ -129,6 +141,11 @@ struct Active {
   cudaEvent_t uploaded = nullptr;
   cudaEvent_t downloaded = nullptr;
   bool downloading = false;
+  // express requests: their own kernels on an express stream
+  bool express = false, computed = false;
+  int lane = 0;
+  double xcost = 0;
+  cudaEvent_t xstart = nullptr, xdone = nullptr;
 };
 
 void server_free(bale_server *s) {
@@ -136,11 +153,14 @@ void server_free(bale_server *s) {
   for (auto &o : s->objects) {
     cudaFree(o.d_a);
     cudaFree(o.d_b);
+    cudaFree(o.d_c);
   }
   cudaFree(s->d_arena);
   if (s->s_compute) cudaStreamDestroy(s->s_compute);
   if (s->s_up) cudaStreamDestroy(s->s_up);
   if (s->s_down) cudaStreamDestroy(s->s_down);
+  for (auto st : s->s_express)
+    if (st) cudaStreamDestroy(st);
   delete s;
 }
 
@@ -196,7 +216,12 @@ bale_server_t *bale_server_create(int64_t arena_bytes, int max_active) {
   s->arena_bytes = static_cast<size_t>(arena_bytes);
   if (cudaStreamCreateWithFlags(&s->s_compute, cudaStreamNonBlocking) != cudaSuccess ||
       cudaStreamCreateWithFlags(&s->s_up, cudaStreamNonBlocking) != cudaSuccess ||
-      cudaStreamCreateWithFlags(&s->s_down, cudaStreamNonBlocking) != cudaSuccess) {
+      cudaStreamCreateWithFlags(&s->s_down, cudaStreamNonBlocking) != cudaSuccess ||
+      [&] {
+        for (auto &st : s->s_express)
+          if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) return true;
+        return false;
+      }()) {
     set_error("bale_server_create: stream creation failed");
     server_free(s);
     return nullptr;
@@ -248,22 +273,36 @@ int bale_server_add_graph(bale_server_t *s, const int64_t *offset, const int64_t
   o.kind = BALE_KIND_TRIANGLES;
   o.n = numrows;
   o.m = nnz;
-  void *a = nullptr, *b = nullptr;
-  int rc = admit_alloc(s, &a, static_cast<size_t>(numrows + 1) * 8 + static_cast<size_t>(nnz) * 8);
+  // the CSR arrays plus the triangle kernels' prepared form (32-bit column
+  // copy, heavy-row list and its length), built once here
+  const size_t hyb = (tri_hybrid_workspace_bytes(numrows, nnz) + 255) & ~size_t(255);
+  void *a = nullptr, *b = nullptr, *c = nullptr;
+  int rc = admit_alloc(s, &a, static_cast<size_t>(numrows + 1) * 8 + static_cast<size_t>(nnz) * 8 + hyb + 256);
   if (rc != BALE_OK) return -rc;
-  cudaFree(a);  // admitted: allocate the two arrays
+  cudaFree(a);  // admitted: allocate the three arrays
+  a = nullptr;
   if (cudaMalloc(&a, static_cast<size_t>(numrows + 1) * 8) != cudaSuccess ||
-      cudaMalloc(&b, static_cast<size_t>(nnz > 0 ? nnz : 1) * 8) != cudaSuccess) {
+      cudaMalloc(&b, static_cast<size_t>(nnz > 0 ? nnz : 1) * 8) != cudaSuccess ||
+      cudaMalloc(&c, hyb + 256) != cudaSuccess) {
     cudaGetLastError();
     cudaFree(a);
+    cudaFree(b);
     return -BALE_ENOMEM;
   }
   o.d_a = static_cast<int64_t *>(a);
   o.d_b = static_cast<int64_t *>(b);
+  o.d_c = static_cast<char *>(c);
+  o.col32 = reinterpret_cast<uint32_t *>(o.d_c);
+  o.heavy = reinterpret_cast<uint32_t *>(o.d_c + ((static_cast<size_t>(nnz > 0 ? nnz : 1) * 4 + 255) & ~size_t(255)));
+  o.nheavy = reinterpret_cast<unsigned long long *>(o.d_c + hyb);
   if (cudaMemcpy(o.d_a, offset, static_cast<size_t>(numrows + 1) * 8, cudaMemcpyHostToDevice) != cudaSuccess ||
-      (nnz && cudaMemcpy(o.d_b, nonzero, static_cast<size_t>(nnz) * 8, cudaMemcpyHostToDevice) != cudaSuccess)) {
+      (nnz && cudaMemcpy(o.d_b, nonzero, static_cast<size_t>(nnz) * 8, cudaMemcpyHostToDevice) != cudaSuccess) ||
+      tri_hybrid_prepare(o.d_a, o.d_b, numrows, nnz, o.col32, o.heavy, o.nheavy, s->s_compute) != BALE_OK ||
+      cudaStreamSynchronize(s->s_compute) != cudaSuccess) {
+    cudaGetLastError();
     cudaFree(a);
     cudaFree(b);
+    cudaFree(c);
     return -BALE_ECUDA;
   }
   o.host_offsets.assign(offset, offset + numrows + 1);
@@ -306,7 +345,7 @@ int bale_server_run(bale_server_t *s, const bale_request_t *req, int64_t nreq, d
   int rc = BALE_OK;
   // device arrays indexed by request id: instance records, bad counts, triangle counts
   Inst *d_inst = nullptr;
-  unsigned long long *d_bad = nullptr, *d_tri = nullptr, *d_words = nullptr;
+  unsigned long long *d_bad = nullptr, *d_tri = nullptr, *d_words = nullptr, *d_xwords = nullptr;
   constexpr int kSlots = 2;  // ticks in flight: the next one is queued while one runs
   Task *d_tasks[kSlots] = {nullptr, nullptr};
   Task *h_tasks[kSlots] = {nullptr, nullptr};
@@ -317,6 +356,11 @@ int bale_server_run(bale_server_t *s, const bale_request_t *req, int64_t nreq, d
   const double tick_cost = static_cast<double>(knob_or("serve.tick_cost", int64_t(1) << 24));
   const double req_cost = static_cast<double>(knob_or("serve.request_cost", int64_t(1) << 22));  // floor
   const int64_t blocks = q::queue_blocks();
+  const bool express_on = knob("serve.express") != 0;
+  const int nlanes = static_cast<int>(
+      std::min<int64_t>(bale_server::kExpress, std::max<int64_t>(1, knob_or("serve.express_streams", 2))));
+  const int rows_per_fetch = static_cast<int>(knob_or("tri.rows_per_fetch", 8));
+  double lane_load[bale_server::kExpress] = {0, 0, 0, 0};
 #define SRV_CUDA(expr)                                                                 \
   do {                                                                                 \
     cudaError_t _e = (expr);                                                           \
@@ -332,6 +376,7 @@ int bale_server_run(bale_server_t *s, const bale_request_t *req, int64_t nreq, d
     SRV_CUDA(cudaMalloc(&d_bad, sizeof(unsigned long long) * static_cast<size_t>(nreq)));
     SRV_CUDA(cudaMalloc(&d_tri, sizeof(unsigned long long) * static_cast<size_t>(nreq)));
     SRV_CUDA(cudaMalloc(&d_words, sizeof(unsigned long long) * 2));
+    SRV_CUDA(cudaMalloc(&d_xwords, sizeof(unsigned long long) * 4 * static_cast<size_t>(nreq)));
     for (int k = 0; k < kSlots; k++) {
       SRV_CUDA(cudaMalloc(&d_tasks[k], sizeof(Task) * static_cast<size_t>(task_cap)));
       SRV_CUDA(cudaMallocHost(&h_tasks[k], sizeof(Task) * static_cast<size_t>(task_cap)));
@@ -376,8 +421,29 @@ int bale_server_run(bale_server_t *s, const bale_request_t *req, int64_t nreq, d
         const int64_t id = pending.front();
         const bale_request_t &x = req[id];
         const Object &o = s->objects[static_cast<size_t>(x.object)];
-        const size_t need = x.kind == BALE_KIND_IG ? 16 * static_cast<size_t>(x.n)
-                            : x.kind == BALE_KIND_HISTO ? 8 * static_cast<size_t>(x.n) : 0;
+        // the public instance, with the arena pointers filled in once allocated
+        bale_instance_t inst;
+        inst.kind = x.kind;
+        inst.shift = x.shift;
+        inst.n = x.kind == BALE_KIND_TRIANGLES ? o.n : x.n;
+        inst.m = x.kind == BALE_KIND_TRIANGLES ? o.m : o.n;
+        inst.in = inst.aux = nullptr;
+        inst.out = nullptr;
+        size_t io = x.kind == BALE_KIND_IG ? 16 * static_cast<size_t>(x.n)
+                    : x.kind == BALE_KIND_HISTO ? 8 * static_cast<size_t>(x.n) : 0;
+        io = (io + 255) & ~size_t(255);
+        bool express = false;
+        size_t ws = 0;
+        if (express_on) {
+          bale_instance_t probe = inst;  // any 256-aligned pointers decide the rule
+          probe.in = probe.aux = reinterpret_cast<const int64_t *>(s->d_arena);
+          probe.out = reinterpret_cast<int64_t *>(s->d_arena);
+          express = x.kind == BALE_KIND_TRIANGLES
+                        ? o.m > 0 && o.m >= knob_or("batch.standalone_min_edges", int64_t(1) << 21)
+                        : q::goes_standalone(probe);
+          if (express && x.kind != BALE_KIND_TRIANGLES) ws = q::standalone_ws(probe);
+        }
+        const size_t need = io + ws;
         char *buf = need ? arena.alloc(need) : nullptr;
         if (need && !buf) {
           if (!waited[static_cast<size_t>(id)]) st.admission_waits++;
@@ -390,13 +456,9 @@ int bale_server_run(bale_server_t *s, const bale_request_t *req, int64_t nreq, d
         a->id = id;
         a->buf = buf;
         a->buf_bytes = need;
+        a->express = express;
         SRV_CUDA(cudaEventCreateWithFlags(&a->uploaded, cudaEventDisableTiming));
         SRV_CUDA(cudaEventCreateWithFlags(&a->downloaded, cudaEventDisableTiming));
-        bale_instance_t inst;
-        inst.kind = x.kind;
-        inst.shift = x.shift;
-        inst.n = x.kind == BALE_KIND_TRIANGLES ? o.n : x.n;
-        inst.m = x.kind == BALE_KIND_TRIANGLES ? o.m : o.n;
         if (x.kind == BALE_KIND_IG) {
           inst.in = reinterpret_cast<int64_t *>(buf);
           inst.out = reinterpret_cast<int64_t *>(buf) + x.n;
@@ -412,14 +474,38 @@ int bale_server_run(bale_server_t *s, const bale_request_t *req, int64_t nreq, d
         }
         if (x.kind != BALE_KIND_TRIANGLES && x.n)
           SRV_CUDA(cudaMemcpyAsync(buf, x.index, 8 * static_cast<size_t>(x.n), cudaMemcpyHostToDevice, s->s_up));
-        h_inst[id] = q::make_inst(inst);
-        SRV_CUDA(cudaMemcpyAsync(d_inst + id, h_inst + id, sizeof(Inst), cudaMemcpyHostToDevice, s->s_up));
-        SRV_CUDA(cudaEventRecord(a->uploaded, s->s_up));
-        std::vector<Planned> plan;
-        q::plan_tasks(inst, static_cast<int32_t>(id), o.host_offsets.data(), plan);
-        for (auto &p : plan) {
-          a->tasks.push_back(p.t);
-          a->cost.push_back(p.cost);
+        if (express) {
+          SRV_CUDA(cudaEventRecord(a->uploaded, s->s_up));
+          // the least loaded express stream runs it once its index is on the device
+          int lane = 0;
+          for (int l = 1; l < nlanes; l++)
+            if (lane_load[l] < lane_load[lane]) lane = l;
+          a->lane = lane;
+          a->xcost = q::standalone_cost(inst);
+          lane_load[lane] += a->xcost;
+          cudaStream_t xs = s->s_express[lane];
+          SRV_CUDA(cudaEventCreate(&a->xstart));
+          SRV_CUDA(cudaEventCreate(&a->xdone));
+          SRV_CUDA(cudaStreamWaitEvent(xs, a->uploaded, 0));
+          SRV_CUDA(cudaEventRecord(a->xstart, xs));
+          if (x.kind == BALE_KIND_TRIANGLES)
+            rc = tri_hybrid_run(o.d_a, o.col32, o.heavy, o.nheavy, o.n, o.m, d_tri + id, nullptr, d_bad + id,
+                                d_xwords + 4 * id, rows_per_fetch, xs);
+          else
+            rc = q::launch_standalone(inst, d_bad + id, buf + io, d_xwords + 4 * id, xs);
+          if (rc != BALE_OK) goto done;
+          SRV_CUDA(cudaEventRecord(a->xdone, xs));
+          st.express++;
+        } else {
+          h_inst[id] = q::make_inst(inst);
+          SRV_CUDA(cudaMemcpyAsync(d_inst + id, h_inst + id, sizeof(Inst), cudaMemcpyHostToDevice, s->s_up));
+          SRV_CUDA(cudaEventRecord(a->uploaded, s->s_up));
+          std::vector<Planned> plan;
+          q::plan_tasks(inst, static_cast<int32_t>(id), o.host_offsets.data(), plan);
+          for (auto &p : plan) {
+            a->tasks.push_back(p.t);
+            a->cost.push_back(p.cost);
+          }
         }
         items += static_cast<double>(x.kind == BALE_KIND_TRIANGLES ? o.m : x.n);
         st.max_active = std::max<int64_t>(st.max_active, static_cast<int64_t>(active.size()));
@@ -440,10 +526,25 @@ int bale_server_run(bale_server_t *s, const bale_request_t *req, int64_t nreq, d
           SRV_CUDA(e);
         }
       }
+      // ---- express requests whose kernels finished ----
+      for (auto &ap : active) {
+        Active *a = ap.get();
+        if (!a->express || a->computed) continue;
+        cudaError_t e = cudaEventQuery(a->xdone);
+        if (e == cudaSuccess) {
+          a->computed = true;
+          lane_load[a->lane] -= a->xcost;
+          float ms = 0.f;
+          if (cudaEventElapsedTime(&ms, a->xstart, a->xdone) == cudaSuccess) st.gpu_busy_s += ms * 1e-3;
+          progressed = true;
+        } else if (e != cudaErrorNotReady) {
+          SRV_CUDA(e);
+        }
+      }
       // ---- requests whose tasks all ran: copy results back ----
       for (auto &ap : active) {
         Active *a = ap.get();
-        if (a->downloading || a->finished < a->tasks.size()) continue;
+        if (a->downloading || (a->express ? !a->computed : a->finished < a->tasks.size())) continue;
         const bale_request_t &x = req[a->id];
         if (x.kind == BALE_KIND_IG && x.n)
           SRV_CUDA(cudaMemcpyAsync(x.out, a->buf + 8 * x.n, 8 * static_cast<size_t>(x.n), cudaMemcpyDeviceToHost,
@@ -526,6 +627,7 @@ int bale_server_run(bale_server_t *s, const bale_request_t *req, int64_t nreq, d
       }
     }
     SRV_CUDA(cudaStreamSynchronize(s->s_compute));
+    for (int l = 0; l < nlanes; l++) SRV_CUDA(cudaStreamSynchronize(s->s_express[l]));
     st.makespan_s = now_s() - t0;
     st.items_per_s = st.makespan_s > 0 ? items / st.makespan_s : 0;
     {
@@ -553,6 +655,7 @@ done:
   cudaFree(d_bad);
   cudaFree(d_tri);
   cudaFree(d_words);
+  cudaFree(d_xwords);
   for (int k = 0; k < kSlots; k++) {
     cudaFree(d_tasks[k]);
     if (h_tasks[k]) cudaFreeHost(h_tasks[k]);

@@ -167,7 +167,7 @@ int launch_triangle(const int64_t *offset, const int64_t *nonzero, int64_t numro
   if (mode != 0 && numrows < 0xffffffffll) {
     int64_t rpf_h = knob("tri.rows_per_fetch");
     if (rpf_h < 1 || rpf_h > 4096) rpf_h = 8;
-    void *ws = device_workspace(tri_hybrid_workspace_bytes(numrows, nnz));
+    void *ws = device_workspace(tri_hybrid_workspace_bytes(numrows, nnz), stream);
     unsigned long long *words = next_cursor_words(3);
     if (!ws || !words) return BALE_ENOMEM;
     return launch_triangle_hybrid(offset, nonzero, numrows, nnz, count, work, bad, ws, words,

@@ -59,6 +59,8 @@ Knob g_knobs[] = {
     {"serve.request_cost", -1},   // work one request may add to a tick (2^22)
     {"serve.tick_tasks", -1},     // tasks per tick (4096)
     {"serve.reserve_bytes", -1},  // free HBM a registration must leave (1 GiB)
+    {"serve.express", -1},          // 0: every request goes through the queue kernel
+    {"serve.express_streams", -1},  // express streams (2, at most 4)
     {"tri.mode", -1},           // 0 warp-per-row merge for every row, 1 bitmap/search hybrid
 };
 std::mutex g_mu;

@@ -484,6 +484,8 @@ def run_serve(ctx) -> dict:
     out_pool = torch.empty(out_total, dtype=torch.int64).pin_memory()
     tri_out = np.zeros((nreq, 1), np.int64)
     items = sum(sizes) + sum(graphs[o].nnz for k, o in zip(kinds, objs) if k == "tri")
+    h2d = 8 * sum(sizes)  # index arrays of the ig and histo requests
+    d2h = 8 * sum(n for k, n in zip(kinds, sizes) if k == "ig") + 8 * kinds.count("tri")
     gen_s = time.perf_counter() - t0
 
     def trace(arrivals):
@@ -509,7 +511,8 @@ def run_serve(ctx) -> dict:
                       "p50_ms": round(st["p50_s"] * 1e3, 3), "p99_ms": round(st["p99_s"] * 1e3, 3),
                       "mean_ms": round(st["mean_s"] * 1e3, 3), "items_per_s": round(st["items_per_s"], 1),
                       "makespan_s": round(st["makespan_s"], 4), "ticks": st["ticks"],
-                      "max_active": st["max_active"], "admission_waits": st["admission_waits"]})
+                      "max_active": st["max_active"], "admission_waits": st["admission_waits"],
+                      "express_requests": st["express"]})
     # exactness of the last run: triangle counts and a sample of ig values
     ok = True
     tri_want = {}
@@ -533,13 +536,14 @@ def run_serve(ctx) -> dict:
             "saturation": {"p50_ms": round(cap["p50_s"] * 1e3, 3), "p99_ms": round(cap["p99_s"] * 1e3, 3),
                            "ticks": cap["ticks"], "max_active": cap["max_active"],
                            "gpu_busy_s": round(cap["gpu_busy_s"], 4), "loop_iters": cap["loop_iters"],
-                           "tasks": cap["tasks"]},
+                           "tasks": cap["tasks"], "express_requests": cap["express"]},
             "rates": rates, "gpu_launches": cap["ticks"],
             "config": {"workload": "serving: Poisson arrivals, 60% ig / 30% histo / 10% triangles, 200 requests, "
                                    "8 resident tables (1K-64M entries), 8 counter arrays (1K-16M), "
                                    "6 resident R-MAT graphs (scales 12-20); request sizes log-uniform "
                                    "(ig 10K-128M, histo 10K-64M); pinned host index and output buffers",
-                       "items_per_trace": items, "setup_s": round(gen_s, 1)}}
+                       "items_per_trace": items, "h2d_bytes_per_trace": h2d, "d2h_bytes_per_trace": d2h,
+                       "setup_s": round(gen_s, 1)}}
 
 
 def roofline(ctx, wl: str, algo_bytes: int, seconds: float, kernel: str, note: str | None = None) -> dict:

@@ -200,8 +200,10 @@ BALE_API void bale_batch_destroy(bale_batch_t *b);
 /* admission are by free device memory.  bale_server_run replays a trace in  */
 /* real time: requests are admitted as slots and arena space free up, cut    */
 /* into the batched kernel's tasks, and run in "ticks" over a slice of every */
-/* active request, so new requests join while long ones are running; results */
-/* are copied back as each request finishes.  New entry points; the         */
+/* active request, so new requests join while long ones are running.  A    */
+/* request large enough to fill the GPU alone runs as its own specialised   */
+/* kernels on an express stream, beside the ticks.  Results are copied back */
+/* as each request finishes.  New entry points; the                         */
 /* reference has no serving form.                                           */
 typedef struct bale_server bale_server_t;
 typedef struct bale_request {
@@ -216,9 +218,10 @@ typedef struct bale_request {
 } bale_request_t;
 typedef struct bale_serve_stats {
   double makespan_s, p50_s, p99_s, mean_s, items_per_s;
-  double gpu_busy_s;     /* sum of the ticks' device time (events) */
+  double gpu_busy_s;     /* sum of the ticks' and express kernels' device time */
   int64_t ticks, tasks, max_active, admission_waits, bad;
   int64_t loop_iters;    /* host scheduling iterations */
+  int64_t express;       /* requests run as their own kernels on express streams */
 } bale_serve_stats_t;
 /* arena_bytes for per-request buffers (<= 0: a quarter of free HBM);       */
 /* max_active requests in flight (<= 0: 64).  NULL on failure.               */

@@ -75,6 +75,47 @@ def test_mixed_trace_is_exact(cuda, bale, oracle):
         _check(oracle, world, s, reqs, expect)
 
 
+class knobs:
+    """Set tuning knobs for a block, restoring the previous values after."""
+
+    def __init__(self, bale, **kv):
+        self.bale, self.kv = bale, {k.replace("__", "."): v for k, v in kv.items()}
+
+    def __enter__(self):
+        self.old = {k: self.bale.tune_get(k) for k in self.kv}
+        for k, v in self.kv.items():
+            self.bale.tune_set(k, v)
+
+    def __exit__(self, *exc):
+        for k, v in self.old.items():
+            self.bale.tune_set(k, v)
+
+
+# thresholds low enough that most requests of the trace run as express
+# kernels, on both the direct and the region-partitioned ig / histo paths
+EXPRESS_RULES = dict(batch__standalone_min=1 << 14, batch__standalone_min_edges=1 << 10,
+                     ig__part_min_table_bytes=1 << 20, ig__part_min_requests=1 << 16,
+                     histo__part_min_table_bytes=1 << 20, histo__part_min_updates=1 << 16)
+
+
+@pytest.mark.parametrize("express", [0, 1])
+def test_express_requests_are_exact(cuda, bale, oracle, express):
+    """Large requests on their own kernels beside the ticks: same results."""
+    from bale_old_gb300 import serve
+
+    with knobs(bale, serve__express=express, serve__express_streams=3, **EXPRESS_RULES):
+        with serve.Server(arena_bytes=1 << 30, max_active=24) as s:
+            world = _world(bale, serve, s, 11)
+            reqs, expect = _trace(bale, serve, world, 120, seed=13, rate=10_000.0)
+            lat, st = s.run(reqs)
+            assert st["bad"] == 0 and (lat > 0).all()
+            if express:
+                assert st["express"] > 10 and st["ticks"] > 0
+            else:
+                assert st["express"] == 0
+            _check(oracle, world, s, reqs, expect)
+
+
 def test_result_is_the_same_alone_and_in_the_mix(cuda, bale, oracle):
     """Run a trace, then each request again on its own: identical results."""
     from bale_old_gb300 import serve

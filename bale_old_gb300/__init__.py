@@ -286,6 +286,41 @@ def triangle_dev(offset, nonzero, count, work=None, bad=None, stream=None) -> No
                                    _stream(stream)), "bale_triangle_dev")
 
 
+class TrianglePrepared:
+    """A device CSR counted repeatedly (bale_triangle_prepare): validation,
+    the 32-bit column copy and the transpose are built once; count() adds
+    the triangle count into a device int64 each call.  offset/nonzero must
+    stay alive and unchanged until close()."""
+
+    def __init__(self, offset, nonzero, bad=None, stream=None):
+        self._keep = (offset, nonzero)
+        h = _lib.bale_triangle_prepare(_dptr(offset, "offset"), _dptr(nonzero, "nonzero"), offset.numel() - 1,
+                                       nonzero.numel(), _dptr(bad, "bad") if bad is not None else None,
+                                       _stream(stream))
+        if not h:
+            raise BaleError(f"bale_triangle_prepare: {_last_error()}")
+        self._h = h
+
+    def count(self, count, work=None, stream=None) -> None:
+        _status(_lib.bale_triangle_count_prepared(self._h, _dptr(count, "count"),
+                                                  _dptr(work, "work") if work is not None else None,
+                                                  _stream(stream)), "bale_triangle_count_prepared")
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            _lib.bale_triangle_release(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
 # --------------------------------------------------------------------------
 # seeded inputs (include/bale_inputs.h)
 # --------------------------------------------------------------------------

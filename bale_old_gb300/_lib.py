@@ -82,6 +82,9 @@ SIGNATURES: dict[str, tuple[object, list[object]]] = {
     "bale_histo_dev": (C.c_int, [VP, i64, VP, i64, C.c_int, VP, VP]),
     "bale_ig_dev": (C.c_int, [VP, VP, i64, VP, i64, C.c_int, VP, VP]),
     "bale_triangle_dev": (C.c_int, [VP, VP, i64, i64, VP, VP, VP, VP]),
+    "bale_triangle_prepare": (VP, [VP, VP, i64, i64, VP, VP]),
+    "bale_triangle_count_prepared": (C.c_int, [VP, VP, VP, VP]),
+    "bale_triangle_release": (None, [VP]),
     "bale_batch_create": (VP, [PINST, i64]),
     "bale_batch_run": (C.c_int, [VP, VP]),
     "bale_batch_bad": (C.c_int, [VP, P64, i64]),

@@ -358,12 +358,13 @@ size_t standalone_ws(const bale_instance_t &x) {
   size_t need = 0;
   if (x.kind == BALE_KIND_IG && partition_worthy(x)) need = ig_part_workspace_bytes(x.n, x.m);
   else if (x.kind == BALE_KIND_HISTO && partition_worthy(x)) need = histo_part_workspace_bytes(x.n, x.m);
-  else if (x.kind == BALE_KIND_TRIANGLES) need = tri_hybrid_workspace_bytes(x.n, x.m);
+  else if (x.kind == BALE_KIND_TRIANGLES)
+    need = tri_wedge_supported(x.n, x.m) ? tri_wedge_workspace_bytes(x.n, x.m) : tri_hybrid_workspace_bytes(x.n, x.m);
   return (need + 255) & ~size_t(255);
 }
 
 double standalone_cost(const bale_instance_t &x) {
-  if (x.kind == BALE_KIND_TRIANGLES) return 30.0 * static_cast<double>(x.m);
+  if (x.kind == BALE_KIND_TRIANGLES) return 15.0 * static_cast<double>(x.m);
   return static_cast<double>(x.n) * (x.kind == BALE_KIND_IG ? 1.5 : 1.0);
 }
 
@@ -377,6 +378,9 @@ int launch_standalone(const bale_instance_t &x, unsigned long long *bad, void *w
     if (partition_worthy(x)) return launch_histo_partitioned(x.out, x.m, x.in, x.n, x.shift, bad, ws, words, st);
     return launch_histo(x.out, x.m, x.in, x.n, x.shift, bad, st);
   }
+  if (tri_wedge_supported(x.n, x.m))
+    return launch_triangle_wedge(x.in, x.aux, x.n, x.m, reinterpret_cast<unsigned long long *>(x.out), nullptr, bad,
+                                 ws, words, st);
   return launch_triangle_hybrid(x.in, x.aux, x.n, x.m, reinterpret_cast<unsigned long long *>(x.out), nullptr, bad,
                                 ws, words, 8, st);
 }

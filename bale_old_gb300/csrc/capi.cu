@@ -13,6 +13,7 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <new>
 #include <mutex>
 
 #include "common.cuh"
@@ -440,6 +441,70 @@ int bale_triangle_dev(const int64_t *d_offset, const int64_t *d_nonzero, int64_t
   return launch_triangle(d_offset, d_nonzero, numrows, nnz, reinterpret_cast<unsigned long long *>(d_count),
                          reinterpret_cast<unsigned long long *>(d_work), bad,
                          static_cast<cudaStream_t>(stream));
+}
+
+struct bale_tri_prepared {
+  const int64_t *offset = nullptr, *nonzero = nullptr;
+  int64_t numrows = 0, nnz = 0;
+  bool wedge = false;        // else each count runs the general path
+  void *ws = nullptr;        // the wedge kernels' prepared form
+  unsigned long long *cursor = nullptr;
+};
+
+bale_tri_prepared_t *bale_triangle_prepare(const int64_t *d_offset, const int64_t *d_nonzero, int64_t numrows,
+                                           int64_t nnz, int64_t *d_bad, void *stream) {
+  if (numrows < 0 || nnz < 0 || (numrows > 0 && !d_offset) || (nnz > 0 && !d_nonzero)) {
+    set_error("bale_triangle_prepare: bad arguments");
+    return nullptr;
+  }
+  bale_tri_prepared *g = new (std::nothrow) bale_tri_prepared();
+  if (!g) {
+    set_error("bale_triangle_prepare: out of host memory");
+    return nullptr;
+  }
+  g->offset = d_offset;
+  g->nonzero = d_nonzero;
+  g->numrows = numrows;
+  g->nnz = nnz;
+  const int64_t mode = knob("tri.mode");
+  g->wedge = (mode < 0 || mode == 2) && tri_wedge_supported(numrows, nnz);
+  if (g->wedge) {
+    DeviceScratch *ds = device_scratch();
+    const size_t bytes = tri_wedge_workspace_bytes(numrows, nnz);
+    if (!ds || cudaMalloc(&g->ws, bytes) != cudaSuccess || cudaMalloc(&g->cursor, 8) != cudaSuccess) {
+      cudaGetLastError();
+      set_error("bale_triangle_prepare: cudaMalloc of %zu bytes failed", bytes);
+      bale_triangle_release(g);
+      return nullptr;
+    }
+    unsigned long long *bad = d_bad ? reinterpret_cast<unsigned long long *>(d_bad) : ds->words + kWordDiscard;
+    if (tri_wedge_prepare(d_offset, d_nonzero, numrows, nnz, g->ws, bad, static_cast<cudaStream_t>(stream)) !=
+        BALE_OK) {
+      bale_triangle_release(g);
+      return nullptr;
+    }
+  }
+  return g;
+}
+
+int bale_triangle_count_prepared(bale_tri_prepared_t *g, int64_t *d_count, int64_t *d_work, void *stream) {
+  if (!g || !d_count) {
+    set_error("bale_triangle_count_prepared: bad arguments");
+    return BALE_EINVAL;
+  }
+  if (g->numrows == 0) return BALE_OK;
+  if (!g->wedge)
+    return bale_triangle_dev(g->offset, g->nonzero, g->numrows, g->nnz, d_count, d_work, nullptr, stream);
+  return tri_wedge_run(g->offset, g->ws, g->numrows, g->nnz, reinterpret_cast<unsigned long long *>(d_count),
+                       reinterpret_cast<unsigned long long *>(d_work), g->cursor, static_cast<cudaStream_t>(stream));
+}
+
+void bale_triangle_release(bale_tri_prepared_t *g) {
+  if (!g) return;
+  if (g->ws || g->cursor) cudaDeviceSynchronize();  // no count in flight may still read them
+  cudaFree(g->ws);
+  cudaFree(g->cursor);
+  delete g;
 }
 
 }  // extern "C"

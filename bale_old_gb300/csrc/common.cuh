@@ -94,6 +94,20 @@ int tri_hybrid_run(const int64_t *offset, const uint32_t *col32, const uint32_t 
                    const unsigned long long *nheavy, int64_t numrows, int64_t nnz, unsigned long long *count,
                    unsigned long long *work, unsigned long long *bad, unsigned long long *cursors,
                    int rows_per_fetch, cudaStream_t stream);
+// Wedge-probe triangle count (tri_wedge.cu), for fewer than 2^32 - 1 rows and
+// about 2^32 nonzeros.  prepare builds the u32 column copy and the transpose
+// into ws (tri_wedge_workspace_bytes) and adds malformed entries to *bad (may
+// be NULL); run counts from a prepared ws (cursor: one device word, zeroed
+// there); launch_triangle_wedge does both.
+bool tri_wedge_supported(int64_t numrows, int64_t nnz);
+size_t tri_wedge_workspace_bytes(int64_t numrows, int64_t nnz);
+int tri_wedge_prepare(const int64_t *offset, const int64_t *nonzero, int64_t numrows, int64_t nnz, void *ws,
+                      unsigned long long *bad, cudaStream_t stream);
+int tri_wedge_run(const int64_t *offset, const void *ws, int64_t numrows, int64_t nnz, unsigned long long *count,
+                  unsigned long long *work, unsigned long long *cursor, cudaStream_t stream);
+int launch_triangle_wedge(const int64_t *offset, const int64_t *nonzero, int64_t numrows, int64_t nnz,
+                          unsigned long long *count, unsigned long long *work, unsigned long long *bad, void *ws,
+                          unsigned long long *cursor, cudaStream_t stream);
 // max over index[i] >> shift into *out (u64, must start at 0); negatives count as huge.
 int launch_index_max(const int64_t *index, int64_t n, int shift, unsigned long long *out,
                      cudaStream_t stream);

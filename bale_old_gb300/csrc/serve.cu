@@ -51,6 +51,7 @@ struct Object {
   int64_t *d_a = nullptr;             // table / counts / row offsets
   int64_t *d_b = nullptr;             // graph nonzeros
   char *d_c = nullptr;                // graphs: the triangle kernels' prepared form
+  bool wedge = false;                 // ... for the wedge kernels (else the hybrid's)
   uint32_t *col32 = nullptr, *heavy = nullptr;
   unsigned long long *nheavy = nullptr;
   std::vector<int64_t> host_offsets;  // graphs: for the planner
@@ -273,9 +274,12 @@ int bale_server_add_graph(bale_server_t *s, const int64_t *offset, const int64_t
   o.kind = BALE_KIND_TRIANGLES;
   o.n = numrows;
   o.m = nnz;
-  // the CSR arrays plus the triangle kernels' prepared form (32-bit column
-  // copy, heavy-row list and its length), built once here
-  const size_t hyb = (tri_hybrid_workspace_bytes(numrows, nnz) + 255) & ~size_t(255);
+  // the CSR arrays plus the triangle kernels' prepared form, built once here:
+  // the wedge kernels' column copy and transpose, or (beyond their 2^32
+  // limits) the hybrid's column copy and heavy-row list
+  o.wedge = tri_wedge_supported(numrows, nnz);
+  const size_t hyb = (o.wedge ? tri_wedge_workspace_bytes(numrows, nnz) : tri_hybrid_workspace_bytes(numrows, nnz)) +
+                     256;
   void *a = nullptr, *b = nullptr, *c = nullptr;
   int rc = admit_alloc(s, &a, static_cast<size_t>(numrows + 1) * 8 + static_cast<size_t>(nnz) * 8 + hyb + 256);
   if (rc != BALE_OK) return -rc;
@@ -292,17 +296,29 @@ int bale_server_add_graph(bale_server_t *s, const int64_t *offset, const int64_t
   o.d_a = static_cast<int64_t *>(a);
   o.d_b = static_cast<int64_t *>(b);
   o.d_c = static_cast<char *>(c);
+  unsigned long long *vbad = reinterpret_cast<unsigned long long *>(o.d_c + hyb);  // malformed entries
   o.col32 = reinterpret_cast<uint32_t *>(o.d_c);
   o.heavy = reinterpret_cast<uint32_t *>(o.d_c + ((static_cast<size_t>(nnz > 0 ? nnz : 1) * 4 + 255) & ~size_t(255)));
-  o.nheavy = reinterpret_cast<unsigned long long *>(o.d_c + hyb);
-  if (cudaMemcpy(o.d_a, offset, static_cast<size_t>(numrows + 1) * 8, cudaMemcpyHostToDevice) != cudaSuccess ||
-      (nnz && cudaMemcpy(o.d_b, nonzero, static_cast<size_t>(nnz) * 8, cudaMemcpyHostToDevice) != cudaSuccess) ||
-      tri_hybrid_prepare(o.d_a, o.d_b, numrows, nnz, o.col32, o.heavy, o.nheavy, s->s_compute) != BALE_OK ||
-      cudaStreamSynchronize(s->s_compute) != cudaSuccess) {
+  o.nheavy = reinterpret_cast<unsigned long long *>(o.d_c + hyb - 256);
+  unsigned long long h_bad = 0;
+  const bool ok =
+      cudaMemcpy(o.d_a, offset, static_cast<size_t>(numrows + 1) * 8, cudaMemcpyHostToDevice) == cudaSuccess &&
+      (nnz == 0 || cudaMemcpy(o.d_b, nonzero, static_cast<size_t>(nnz) * 8, cudaMemcpyHostToDevice) == cudaSuccess) &&
+      cudaMemsetAsync(vbad, 0, 8, s->s_compute) == cudaSuccess &&
+      (o.wedge ? tri_wedge_prepare(o.d_a, o.d_b, numrows, nnz, o.d_c, vbad, s->s_compute)
+               : tri_hybrid_prepare(o.d_a, o.d_b, numrows, nnz, o.col32, o.heavy, o.nheavy, s->s_compute)) ==
+          BALE_OK &&
+      cudaMemcpyAsync(&h_bad, vbad, 8, cudaMemcpyDeviceToHost, s->s_compute) == cudaSuccess &&
+      cudaStreamSynchronize(s->s_compute) == cudaSuccess;
+  if (!ok || h_bad) {
     cudaGetLastError();
     cudaFree(a);
     cudaFree(b);
     cudaFree(c);
+    if (h_bad) {
+      set_error("bale_server_add_graph: %llu malformed entries (rows must ascend inside [0,i))", h_bad);
+      return -BALE_EINPUT;
+    }
     return -BALE_ECUDA;
   }
   o.host_offsets.assign(offset, offset + numrows + 1);
@@ -488,7 +504,9 @@ int bale_server_run(bale_server_t *s, const bale_request_t *req, int64_t nreq, d
           SRV_CUDA(cudaEventCreate(&a->xdone));
           SRV_CUDA(cudaStreamWaitEvent(xs, a->uploaded, 0));
           SRV_CUDA(cudaEventRecord(a->xstart, xs));
-          if (x.kind == BALE_KIND_TRIANGLES)
+          if (x.kind == BALE_KIND_TRIANGLES && o.wedge)
+            rc = tri_wedge_run(o.d_a, o.d_c, o.n, o.m, d_tri + id, nullptr, d_xwords + 4 * id, xs);
+          else if (x.kind == BALE_KIND_TRIANGLES)
             rc = tri_hybrid_run(o.d_a, o.col32, o.heavy, o.nheavy, o.n, o.m, d_tri + id, nullptr, d_bad + id,
                                 d_xwords + 4 * id, rows_per_fetch, xs);
           else

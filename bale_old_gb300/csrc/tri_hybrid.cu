@@ -1,4 +1,5 @@
-// tri_hybrid.cu -- triangle counting, bitmap/search hybrid (default mode).
+// tri_hybrid.cu -- triangle counting, bitmap/search hybrid over rows i (tri.mode 1;
+// also the path for matrices beyond the wedge kernels' 32-bit limits).
 //
 // Same count as apps/triangle_src/triangle_agi.upc:69-99 (alg 0): for every
 // nonzero L[i][j] after the first of row i, |row_i and row_j|.  The rows of a

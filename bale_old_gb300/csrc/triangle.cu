@@ -161,9 +161,16 @@ int launch_triangle(const int64_t *offset, const int64_t *nonzero, int64_t numro
                     unsigned long long *count, unsigned long long *work, unsigned long long *bad,
                     cudaStream_t stream) {
   if (numrows <= 0) return BALE_OK;
-  // Default: the bitmap/search hybrid (tri_hybrid.cu); mode 0 keeps this
-  // file's warp-per-row merge kernel for every row.
+  // Default: wedge probes at the far vertex (tri_wedge.cu); mode 1 the
+  // bitmap/search hybrid over rows i (tri_hybrid.cu); mode 0 this file's
+  // warp-per-row merge kernel for every row.
   const int64_t mode = knob("tri.mode");
+  if ((mode < 0 || mode == 2) && tri_wedge_supported(numrows, nnz)) {
+    void *ws = device_workspace(tri_wedge_workspace_bytes(numrows, nnz), stream);
+    unsigned long long *cursor = next_cursor_word();
+    if (!ws || !cursor) return BALE_ENOMEM;
+    return launch_triangle_wedge(offset, nonzero, numrows, nnz, count, work, bad, ws, cursor, stream);
+  }
   if (mode != 0 && numrows < 0xffffffffll) {
     int64_t rpf_h = knob("tri.rows_per_fetch");
     if (rpf_h < 1 || rpf_h > 4096) rpf_h = 8;

@@ -349,19 +349,41 @@ def run_triangles(ctx) -> dict:
     per_step = int(cnt.item()) // (args.steps + args.warmup)
     deg = np.diff(L.offset)
     pulls = int(deg[L.nonzero].sum())
-    algo = 8 * (n + 1) + 8 * nnz + 8 * pulls
+    rowid = np.repeat(np.arange(n, dtype=np.int64), deg)
+    pos = np.arange(nnz, dtype=np.int64) - L.offset[rowid]
+    live = (pos > 0) & (deg[L.nonzero] > 0)
+    pushes = int(pos[live].sum())
+    records = int(live.sum())
+    del rowid, pos, live
+    # the dominant kernel alone: counting from a prepared graph (the wedge
+    # count kernel); its algorithmic bytes are the push model's -- every
+    # probed prefix element read once as a u32, the 8-byte prefix records,
+    # and rows j read twice (set and clear) as u32
+    wedge_bytes = 4 * pushes + 8 * records + 8 * nnz
+    with bale.TrianglePrepared(off, col) as g:
+        cnt2 = torch.zeros(1, dtype=torch.int64, device=dev)
+        count_ms = time_device(lambda: g.count(cnt2), args.steps, args.warmup, between)
+    count_ms = ctx["dist"].max(count_ms)
     out = {"metric": "edges/s triangle counting (nnz(L) per second)",
            "value": round(job_rate(nnz, ms_max / 1e3, ctx["dist"].world) / 1e9, 4), "unit": "Gedges/s",
            "ms_per_step": round(ms_max, 4), "triangles": per_step,
-           "roofline": roofline(ctx, "triangles", algo, ms / 1e3,
-                                "triangle hybrid (convert + classify + heavy bitmap + light search)",
-                                note="algorithmic bytes count every row-j element as an 8 B HBM read "
-                                     "(8(n+1) + 8 nnz + 8 pulls); repeated rows are L2 hits, so the "
-                                     "fraction can exceed 1"),
-           "clocks": clocks.summary(), "gpu_launches": 4 * args.steps,
+           "roofline": roofline(ctx, "triangles", wedge_bytes, count_ms / 1e3,
+                                "wedge_count_kernel (one warp per row j: bitmap / staged search over the "
+                                "incoming prefixes)",
+                                note="push work model: 4 B per probed prefix element (exstack pushes, "
+                                     "apps/triangle_src/triangle.upc:344-349), 8 B per prefix record, 8 B "
+                                     "per nonzero for row j; the step also runs the prepare kernels "
+                                     f"(validate, transpose), {round(ms_max - count_ms, 3)} ms of the "
+                                     f"{round(ms_max, 3)} ms step"),
+           "roofline_pull_model": {"algorithmic_bytes_per_step": 8 * (n + 1) + 8 * nnz + 8 * pulls,
+                                   "achieved_gbs": round((8 * (n + 1) + 8 * nnz + 8 * pulls) / ms_max * 1e-6, 1),
+                                   "note": "the AGI loop's pull model (8 B per row-j element scanned); the "
+                                           "wedge kernels probe 4x fewer elements, so this reads above 1"},
+           "count_kernel_ms": round(count_ms, 4),
+           "clocks": clocks.summary(), "gpu_launches": 7 * args.steps,
            "config": {"workload": "triangles: R-MAT scale 22, edge factor 16, (0.57,0.19,0.19,0.05), "
                                   "symmetrised, deduplicated, degree-ordered strictly lower L",
-                      "n": n, "nnz": nnz, "pulls": pulls, "generate_s": round(gen_s, 2),
+                      "n": n, "nnz": nnz, "pulls": pulls, "pushes": pushes, "generate_s": round(gen_s, 2),
                       "l2": "the 513 MiB CSR exceeds L2; a 256 MiB buffer is also rewritten between steps"}}
     del off, col, flush
     torch.cuda.empty_cache()

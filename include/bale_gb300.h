@@ -155,10 +155,23 @@ BALE_API int bale_histo_dev(int64_t *d_counts, int64_t ncounts, const int64_t *d
 BALE_API int bale_ig_dev(int64_t *d_tgt, const int64_t *d_index, int64_t n, const int64_t *d_table,
                 int64_t table_len, int shift, int64_t *d_bad, void *stream);
 /* *d_count += triangle count of the strictly lower CSR (d_offset[n+1],     */
-/* d_nonzero[nnz]); *d_work (may be NULL) += row-j elements examined.       */
+/* d_nonzero[nnz]); *d_work (may be NULL) += the kernels' work tally (the   */
+/* default wedge kernels: elements probed, the reference's exstack pushes). */
+/* With *d_bad raised the count is not meaningful.                          */
 BALE_API int bale_triangle_dev(const int64_t *d_offset, const int64_t *d_nonzero, int64_t numrows,
                       int64_t nnz, int64_t *d_count, int64_t *d_work, int64_t *d_bad,
                       void *stream);
+/* A graph counted repeatedly: bale_triangle_prepare validates the matrix    */
+/* (malformed entries added to *d_bad) and builds its 32-bit column copy and */
+/* transpose once, in device memory it owns (about 16 bytes per nonzero);   */
+/* each bale_triangle_count_prepared then runs only the counting kernel.    */
+/* d_offset/d_nonzero must stay valid and unchanged until release.  NULL on */
+/* failure (bale_last_error).  New entry points; the reference counts once. */
+typedef struct bale_tri_prepared bale_tri_prepared_t;
+BALE_API bale_tri_prepared_t *bale_triangle_prepare(const int64_t *d_offset, const int64_t *d_nonzero,
+                                                    int64_t numrows, int64_t nnz, int64_t *d_bad, void *stream);
+BALE_API int bale_triangle_count_prepared(bale_tri_prepared_t *g, int64_t *d_count, int64_t *d_work, void *stream);
+BALE_API void bale_triangle_release(bale_tri_prepared_t *g);
 
 /* ======================= batched execution ============================== */
 /* Many instances of uneven size in one CUDA graph: a persistent work-queue  */

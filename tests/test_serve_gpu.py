@@ -177,6 +177,26 @@ def test_registration_refused_when_free_hbm_is_short(cuda, bale):
         assert s.add_table(np.arange(1000, dtype=np.int64)) >= 0
 
 
+def test_malformed_graph_is_refused_at_registration(cuda, bale):
+    """A graph whose rows are not ascending inside [0,i) is refused with
+    BALE_EINPUT (status 2) when it is registered; a good one is accepted."""
+    from bale_old_gb300 import serve
+
+    m = 40
+    off = np.zeros(m + 1, np.int64)
+    off[1:] = np.cumsum(np.arange(m))
+    col = np.concatenate([np.arange(i, dtype=np.int64) for i in range(m)])
+    bad = col.copy()
+    bad[off[30] + 3], bad[off[30] + 4] = bad[off[30] + 4], bad[off[30] + 3]
+    with serve.Server(arena_bytes=1 << 20, max_active=4) as s:
+        with pytest.raises(bale.BaleError, match="status 2"):
+            s.add_graph(bale.SparseMatrix(off, bad))
+        g = s.add_graph(bale.SparseMatrix(off, col))
+        out = np.zeros(1, np.int64)
+        s.run([serve.triangles(g, out)])
+        assert int(out[0]) == m * (m - 1) * (m - 2) // 6
+
+
 def test_invalid_requests_are_rejected(cuda, bale):
     from bale_old_gb300 import serve
 

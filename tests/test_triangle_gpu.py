@@ -12,9 +12,10 @@ DROPINS = ("triangle_agi", "triangle_exstack_push", "triangle_exstack2_push",
            "triangle_convey_push", "triangle_agi_iter")
 
 
-@pytest.fixture(params=[0, 1], ids=["merge", "hybrid"])
+@pytest.fixture(params=[0, 1, 2], ids=["merge", "hybrid", "wedge"])
 def mode(request, bale):
-    """tri.mode 0: warp-per-row merge for every row; 1: bitmap/search hybrid."""
+    """tri.mode 0: warp-per-row merge for every row; 1: bitmap/search hybrid
+    over rows i; 2 (the default): wedge probes grouped at the far vertex j."""
     bale.tune_set("tri.mode", request.param)
     yield request.param
     bale.tune_set("tri.mode", -1)
@@ -56,6 +57,12 @@ def test_rmat_matches_oracle(cuda, bale, oracle, scale, mode):
         # the merge kernel scans every row-j element: the reference's pulls
         # for every (i,j) except the first nonzero of each row
         assert sr == pulls
+    elif mode == 2:
+        # one probe per element of row i below j, for every (i,j) whose row j
+        # is not empty: the reference's exstack pushes, less those
+        rowid = np.repeat(np.arange(L.numrows), deg)
+        pos = np.arange(L.nnz) - L.offset[rowid]
+        assert sr == int(pos[deg[L.nonzero] > 0].sum())
     else:
         # the hybrid streams or searches the cheaper side of each (i,j)
         assert 0 < sr <= pulls + int((deg * (deg - 1) // 2).sum())
@@ -153,3 +160,43 @@ def test_mixed_heavy_and_light_rows_match_oracle(cuda, bale, oracle, mode):
     M = bale.SparseMatrix(noff, ncol)
     assert oracle.is_strict_lower_tidy(noff, ncol)
     assert bale.triangle_agi(M)[0] == oracle.triangle_agi(noff, ncol)[0]
+
+
+def test_prepared_graph_counts_repeatedly(cuda, bale, oracle):
+    """bale_triangle_prepare once, bale_triangle_count_prepared three times:
+    three times the count, the probe tally each time, nothing flagged."""
+    import torch
+
+    L = bale.gen_rmat(14, 16, 0.57, 0.19, 0.19, 41)
+    off = torch.from_numpy(L.offset).to(cuda)
+    col = torch.from_numpy(L.nonzero).to(cuda)
+    count = torch.zeros(1, dtype=torch.int64, device=cuda)
+    work = torch.zeros(1, dtype=torch.int64, device=cuda)
+    bad = torch.zeros(1, dtype=torch.int64, device=cuda)
+    with bale.TrianglePrepared(off, col, bad=bad) as g:
+        for _ in range(3):
+            g.count(count, work)
+    torch.cuda.synchronize()
+    want = oracle.triangle_agi(L.offset, L.nonzero)[0]
+    deg = np.diff(L.offset)
+    rowid = np.repeat(np.arange(L.numrows), deg)
+    pos = np.arange(L.nnz) - L.offset[rowid]
+    assert int(count.item()) == 3 * want and int(bad.item()) == 0
+    assert int(work.item()) == 3 * int(pos[deg[L.nonzero] > 0].sum())
+
+
+def test_prepared_graph_malformed_is_flagged(cuda, bale):
+    """A malformed matrix raises *bad at prepare time and counts nothing."""
+    import torch
+
+    off, col = _clique(70)
+    c = col.copy()
+    c[off[65] + 1], c[off[65] + 2] = c[off[65] + 2], c[off[65] + 1]
+    d_off = torch.from_numpy(off).to(cuda)
+    d_col = torch.from_numpy(c).to(cuda)
+    count = torch.zeros(1, dtype=torch.int64, device=cuda)
+    bad = torch.zeros(1, dtype=torch.int64, device=cuda)
+    with bale.TrianglePrepared(d_off, d_col, bad=bad) as g:
+        g.count(count)
+    torch.cuda.synchronize()
+    assert int(bad.item()) > 0 and int(count.item()) == 0

@@ -168,9 +168,9 @@ def tune_batch(quick: bool) -> tuple[dict, list]:
     torch.cuda.empty_cache()
     if not quick:
         full = build_mix(dev, MIX_FULL)
-        for name, cands in (("batch.standalone_min", (1 << 21, 1 << 22, 1 << 23, 1 << 24)),
-                            ("batch.standalone_min_edges", (1 << 19, 1 << 20, 1 << 21, 1 << 22)),
-                            ("batch.streams", (2, 4, 8))):
+        for name, cands in (("batch.standalone_min_edges", (1 << 14, 1 << 16, 1 << 18, 1 << 19, 1 << 20, 1 << 21)),
+                            ("batch.standalone_min", (1 << 19, 1 << 20, 1 << 21, 1 << 22, 1 << 23)),
+                            ("batch.streams", (4, 8, 16))):
             res = {}
             for v in cands:
                 bale.tune_set(name, v)

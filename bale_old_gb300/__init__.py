@@ -286,6 +286,13 @@ def triangle_dev(offset, nonzero, count, work=None, bad=None, stream=None) -> No
                                    _stream(stream)), "bale_triangle_dev")
 
 
+def l2_red_rate(counts, n: int, stream=None) -> None:
+    """n +1 reductions at hashed positions of counts (device int64): the L2
+    reduction-rate probe that bounds a histogram whose table fits in L2."""
+    _status(_lib.bale_l2_red_rate(_dptr(counts, "counts"), counts.numel(), int(n), _stream(stream)),
+            "bale_l2_red_rate")
+
+
 class TrianglePrepared:
     """A device CSR counted repeatedly (bale_triangle_prepare): validation,
     the 32-bit column copy and the transpose are built once; count() adds

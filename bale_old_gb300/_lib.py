@@ -82,6 +82,7 @@ SIGNATURES: dict[str, tuple[object, list[object]]] = {
     "bale_histo_dev": (C.c_int, [VP, i64, VP, i64, C.c_int, VP, VP]),
     "bale_ig_dev": (C.c_int, [VP, VP, i64, VP, i64, C.c_int, VP, VP]),
     "bale_triangle_dev": (C.c_int, [VP, VP, i64, i64, VP, VP, VP, VP]),
+    "bale_l2_red_rate": (C.c_int, [VP, i64, i64, VP]),
     "bale_triangle_prepare": (VP, [VP, VP, i64, i64, VP, VP]),
     "bale_triangle_count_prepared": (C.c_int, [VP, VP, VP, VP]),
     "bale_triangle_release": (None, [VP]),

@@ -19,11 +19,14 @@
 //   triangles, heavy rows          : the whole block per heavy row, row i as
 //                                    a shared-memory bitmap (heavy_row).
 //
-// Instances that need the multi-pass region-partitioned algorithms (ig and
-// histo tables well beyond L2 with >= 2^20 elements) are launched as their
-// own kernels on a second captured stream, in parallel with the queue.
-// The whole run -- queue reset, the persistent kernel and those launches --
-// is one CUDA graph, replayed by bale_batch_run.
+// Instances large enough to fill the GPU by themselves (the standalone rule:
+// the partition thresholds, batch.standalone_min elements, or
+// batch.standalone_min_edges nonzeros for a graph) run their specialised
+// kernels instead -- region-partitioned ig / histo, the wedge triangle
+// kernels -- on up to batch.streams captured side streams, longest first to
+// the least loaded, in parallel with the queue.  The whole run -- queue
+// reset, the persistent kernel and those launches -- is one CUDA graph,
+// replayed by bale_batch_run.
 //
 // Results match the per-instance entry points bit for bit: histo ADDS into
 // its counts, ig OVERWRITES tgt, triangles ADD their count into out[0].

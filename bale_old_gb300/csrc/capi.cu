@@ -414,6 +414,14 @@ int bale_histo_dev(int64_t *d_counts, int64_t ncounts, const int64_t *d_index, i
   return launch_histo(d_counts, ncounts, d_index, n, shift, bad, static_cast<cudaStream_t>(stream));
 }
 
+int bale_l2_red_rate(int64_t *d_counts, int64_t ncounts, int64_t n, void *stream) {
+  if (n < 0 || ncounts < 0 || (n > 0 && (!d_counts || ncounts == 0))) {
+    set_error("bale_l2_red_rate: bad arguments");
+    return BALE_EINVAL;
+  }
+  return launch_l2_red_rate(d_counts, ncounts, n, static_cast<cudaStream_t>(stream));
+}
+
 int bale_ig_dev(int64_t *d_tgt, const int64_t *d_index, int64_t n, const int64_t *d_table, int64_t table_len,
                 int shift, int64_t *d_bad, void *stream) {
   if (n < 0 || table_len < 0 || (shift != 0 && shift != 16) ||

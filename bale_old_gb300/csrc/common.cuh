@@ -108,6 +108,8 @@ int tri_wedge_run(const int64_t *offset, const void *ws, int64_t numrows, int64_
 int launch_triangle_wedge(const int64_t *offset, const int64_t *nonzero, int64_t numrows, int64_t nnz,
                           unsigned long long *count, unsigned long long *work, unsigned long long *bad, void *ws,
                           unsigned long long *cursor, cudaStream_t stream);
+// n +1 L2 reductions at hashed positions of counts (the L2 reduction-rate probe).
+int launch_l2_red_rate(int64_t *counts, int64_t ncounts, int64_t n, cudaStream_t stream);
 // max over index[i] >> shift into *out (u64, must start at 0); negatives count as huge.
 int launch_index_max(const int64_t *index, int64_t n, int shift, unsigned long long *out,
                      cudaStream_t stream);

@@ -135,7 +135,28 @@ __global__ void __launch_bounds__(kSmemThreads)
 
 bool g_smem_attr_set[64] = {false};
 
+// The L2 reduction rate the histogram is bound by when its table lives in
+// L2: n +1 reductions at hashed positions of counts, with no index stream
+// to read -- the histogram's update minus its input.
+__global__ void __launch_bounds__(256) l2_red_rate_kernel(int64_t *__restrict__ counts, uint64_t m, int64_t n) {
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += stride) {
+    uint64_t x = static_cast<uint64_t>(i) * 0x9E3779B97F4A7C15ull;
+    x ^= x >> 29;
+    red_add_u64(counts + __umul64hi(x, m), 1ull);
+  }
+}
+
 }  // namespace
+
+int launch_l2_red_rate(int64_t *counts, int64_t ncounts, int64_t n, cudaStream_t stream) {
+  if (n <= 0 || ncounts <= 0) return BALE_OK;
+  const int64_t want = (n + 255) / 256, full = static_cast<int64_t>(num_sms()) * 8;
+  l2_red_rate_kernel<<<static_cast<unsigned>(want < full ? want : full), 256, 0, stream>>>(
+      counts, static_cast<uint64_t>(ncounts), n);
+  BALE_CUDA_OK(cudaGetLastError());
+  return BALE_OK;
+}
 
 // Mode: 0 shared-memory private table, 1 warp-aggregated L2 reductions,
 // 2 plain L2 reductions, 3 region-partitioned L2 reductions.  Automatic:

@@ -151,6 +151,10 @@ BALE_API const char *bale_tune_name(int i);
 /* exstack indices).  Counters are int64, ncounts of them.                  */
 BALE_API int bale_histo_dev(int64_t *d_counts, int64_t ncounts, const int64_t *d_index, int64_t n,
                    int shift, int64_t *d_bad, void *stream);
+/* Measurement probe (no counterpart in the reference): n +1 reductions at  */
+/* hashed positions of counts[ncounts], no index read -- the L2 reduction    */
+/* rate that bounds a histogram whose table fits in L2.                     */
+BALE_API int bale_l2_red_rate(int64_t *d_counts, int64_t ncounts, int64_t n, void *stream);
 /* tgt[i] = table[index[i] >> shift] for i < n; out-of-range -> tgt[i] = 0. */
 BALE_API int bale_ig_dev(int64_t *d_tgt, const int64_t *d_index, int64_t n, const int64_t *d_table,
                 int64_t table_len, int shift, int64_t *d_bad, void *stream);

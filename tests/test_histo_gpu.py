@@ -128,3 +128,13 @@ def test_every_mode_matches_oracle(cuda, bale, oracle, hmode, n, tsize):
         np.testing.assert_array_equal(c.cpu().numpy(), np.bincount(idx_h[ok], minlength=tsize))
     finally:
         bale.tune_set("histo.mode", -1)
+
+
+def test_l2_reduction_probe_adds_exactly_n(cuda, bale):
+    """The roofline probe lands every one of its n reductions inside the table."""
+    import torch
+
+    counts = torch.zeros(1_000_003, dtype=torch.int64, device=cuda)
+    bale.l2_red_rate(counts, 12_345_678)
+    torch.cuda.synchronize()
+    assert int(counts.sum().item()) == 12_345_678 and int(counts.min().item()) >= 0

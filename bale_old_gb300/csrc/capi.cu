@@ -8,6 +8,7 @@
 // call can touch from the data: the largest index, computed on the device
 // after the index array is uploaded.  Exactly counts[0..max] / table[0..max]
 // are moved, which the reference would also have been allowed to access.
+#include <algorithm>
 #include <chrono>
 #include <cstdarg>
 #include <cstdio>
@@ -15,6 +16,7 @@
 #include <map>
 #include <new>
 #include <mutex>
+#include <vector>
 
 #include "common.cuh"
 
@@ -122,7 +124,11 @@ struct DevBuf {
 
 struct DropinState {
   cudaStream_t stream = nullptr;
+  cudaStream_t s_comp = nullptr, s_down = nullptr;  // the pipelined gather's compute and download streams
   DevBuf buf[4];
+  unsigned long long *h_max = nullptr;  // mapped pinned per-chunk maxima (host address)
+  unsigned long long *h_max_dev = nullptr;  // ... and their device alias
+  size_t h_max_cap = 0;
 };
 
 static std::mutex g_dropin_mu;
@@ -149,9 +155,11 @@ static DropinState *dropin_state() {
   if (d < 0 || d >= 64) return nullptr;
   DropinState &s = g_state[d];
   if (!s.stream) {
-    if (cudaStreamCreateWithFlags(&s.stream, cudaStreamNonBlocking) != cudaSuccess) {
+    if (cudaStreamCreateWithFlags(&s.stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&s.s_comp, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&s.s_down, cudaStreamNonBlocking) != cudaSuccess) {
       set_error("cudaStreamCreate failed");
-      s.stream = nullptr;
+      s.stream = s.s_comp = s.s_down = nullptr;
       return nullptr;
     }
   }
@@ -229,6 +237,189 @@ static double histo_dropin(const int64_t *index, int64_t n, int64_t *counts, int
   return now_seconds() - t0;
 }
 
+// Events of one pipelined call, destroyed on every return path.
+struct EventSet {
+  std::vector<cudaEvent_t> ev;
+  ~EventSet() {
+    for (auto e : ev)
+      if (e) cudaEventDestroy(e);
+  }
+  cudaEvent_t make() {
+    cudaEvent_t e = nullptr;
+    if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return nullptr;
+    ev.push_back(e);
+    return e;
+  }
+};
+
+// Large gathers are pipelined in chunks of requests so that the copies in
+// both directions and the gathers overlap.  The table's extent is not known
+// before the requests are (the reference passes no table length), so:
+//   1. chunk 0 is uploaded and its largest index found; the table is then
+//      uploaded up to it (plus a margin for later chunks' larger indices);
+//   2. the other chunks are uploaded behind it, each with its maximum, and
+//      each is gathered as soon as it and the table are on the device and
+//      copied back on a third stream while later chunks still upload;
+//   3. a chunk whose indices reach beyond the uploaded part first extends
+//      the device table on the gather stream (into a larger buffer, after
+//      the uploads, only when the margin is used up).
+// Results are identical to the single-pass path; the call stays synchronous.
+static double ig_dropin_pipelined(int64_t *tgt, const int64_t *index, int64_t n, const int64_t *table, int shift,
+                                  int64_t chunk, DropinState *st, DeviceScratch *ds, double t0) {
+  const int64_t nch = (n + chunk - 1) / chunk;
+  const size_t ibytes = static_cast<size_t>(n) * sizeof(int64_t);
+  DROPIN_TRY(st->buf[0].ensure(ibytes));  // index
+  DROPIN_TRY(st->buf[2].ensure(ibytes));  // output
+  DROPIN_TRY(st->buf[3].ensure(static_cast<size_t>(nch) * sizeof(unsigned long long)));  // chunk maxima
+  if (st->h_max_cap < static_cast<size_t>(nch)) {
+    if (st->h_max) cudaFreeHost(st->h_max);
+    st->h_max = st->h_max_dev = nullptr;
+    st->h_max_cap = 0;
+    void *hp = nullptr, *dp = nullptr;
+    DROPIN_CUDA(cudaHostAlloc(&hp, static_cast<size_t>(nch) * sizeof(unsigned long long), cudaHostAllocMapped));
+    st->h_max = static_cast<unsigned long long *>(hp);
+    DROPIN_CUDA(cudaHostGetDevicePointer(&dp, hp, 0));
+    st->h_max_dev = static_cast<unsigned long long *>(dp);
+    st->h_max_cap = static_cast<size_t>(nch);
+  }
+  int64_t *d_idx = static_cast<int64_t *>(st->buf[0].p);
+  int64_t *d_out = static_cast<int64_t *>(st->buf[2].p);
+  unsigned long long *d_max = static_cast<unsigned long long *>(st->buf[3].p);
+  unsigned long long *h_max = st->h_max, *h_max_dev = st->h_max_dev;
+  EventSet es;
+  DevBuf grown;  // a larger table buffer, if a chunk needs one
+  // Every failure drains the streams first: copies into the caller's host
+  // buffers may still be in flight.
+  auto fail = [&]() -> double {
+    cudaStreamSynchronize(st->stream);
+    cudaStreamSynchronize(st->s_comp);
+    cudaStreamSynchronize(st->s_down);
+    cudaGetLastError();
+    grown.release();
+    return -1.0;
+  };
+#define PIPE_TRY(expr)                  \
+  do {                                  \
+    if ((expr) != BALE_OK) return fail(); \
+  } while (0)
+#define PIPE_CUDA(expr)                                                          \
+  do {                                                                           \
+    cudaError_t _e = (expr);                                                     \
+    if (_e != cudaSuccess) {                                                     \
+      set_error("%s failed: %s", #expr, cudaGetErrorString(_e));                 \
+      return fail();                                                             \
+    }                                                                            \
+  } while (0)
+  std::vector<cudaEvent_t> ev_max(static_cast<size_t>(nch)), ev_up(static_cast<size_t>(nch)),
+      ev_gat(static_cast<size_t>(nch));
+  for (int64_t k = 0; k < nch; k++) {
+    ev_max[k] = es.make();
+    ev_up[k] = es.make();
+    ev_gat[k] = es.make();
+    if (!ev_max[k] || !ev_up[k] || !ev_gat[k]) {
+      set_error("ig: cudaEventCreate failed");
+      return fail();
+    }
+  }
+  cudaEvent_t ev_tab = es.make();
+  if (!ev_tab) {
+    set_error("ig: cudaEventCreate failed");
+    return fail();
+  }
+  PIPE_CUDA(cudaMemsetAsync(ds->words, 0, 8 * sizeof(unsigned long long), st->stream));
+  PIPE_CUDA(cudaMemsetAsync(d_max, 0, static_cast<size_t>(nch) * sizeof(unsigned long long), st->stream));
+  auto upload = [&](int64_t k) -> int {
+    const int64_t lo = k * chunk, len = std::min(chunk, n - lo);
+    if (cudaMemcpyAsync(d_idx + lo, index + lo, static_cast<size_t>(len) * 8, cudaMemcpyHostToDevice,
+                        st->stream) != cudaSuccess ||
+        cudaEventRecord(ev_up[k], st->stream) != cudaSuccess)
+      return BALE_ECUDA;
+    // the maximum goes to the host by a kernel's write, not a copy: a
+    // device-to-host copy here would queue behind the result downloads
+    int rc = launch_index_max(d_idx + lo, len, shift, d_max + k, st->stream);
+    if (rc == BALE_OK) rc = launch_copy_word(d_max + k, h_max_dev + k, st->stream);
+    if (rc != BALE_OK) return rc;
+    if (cudaEventRecord(ev_max[k], st->stream) != cudaSuccess) return BALE_ECUDA;
+    return BALE_OK;
+  };
+  auto too_big = [&](unsigned long long m) {
+    if (m < (1ull << 60)) return false;
+    set_error("index out of range (negative or >= 2^60): max index %llu", m);
+    return true;
+  };
+  if (upload(0) != BALE_OK) {
+    set_error("ig: upload failed");
+    return fail();
+  }
+  PIPE_CUDA(cudaEventSynchronize(ev_max[0]));
+  if (too_big(h_max[0])) {
+    return fail();
+  }
+  int64_t ext = static_cast<int64_t>(h_max[0]) + 1;  // table entries on the device
+  size_t cap = static_cast<size_t>(ext) + static_cast<size_t>(ext) / 4 + 1024;
+  PIPE_TRY(st->buf[1].ensure(cap * sizeof(int64_t)));
+  int64_t *d_tab = static_cast<int64_t *>(st->buf[1].p);
+  PIPE_CUDA(cudaMemcpyAsync(d_tab, table, static_cast<size_t>(ext) * 8, cudaMemcpyHostToDevice, st->stream));
+  PIPE_CUDA(cudaEventRecord(ev_tab, st->stream));
+  for (int64_t k = 1; k < nch; k++)
+    if (upload(k) != BALE_OK) {
+      set_error("ig: upload failed");
+      return fail();
+    }
+  PIPE_CUDA(cudaStreamWaitEvent(st->s_comp, ev_tab, 0));
+  for (int64_t k = 0; k < nch; k++) {
+    PIPE_CUDA(cudaEventSynchronize(ev_max[k]));
+    if (too_big(h_max[k])) {
+      return fail();
+    }
+    const int64_t need = static_cast<int64_t>(h_max[k]) + 1;
+    if (need > ext) {
+      // Extend the device table to this chunk's largest index, on the gather
+      // stream (usually a few entries: independent chunks of random requests
+      // have nearly the same maximum).  Only when the buffer's margin is used
+      // up is a larger buffer taken -- sized from every chunk's maximum, so
+      // this waits for the uploads -- after the gathers reading the old one.
+      int64_t top = need;
+      if (static_cast<size_t>(need) > cap) {
+        PIPE_CUDA(cudaStreamSynchronize(st->stream));
+        for (int64_t r = k; r < nch; r++) {
+          if (too_big(h_max[r])) return fail();
+          top = std::max<int64_t>(top, static_cast<int64_t>(h_max[r]) + 1);
+        }
+        PIPE_CUDA(cudaStreamSynchronize(st->s_comp));
+        PIPE_TRY(grown.ensure(static_cast<size_t>(top) * sizeof(int64_t)));
+        PIPE_CUDA(cudaMemcpyAsync(grown.p, d_tab, static_cast<size_t>(ext) * 8, cudaMemcpyDeviceToDevice,
+                                  st->s_comp));
+        d_tab = static_cast<int64_t *>(grown.p);
+        cap = static_cast<size_t>(top);
+      }
+      PIPE_CUDA(cudaMemcpyAsync(d_tab + ext, table + ext, static_cast<size_t>(top - ext) * 8,
+                                cudaMemcpyHostToDevice, st->s_comp));
+      ext = top;
+    }
+    const int64_t lo = k * chunk, len = std::min(chunk, n - lo);
+    PIPE_CUDA(cudaStreamWaitEvent(st->s_comp, ev_up[k], 0));
+    PIPE_TRY(launch_ig(d_out + lo, d_idx + lo, len, d_tab, ext, shift, ds->words + kWordBad, st->s_comp));
+    PIPE_CUDA(cudaEventRecord(ev_gat[k], st->s_comp));
+    PIPE_CUDA(cudaStreamWaitEvent(st->s_down, ev_gat[k], 0));
+    PIPE_CUDA(cudaMemcpyAsync(tgt + lo, d_out + lo, static_cast<size_t>(len) * 8, cudaMemcpyDeviceToHost,
+                                st->s_down));
+  }
+  unsigned long long bad = 0;
+  PIPE_CUDA(cudaStreamSynchronize(st->s_comp));
+  PIPE_CUDA(cudaMemcpyAsync(&bad, ds->words + kWordBad, sizeof(bad), cudaMemcpyDeviceToHost, st->s_down));
+  PIPE_CUDA(cudaStreamSynchronize(st->s_down));
+  PIPE_CUDA(cudaStreamSynchronize(st->stream));
+  grown.release();
+#undef PIPE_TRY
+#undef PIPE_CUDA
+  if (bad) {
+    set_error("ig: %llu out-of-range indices", bad);
+    return -1.0;
+  }
+  return now_seconds() - t0;
+}
+
 static double ig_dropin(int64_t *tgt, const int64_t *index, int64_t n, const int64_t *table,
                         int shift) {
   const double t0 = now_seconds();
@@ -241,6 +432,8 @@ static double ig_dropin(int64_t *tgt, const int64_t *index, int64_t n, const int
   DropinState *st = dropin_state();
   DeviceScratch *ds = device_scratch();
   if (!st || !ds) return -1.0;
+  const int64_t chunk = knob_or("dropin.ig_chunk", int64_t(1) << 24);
+  if (chunk > 0 && n > 2 * chunk) return ig_dropin_pipelined(tgt, index, n, table, shift, chunk, st, ds, t0);
   int64_t extent = 0;
   if (extent_of(st, ds, index, n, shift, &extent) < 0) return -1.0;
   const size_t tbytes = static_cast<size_t>(extent) * sizeof(int64_t);

@@ -110,6 +110,9 @@ int launch_triangle_wedge(const int64_t *offset, const int64_t *nonzero, int64_t
                           unsigned long long *cursor, cudaStream_t stream);
 // n +1 L2 reductions at hashed positions of counts (the L2 reduction-rate probe).
 int launch_l2_red_rate(int64_t *counts, int64_t ncounts, int64_t n, cudaStream_t stream);
+// *mapped_dst = *src by a one-thread kernel (mapped_dst: the device alias of
+// mapped pinned host memory).
+int launch_copy_word(const unsigned long long *src, unsigned long long *mapped_dst, cudaStream_t stream);
 // max over index[i] >> shift into *out (u64, must start at 0); negatives count as huge.
 int launch_index_max(const int64_t *index, int64_t n, int shift, unsigned long long *out,
                      cudaStream_t stream);

@@ -212,6 +212,18 @@ int launch_ig(int64_t *tgt, const int64_t *index, int64_t n, const int64_t *tabl
   return BALE_OK;
 }
 
+// One word from device memory to a mapped host word, written by the kernel:
+// no copy engine is involved, so it never queues behind large copies.
+__global__ void copy_word_kernel(const unsigned long long *__restrict__ src, volatile unsigned long long *dst) {
+  *dst = *src;
+}
+
+int launch_copy_word(const unsigned long long *src, unsigned long long *mapped_dst, cudaStream_t stream) {
+  copy_word_kernel<<<1, 1, 0, stream>>>(src, mapped_dst);
+  BALE_CUDA_OK(cudaGetLastError());
+  return BALE_OK;
+}
+
 int launch_index_max(const int64_t *index, int64_t n, int shift, unsigned long long *out,
                      cudaStream_t stream) {
   if (n <= 0) return BALE_OK;

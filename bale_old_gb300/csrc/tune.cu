@@ -55,6 +55,7 @@ Knob g_knobs[] = {
     {"batch.tri_light_rows.small", -1},
     {"batch.tri_light_rows.medium", -1},
     {"batch.tri_light_rows.large", -1},
+    {"dropin.ig_chunk", -1},      // requests per chunk of the pipelined ig drop-in (2^24; 0 = one pass)
     {"serve.tick_cost", -1},      // work per tick (element-cost units, 2^24)
     {"serve.request_cost", -1},   // work one request may add to a tick (2^22)
     {"serve.tick_tasks", -1},     // tasks per tick (4096)

@@ -141,3 +141,47 @@ def test_both_modes_count_bad_indices(cuda, bale, mode):
         assert not got[~ok].any()
     finally:
         bale.tune_set("ig.mode", -1)
+
+
+@pytest.fixture
+def small_chunks(bale):
+    """Pipelined drop-in with 4096-request chunks, so small calls take it."""
+    bale.tune_set("dropin.ig_chunk", 4096)
+    yield 4096
+    bale.tune_set("dropin.ig_chunk", -1)
+
+
+@pytest.mark.parametrize("order", ["uniform", "ascending", "late_max", "packed"])
+def test_pipelined_dropin_matches_oracle(cuda, bale, oracle, small_chunks, order):
+    """Chunked uploads, per-chunk maxima and overlapped gathers and downloads
+    give the single-pass result.  "ascending" indices make every chunk reach
+    beyond the table uploaded for the first one (extension and a larger
+    buffer); "late_max" puts the only large index in the last chunk."""
+    n, t = 50_001, 1 << 18
+    table = bale.gen_values(t, 11)
+    if order == "uniform":
+        idx = bale.gen_uniform(n, t, 12)
+    elif order == "ascending":
+        idx = np.sort(bale.gen_uniform(n, t, 13))
+    else:
+        idx = bale.gen_uniform(n, 1000, 14)
+        idx[-3] = t - 1
+    tgt = np.full(n, -7, np.int64)
+    if order == "packed":
+        bale.ig_exstack(tgt, bale.pack_index(idx), table)
+    else:
+        bale.ig_agi(tgt, idx, table)
+    np.testing.assert_array_equal(tgt, table[idx])
+
+
+def test_pipelined_dropin_bad_index_is_an_error(cuda, bale, small_chunks):
+    n, t = 40_000, 5000
+    table = bale.gen_values(t, 3)
+    idx = bale.gen_uniform(n, t, 4)
+    idx[-10] = -5  # a negative index in the last chunk
+    with pytest.raises(bale.BaleError):
+        bale.ig_agi(np.zeros(n, np.int64), idx, table)
+    idx[-10] = 7
+    tgt = np.zeros(n, np.int64)
+    bale.ig_agi(tgt, idx, table)
+    np.testing.assert_array_equal(tgt, table[idx])

@@ -151,7 +151,7 @@ __device__ void cta_tri_heavy(const Inst &in, int64_t lo, int64_t hi, uint32_t *
   flush_tri(t, in, bad, work);
 }
 
-__global__ void __launch_bounds__(kThreads, 1)
+__global__ void __launch_bounds__(kThreads, 2)
     batch_kernel(const Task *__restrict__ tasks, int64_t ntasks, const Inst *__restrict__ insts,
                  unsigned long long *__restrict__ head, unsigned long long *__restrict__ bad,
                  unsigned long long *__restrict__ work) {

@@ -27,8 +27,8 @@ struct Task {
 
 constexpr int kThreads = 512;
 constexpr int kWarps = kThreads / 32;
-constexpr int64_t kSmemCounters = 48 * 1024;
-constexpr size_t kSmemBytes = static_cast<size_t>(kSmemCounters) * sizeof(uint32_t);  // 192 KiB
+constexpr int64_t kSmemCounters = 24 * 1024;
+constexpr size_t kSmemBytes = static_cast<size_t>(kSmemCounters) * sizeof(uint32_t);  // 96 KiB: two blocks per SM
 static_assert(kSmemBytes >= static_cast<size_t>(tri::kHeavyBits / 8), "bitmap must fit");
 static_assert(kSmemBytes >= static_cast<size_t>(kWarps) * tri::kLightCap * sizeof(uint32_t), "row slots must fit");
 

@@ -293,6 +293,39 @@ def l2_red_rate(counts, n: int, stream=None) -> None:
             "bale_l2_red_rate")
 
 
+def graph_build_dev(u, v, n: int, stream=None):
+    """Degree-ordered strictly lower CSR of the undirected edges (u[e], v[e])
+    (device int64 tensors) on n vertices, built on the device: returns
+    (offset, nonzero) device tensors, nonzero trimmed to nnz."""
+    import torch
+
+    m = u.numel()
+    if v.numel() != m:
+        raise ValueError("u and v differ in length")
+    off = torch.empty(n + 1, dtype=torch.int64, device=u.device)
+    nz = torch.empty(max(m, 1), dtype=torch.int64, device=u.device)
+    nnz = C.c_int64(0)
+    _status(_lib.bale_graph_build_dev(_dptr(u, "u") if m else None, _dptr(v, "v") if m else None, m, int(n),
+                                      _dptr(off, "offset"), _dptr(nz, "nonzero"), C.byref(nnz), _stream(stream)),
+            "bale_graph_build_dev")
+    return off, nz[: nnz.value]
+
+
+def gen_rmat_dev(scale: int, edgefactor: int, a: float, b: float, c: float, seed: int, device=None, stream=None):
+    """gen_rmat's graph generated and built on the device (bit-identical):
+    returns (offset, nonzero) device int64 tensors."""
+    import torch
+
+    dev = device if device is not None else torch.device("cuda", torch.cuda.current_device())
+    n = 1 << scale
+    off = torch.empty(n + 1, dtype=torch.int64, device=dev)
+    nz = torch.empty(edgefactor * n, dtype=torch.int64, device=dev)
+    nnz = C.c_int64(0)
+    _status(_lib.bale_gen_rmat_dev(scale, edgefactor, a, b, c, seed & (2**64 - 1), _dptr(off, "offset"),
+                                   _dptr(nz, "nonzero"), C.byref(nnz), _stream(stream)), "bale_gen_rmat_dev")
+    return off, nz[: nnz.value]
+
+
 class TrianglePrepared:
     """A device CSR counted repeatedly (bale_triangle_prepare): validation,
     the 32-bit column copy and the transpose are built once; count() adds

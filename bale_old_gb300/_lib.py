@@ -83,6 +83,9 @@ SIGNATURES: dict[str, tuple[object, list[object]]] = {
     "bale_ig_dev": (C.c_int, [VP, VP, i64, VP, i64, C.c_int, VP, VP]),
     "bale_triangle_dev": (C.c_int, [VP, VP, i64, i64, VP, VP, VP, VP]),
     "bale_l2_red_rate": (C.c_int, [VP, i64, i64, VP]),
+    "bale_graph_build_dev": (C.c_int, [VP, VP, i64, i64, VP, VP, P64, VP]),
+    "bale_graph_build_workspace": (i64, [i64, i64]),
+    "bale_gen_rmat_dev": (C.c_int, [i64, i64, C.c_double, C.c_double, C.c_double, C.c_uint64, VP, VP, P64, VP]),
     "bale_triangle_prepare": (VP, [VP, VP, i64, i64, VP, VP]),
     "bale_triangle_count_prepared": (C.c_int, [VP, VP, VP, VP]),
     "bale_triangle_release": (None, [VP]),

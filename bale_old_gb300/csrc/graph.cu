@@ -1,0 +1,507 @@
+// graph.cu -- building the triangle kernels' input on the device: the
+// degree-ordered, strictly lower-triangular CSR of an undirected graph.
+//
+// From an edge list (or R-MAT edges generated in place, bit-identical to
+// bale_gen_rmat in host/inputs.c):
+//   1. keys: each edge {u,v}, u != v, becomes min << S | max (S = label
+//      bits); self loops become an all-ones key that sorts last;
+//   2. sort the keys (LSD radix sort below), drop the duplicates and the
+//      self loops;
+//   3. degrees; labels by descending degree, ties by ascending original
+//      label: a second sort of (maxdeg - deg) << S | v;
+//   4. each edge relabelled to row = max, col = min of the new labels, a
+//      third sort, and the CSR read off the sorted keys: rows in order,
+//      columns ascending within each row -- the reference's tidy lower
+//      matrix (spmat/spmat_utils.upc:455-473 tril, :1055-1062 sort_nonzeros).
+// The radix sort is stable, 8 bits per pass: per tile of 4096 keys a digit
+// histogram, one exclusive scan over (digit, tile), then a scatter in which
+// every key's rank among equal digits of its tile comes from a warp match
+// and per-warp counts in shared memory.
+#include <algorithm>
+#include <cmath>
+
+#include "bale_inputs.h"
+#include "common.cuh"
+
+namespace bale {
+namespace {
+
+constexpr unsigned kFull = 0xffffffffu;
+constexpr int kThreads = 256;
+constexpr int kWarps = kThreads / 32;
+constexpr int kPer = 16;                      // keys per thread per tile
+constexpr int64_t kTile = kThreads * kPer;    // 4096 keys per sort block
+constexpr int kDigitBits = 8;
+constexpr int kDigits = 1 << kDigitBits;      // == kThreads: one digit per thread
+static_assert(kDigits == kThreads, "one digit per thread");
+constexpr int kScanThreads = 1024;
+constexpr int64_t kScanBlock = kScanThreads * 4;
+
+__device__ __forceinline__ uint64_t sm64(uint64_t seed, uint64_t i) {
+  uint64_t z = seed + (i + 1) * 0x9E3779B97F4A7C15ULL;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+  return z ^ (z >> 31);
+}
+
+// ---------------------------------------------------------------- scan
+__device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t *total) {
+  __shared__ uint32_t warp_tot[kScanThreads / 32];
+  const unsigned lane = lane_id(), warp = threadIdx.x >> 5;
+  uint32_t inc = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(kFull, inc, o);
+    if (static_cast<int>(lane) >= o) inc += y;
+  }
+  if (lane == 31) warp_tot[warp] = inc;
+  __syncthreads();
+  if (warp == 0) {
+    const uint32_t t = warp_tot[lane];
+    uint32_t ti = t;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(kFull, ti, o);
+      if (static_cast<int>(lane) >= o) ti += y;
+    }
+    warp_tot[lane] = ti - t;
+    if (lane == 31) *total = ti;
+  }
+  __syncthreads();
+  const uint32_t r = warp_tot[warp] + inc - v;
+  __syncthreads();
+  return r;
+}
+
+__device__ __forceinline__ void load4(const uint32_t *__restrict__ a, int64_t n, int64_t idx, uint32_t v[4]) {
+#pragma unroll
+  for (int q = 0; q < 4; q++) v[q] = idx + q < n ? a[idx + q] : 0u;
+}
+
+__global__ void __launch_bounds__(kScanThreads)
+    scan_blocksum_kernel(const uint32_t *__restrict__ in, int64_t n, uint32_t *__restrict__ bsum) {
+  __shared__ uint32_t tot;
+  const int64_t idx = static_cast<int64_t>(blockIdx.x) * kScanBlock + threadIdx.x * 4;
+  uint32_t v[4];
+  load4(in, n, idx, v);
+  block_excl_scan(v[0] + v[1] + v[2] + v[3], &tot);
+  if (threadIdx.x == 0) bsum[blockIdx.x] = tot;
+}
+
+__global__ void __launch_bounds__(kScanThreads)
+    scan_top_kernel(uint32_t *__restrict__ bsum, int64_t nb, uint32_t *__restrict__ total) {
+  __shared__ uint32_t tot;
+  uint32_t carry = 0;
+  for (int64_t base = 0; base < nb; base += kScanBlock) {
+    const int64_t idx = base + threadIdx.x * 4;
+    uint32_t v[4];
+    load4(bsum, nb, idx, v);
+    uint32_t x = block_excl_scan(v[0] + v[1] + v[2] + v[3], &tot) + carry;
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      if (idx + q < nb) bsum[idx + q] = x;
+      x += v[q];
+    }
+    carry += tot;
+  }
+  if (threadIdx.x == 0) *total = carry;
+}
+
+__global__ void __launch_bounds__(kScanThreads)
+    scan_apply_kernel(const uint32_t *__restrict__ in, int64_t n, const uint32_t *__restrict__ bsum,
+                      uint32_t *__restrict__ out) {
+  __shared__ uint32_t tot;
+  const int64_t idx = static_cast<int64_t>(blockIdx.x) * kScanBlock + threadIdx.x * 4;
+  uint32_t v[4];
+  load4(in, n, idx, v);
+  uint32_t x = block_excl_scan(v[0] + v[1] + v[2] + v[3], &tot) + bsum[blockIdx.x];
+#pragma unroll
+  for (int q = 0; q < 4; q++) {
+    if (idx + q < n) out[idx + q] = x;
+    x += v[q];
+  }
+}
+
+// ---------------------------------------------------------------- radix sort
+__global__ void __launch_bounds__(kThreads)
+    radix_hist_kernel(const uint64_t *__restrict__ keys, int64_t n, int shift, uint32_t *__restrict__ hist,
+                      int64_t ntiles) {
+  __shared__ uint32_t cnt[kDigits];
+  cnt[threadIdx.x] = 0;
+  __syncthreads();
+  const int64_t base = static_cast<int64_t>(blockIdx.x) * kTile;
+#pragma unroll 4
+  for (int r = 0; r < kPer; r++) {
+    const int64_t i = base + r * kThreads + threadIdx.x;
+    if (i < n) atomicAdd(&cnt[static_cast<uint32_t>(keys[i] >> shift) & (kDigits - 1)], 1u);
+  }
+  __syncthreads();
+  hist[static_cast<int64_t>(threadIdx.x) * ntiles + blockIdx.x] = cnt[threadIdx.x];
+}
+
+// offs[d * ntiles + t]: where tile t's keys with digit d start in dst.
+__global__ void __launch_bounds__(kThreads)
+    radix_scatter_kernel(const uint64_t *__restrict__ src, uint64_t *__restrict__ dst, int64_t n, int shift,
+                         const uint32_t *__restrict__ offs, int64_t ntiles) {
+  __shared__ uint32_t base[kDigits];
+  __shared__ uint32_t wcnt[kWarps][kDigits];
+  const unsigned lane = lane_id(), warp = threadIdx.x >> 5;
+  base[threadIdx.x] = offs[static_cast<int64_t>(threadIdx.x) * ntiles + blockIdx.x];
+#pragma unroll
+  for (int w = 0; w < kWarps; w++) wcnt[w][threadIdx.x] = 0;
+  __syncthreads();
+  const int64_t tile = static_cast<int64_t>(blockIdx.x) * kTile;
+  for (int r = 0; r < kPer; r++) {
+    const int64_t i = tile + r * kThreads + threadIdx.x;
+    const bool valid = i < n;
+    const uint64_t key = valid ? src[i] : 0ull;
+    const uint32_t d = valid ? static_cast<uint32_t>(key >> shift) & (kDigits - 1) : kDigits;  // kDigits: none
+    const unsigned peers = __match_any_sync(kFull, d);
+    const uint32_t rank = __popc(peers & ((1u << lane) - 1u));
+    if (valid && rank == 0) wcnt[warp][d] = __popc(peers);
+    __syncthreads();
+    if (valid) {
+      uint32_t pre = base[d] + rank;
+      for (unsigned w = 0; w < warp; w++) pre += wcnt[w][d];
+      dst[pre] = key;
+    }
+    __syncthreads();
+    uint32_t t = 0;
+#pragma unroll
+    for (int w = 0; w < kWarps; w++) {
+      t += wcnt[w][threadIdx.x];
+      wcnt[w][threadIdx.x] = 0;
+    }
+    base[threadIdx.x] += t;
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------- graph steps
+__global__ void __launch_bounds__(256)
+    rmat_keys_kernel(uint64_t *__restrict__ keys, int64_t m, int S, uint32_t ta, uint32_t tab, uint32_t tabc,
+                     uint64_t seed) {
+  const uint64_t draws = static_cast<uint64_t>(S + 1) / 2;  // two 32-bit levels per draw
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  for (int64_t e = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; e < m; e += stride) {
+    uint64_t u = 0, v = 0, r = 0;
+    for (int l = 0; l < S; l++) {
+      if ((l & 1) == 0) r = sm64(seed, static_cast<uint64_t>(e) * draws + static_cast<uint64_t>(l >> 1));
+      const uint32_t x = (l & 1) ? static_cast<uint32_t>(r >> 32) : static_cast<uint32_t>(r);
+      const uint64_t ub = x >= tab ? 1u : 0u;
+      const uint64_t vb = (x >= ta && x < tab) || x >= tabc ? 1u : 0u;
+      u = (u << 1) | ub;
+      v = (v << 1) | vb;
+    }
+    keys[e] = u == v ? ~0ull : (u < v ? (u << S) | v : (v << S) | u);
+  }
+}
+
+__global__ void __launch_bounds__(256)
+    edge_keys_kernel(const int64_t *__restrict__ eu, const int64_t *__restrict__ ev, int64_t m, int64_t n, int S,
+                     uint64_t *__restrict__ keys, unsigned long long *__restrict__ bad) {
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  unsigned long long nb = 0;
+  for (int64_t e = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; e < m; e += stride) {
+    const int64_t u = eu[e], v = ev[e];
+    if (u < 0 || u >= n || v < 0 || v >= n) {
+      nb++;
+      keys[e] = ~0ull;
+      continue;
+    }
+    const uint64_t a = static_cast<uint64_t>(u < v ? u : v), b = static_cast<uint64_t>(u < v ? v : u);
+    keys[e] = a == b ? ~0ull : (a << S) | b;
+  }
+  nb = warp_sum_u64(nb);
+  if (lane_id() == 0 && nb) atomicAdd(bad, nb);
+}
+
+// flag[e] = 1 for the first copy of each edge key (sorted input); self loops
+// and rejected edges (bits at or above 2S) are dropped.
+__global__ void __launch_bounds__(256)
+    unique_flag_kernel(const uint64_t *__restrict__ keys, int64_t m, int S, uint32_t *__restrict__ flag) {
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  for (int64_t e = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; e < m; e += stride) {
+    const uint64_t k = keys[e];
+    flag[e] = (k >> (2 * S)) == 0 && (e == 0 || keys[e - 1] != k) ? 1u : 0u;
+  }
+}
+
+// Degrees of vertices below kHubIds are counted per block in shared memory
+// first: skewed graphs send most edges to a few low-labelled hubs, whose
+// global counters would serialise in L2.
+constexpr int kHubIds = 8192;
+
+__global__ void __launch_bounds__(256)
+    compact_degree_kernel(const uint64_t *__restrict__ keys, int64_t m, int S, int64_t n,
+                          const uint32_t *__restrict__ flag, const uint32_t *__restrict__ pos,
+                          uint64_t *__restrict__ out, uint32_t *__restrict__ deg) {
+  __shared__ uint32_t hub[kHubIds];
+  for (int h = threadIdx.x; h < kHubIds; h += 256) hub[h] = 0;
+  __syncthreads();
+  const uint64_t mask = (uint64_t(1) << S) - 1;
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  for (int64_t e = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; e < m; e += stride) {
+    if (!flag[e]) continue;
+    const uint64_t k = keys[e];
+    out[pos[e]] = k;
+    const uint64_t a = k >> S, b = k & mask;
+    if (a < kHubIds) atomicAdd(&hub[a], 1u); else atomicAdd(deg + a, 1u);
+    if (b < kHubIds) atomicAdd(&hub[b], 1u); else atomicAdd(deg + b, 1u);
+  }
+  __syncthreads();
+  for (int h = threadIdx.x; h < kHubIds && h < n; h += 256)
+    if (hub[h]) atomicAdd(deg + h, hub[h]);
+}
+
+__global__ void __launch_bounds__(256)
+    max_kernel(const uint32_t *__restrict__ a, int64_t n, unsigned int *__restrict__ out) {
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  uint32_t m = 0;
+  for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += stride)
+    m = a[i] > m ? a[i] : m;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(kFull, m, o));
+  if (lane_id() == 0 && m) atomicMax(out, m);
+}
+
+__global__ void __launch_bounds__(256)
+    vertex_keys_kernel(const uint32_t *__restrict__ deg, int64_t n, int S, const unsigned int *__restrict__ maxdeg,
+                       uint64_t *__restrict__ vk) {
+  const uint64_t md = *maxdeg;
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  for (int64_t v = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; v < n; v += stride)
+    vk[v] = ((md - deg[v]) << S) | static_cast<uint64_t>(v);
+}
+
+__global__ void __launch_bounds__(256)
+    new_label_kernel(const uint64_t *__restrict__ vk, int64_t n, int S, uint32_t *__restrict__ newid) {
+  const uint64_t mask = (uint64_t(1) << S) - 1;
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  for (int64_t r = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; r < n; r += stride)
+    newid[vk[r] & mask] = static_cast<uint32_t>(r);
+}
+
+__global__ void __launch_bounds__(256)
+    lower_keys_kernel(const uint64_t *__restrict__ ukeys, int64_t nu, int S, const uint32_t *__restrict__ newid,
+                      uint64_t *__restrict__ lk) {
+  const uint64_t mask = (uint64_t(1) << S) - 1;
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  for (int64_t e = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; e < nu; e += stride) {
+    const uint64_t x = newid[ukeys[e] >> S], y = newid[ukeys[e] & mask];
+    lk[e] = x > y ? (x << S) | y : (y << S) | x;
+  }
+}
+
+// CSR from row-major sorted keys: offset[r] = first entry of row >= r, by a
+// binary search per row (rows may be empty in long runs: the isolated
+// vertices all take the last labels); nonzero[e] = the column.
+__global__ void __launch_bounds__(256)
+    csr_offsets_kernel(const uint64_t *__restrict__ lk, int64_t nu, int64_t n, int S,
+                       int64_t *__restrict__ offset) {
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  for (int64_t r = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; r <= n; r += stride) {
+    int64_t lo = 0, hi = nu;
+    while (lo < hi) {
+      const int64_t mid = (lo + hi) >> 1;
+      if (static_cast<int64_t>(lk[mid] >> S) < r) lo = mid + 1; else hi = mid;
+    }
+    offset[r] = lo;
+  }
+}
+
+__global__ void __launch_bounds__(256)
+    csr_cols_kernel(const uint64_t *__restrict__ lk, int64_t nu, int S, int64_t *__restrict__ nonzero) {
+  const uint64_t mask = (uint64_t(1) << S) - 1;
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  for (int64_t e = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; e < nu; e += stride)
+    nonzero[e] = static_cast<int64_t>(lk[e] & mask);
+}
+
+unsigned grid_for(int64_t n) {
+  const int64_t want = (n + 255) / 256, cap = static_cast<int64_t>(num_sms()) * 16;
+  return static_cast<unsigned>(std::max<int64_t>(1, std::min(want, cap)));
+}
+
+int label_bits(int64_t n) {
+  int S = 1;
+  while ((int64_t(1) << S) < n) S++;
+  return S;
+}
+
+// Workspace of one build: two key buffers (m), flags and positions (m + 1),
+// the sort histogram and its scan, degrees, labels, vertex keys (n each).
+struct Ws {
+  uint64_t *ka, *kb, *va, *vb;
+  uint32_t *flag, *pos, *hist, *hoff, *bsum, *deg, *newid;
+  unsigned int *words;  // [0] scan total, [1] max degree
+};
+
+size_t up256(size_t x) { return (x + 255) & ~size_t(255); }
+
+size_t ws_bytes(int64_t m, int64_t n, Ws *w, char *base) {
+  const int64_t mm = std::max<int64_t>(m, 1), nn = std::max<int64_t>(n, 1);
+  const int64_t tiles = (std::max(mm, nn) + kTile - 1) / kTile;
+  const int64_t hist_n = tiles * kDigits;
+  const int64_t scan_n = std::max(mm + 1, hist_n);
+  const int64_t nb = (scan_n + kScanBlock - 1) / kScanBlock + 1;
+  size_t o = 0;
+  auto take = [&](size_t bytes) {
+    const size_t at = o;
+    o += up256(bytes);
+    return base ? base + at : nullptr;
+  };
+  char *p;
+  p = take(8 * mm); if (w) w->ka = reinterpret_cast<uint64_t *>(p);
+  p = take(8 * mm); if (w) w->kb = reinterpret_cast<uint64_t *>(p);
+  p = take(8 * nn); if (w) w->va = reinterpret_cast<uint64_t *>(p);
+  p = take(8 * nn); if (w) w->vb = reinterpret_cast<uint64_t *>(p);
+  p = take(4 * (mm + 1)); if (w) w->flag = reinterpret_cast<uint32_t *>(p);
+  p = take(4 * (mm + 1)); if (w) w->pos = reinterpret_cast<uint32_t *>(p);
+  p = take(4 * hist_n); if (w) w->hist = reinterpret_cast<uint32_t *>(p);
+  p = take(4 * hist_n); if (w) w->hoff = reinterpret_cast<uint32_t *>(p);
+  p = take(4 * nb); if (w) w->bsum = reinterpret_cast<uint32_t *>(p);
+  p = take(4 * nn); if (w) w->deg = reinterpret_cast<uint32_t *>(p);
+  p = take(4 * nn); if (w) w->newid = reinterpret_cast<uint32_t *>(p);
+  p = take(64); if (w) w->words = reinterpret_cast<unsigned int *>(p);
+  return o;
+}
+
+// out[0,n) = exclusive prefix of in[0,n); *total = the sum.
+int excl_scan(const uint32_t *in, uint32_t *out, int64_t n, uint32_t *bsum, unsigned int *total, cudaStream_t st) {
+  const int64_t nb = std::max<int64_t>(1, (n + kScanBlock - 1) / kScanBlock);
+  scan_blocksum_kernel<<<static_cast<unsigned>(nb), kScanThreads, 0, st>>>(in, n, bsum);
+  scan_top_kernel<<<1, kScanThreads, 0, st>>>(bsum, nb, total);
+  scan_apply_kernel<<<static_cast<unsigned>(nb), kScanThreads, 0, st>>>(in, n, bsum, out);
+  BALE_CUDA_OK(cudaGetLastError());
+  return BALE_OK;
+}
+
+// Stable sort of n keys on bits [0, bits); returns the buffer holding the result.
+uint64_t *radix_sort(uint64_t *a, uint64_t *b, int64_t n, int bits, Ws &w, cudaStream_t st, int *rc) {
+  *rc = BALE_OK;
+  if (n <= 1) return a;
+  const int64_t tiles = (n + kTile - 1) / kTile;
+  for (int shift = 0; shift < bits; shift += kDigitBits) {
+    radix_hist_kernel<<<static_cast<unsigned>(tiles), kThreads, 0, st>>>(a, n, shift, w.hist, tiles);
+    *rc = excl_scan(w.hist, w.hoff, tiles * kDigits, w.bsum, w.words, st);
+    if (*rc != BALE_OK) return a;
+    radix_scatter_kernel<<<static_cast<unsigned>(tiles), kThreads, 0, st>>>(a, b, n, shift, w.hoff, tiles);
+    if (cudaGetLastError() != cudaSuccess) {
+      *rc = BALE_ECUDA;
+      return a;
+    }
+    std::swap(a, b);
+  }
+  return a;
+}
+
+// Steps 2-4 from the edge keys in w.ka (m of them).
+int build_from_keys(Ws &w, int64_t m, int64_t n, int S, int64_t *d_offset, int64_t *d_nonzero, int64_t *nnz,
+                    cudaStream_t st) {
+  int rc = BALE_OK;
+  const int kbits = std::min(64, 2 * S + 1);
+  uint64_t *sorted = radix_sort(w.ka, w.kb, m, kbits, w, st, &rc);
+  if (rc != BALE_OK) return rc;
+  uint64_t *other = sorted == w.ka ? w.kb : w.ka;
+  unique_flag_kernel<<<grid_for(m), 256, 0, st>>>(sorted, m, S, w.flag);
+  rc = excl_scan(w.flag, w.pos, m, w.bsum, w.words, st);
+  if (rc != BALE_OK) return rc;
+  BALE_CUDA_OK(cudaMemsetAsync(w.deg, 0, static_cast<size_t>(n) * 4, st));
+  compact_degree_kernel<<<grid_for(m), 256, 0, st>>>(sorted, m, S, n, w.flag, w.pos, other, w.deg);
+  unsigned int nu32 = 0;
+  BALE_CUDA_OK(cudaMemcpyAsync(&nu32, w.words, 4, cudaMemcpyDeviceToHost, st));
+  BALE_CUDA_OK(cudaMemsetAsync(w.words + 1, 0, 4, st));
+  max_kernel<<<grid_for(n), 256, 0, st>>>(w.deg, n, w.words + 1);
+  unsigned int maxdeg = 0;
+  BALE_CUDA_OK(cudaMemcpyAsync(&maxdeg, w.words + 1, 4, cudaMemcpyDeviceToHost, st));
+  BALE_CUDA_OK(cudaStreamSynchronize(st));
+  const int64_t nu = nu32;
+  vertex_keys_kernel<<<grid_for(n), 256, 0, st>>>(w.deg, n, S, w.words + 1, w.va);
+  int dbits = 1;
+  while ((uint64_t(1) << dbits) <= maxdeg) dbits++;
+  uint64_t *vs = radix_sort(w.va, w.vb, n, std::min(64, S + dbits), w, st, &rc);
+  if (rc != BALE_OK) return rc;
+  new_label_kernel<<<grid_for(n), 256, 0, st>>>(vs, n, S, w.newid);
+  uint64_t *lk = sorted;  // the unique keys are in `other`; reuse `sorted` for the lower keys
+  lower_keys_kernel<<<grid_for(nu), 256, 0, st>>>(other, nu, S, w.newid, lk);
+  uint64_t *ls = radix_sort(lk, other, nu, 2 * S, w, st, &rc);
+  if (rc != BALE_OK) return rc;
+  csr_offsets_kernel<<<grid_for(n + 1), 256, 0, st>>>(ls, nu, n, S, d_offset);
+  if (nu > 0) csr_cols_kernel<<<grid_for(nu), 256, 0, st>>>(ls, nu, S, d_nonzero);
+  BALE_CUDA_OK(cudaGetLastError());
+  BALE_CUDA_OK(cudaStreamSynchronize(st));
+  *nnz = nu;
+  return BALE_OK;
+}
+
+uint32_t prob_threshold(double p) {
+  if (p <= 0.0) return 0;
+  if (p >= 1.0) return UINT32_MAX;
+  return static_cast<uint32_t>(llround(p * 4294967296.0));
+}
+
+}  // namespace
+}  // namespace bale
+
+using namespace bale;
+
+extern "C" {
+
+int64_t bale_graph_build_workspace(int64_t m, int64_t n) {
+  if (m < 0 || n < 1) return -1;
+  return static_cast<int64_t>(ws_bytes(m, n, nullptr, nullptr));
+}
+
+int bale_graph_build_dev(const int64_t *d_u, const int64_t *d_v, int64_t m, int64_t n, int64_t *d_offset,
+                         int64_t *d_nonzero, int64_t *nnz, void *stream) {
+  if (m < 0 || n < 1 || n > (int64_t(1) << 31) || m >= (int64_t(1) << 32) - 1 || !d_offset || !nnz ||
+      (m > 0 && (!d_u || !d_v || !d_nonzero))) {
+    set_error("bale_graph_build_dev: bad arguments (m=%lld, n=%lld)", static_cast<long long>(m),
+              static_cast<long long>(n));
+    return BALE_EINVAL;
+  }
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const int S = label_bits(n);
+  Ws w;
+  void *ws = device_workspace(ws_bytes(m, n, nullptr, nullptr), st);
+  if (!ws) return BALE_ENOMEM;
+  ws_bytes(m, n, &w, static_cast<char *>(ws));
+  unsigned long long *bad = reinterpret_cast<unsigned long long *>(w.words + 4);
+  BALE_CUDA_OK(cudaMemsetAsync(w.words, 0, 64, st));
+  if (m > 0) {
+    edge_keys_kernel<<<grid_for(m), 256, 0, st>>>(d_u, d_v, m, n, S, w.ka, bad);
+    BALE_CUDA_OK(cudaGetLastError());
+  }
+  unsigned long long nbad = 0;
+  BALE_CUDA_OK(cudaMemcpyAsync(&nbad, bad, 8, cudaMemcpyDeviceToHost, st));
+  BALE_CUDA_OK(cudaStreamSynchronize(st));
+  if (nbad) {
+    set_error("bale_graph_build_dev: %llu edges with an endpoint outside [0, n)", nbad);
+    return BALE_EINPUT;
+  }
+  return build_from_keys(w, m, n, S, d_offset, d_nonzero, nnz, st);
+}
+
+int bale_gen_rmat_dev(int64_t scale, int64_t edgefactor, double a, double b, double c, uint64_t seed,
+                      int64_t *d_offset, int64_t *d_nonzero, int64_t *nnz, void *stream) {
+  if (scale < 1 || scale > 31 || edgefactor < 1 || a < 0 || b < 0 || c < 0 || a + b + c > 1.0 || !d_offset ||
+      !d_nonzero || !nnz || (edgefactor << scale) >= (int64_t(1) << 32) - 1) {
+    set_error("bale_gen_rmat_dev: bad arguments");
+    return BALE_EINVAL;
+  }
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const int S = static_cast<int>(scale);
+  const int64_t n = int64_t(1) << S, m = edgefactor * n;
+  Ws w;
+  void *ws = device_workspace(ws_bytes(m, n, nullptr, nullptr), st);
+  if (!ws) return BALE_ENOMEM;
+  ws_bytes(m, n, &w, static_cast<char *>(ws));
+  BALE_CUDA_OK(cudaMemsetAsync(w.words, 0, 64, st));
+  rmat_keys_kernel<<<grid_for(m), 256, 0, st>>>(w.ka, m, S, prob_threshold(a), prob_threshold(a + b),
+                                                 prob_threshold(a + b + c), seed);
+  BALE_CUDA_OK(cudaGetLastError());
+  return build_from_keys(w, m, n, S, d_offset, d_nonzero, nnz, st);
+}
+
+}  // extern "C"

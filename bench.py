@@ -416,6 +416,59 @@ def run_triangles(ctx) -> dict:
     return out
 
 
+def run_graph(ctx) -> dict:
+    """Building the triangle input on the device: R-MAT scale 22 generated
+    and turned into the degree-ordered strictly lower CSR (bale_gen_rmat_dev),
+    against the same build on the host cores (bale_gen_rmat)."""
+    import torch
+
+    bale, dev, args = ctx["bale"], ctx["dev"], ctx["args"]
+    S, ef = TRI_SCALE, 16
+    m = ef << S
+    holder = {}
+
+    def fn():
+        holder["g"] = bale.gen_rmat_dev(S, ef, 0.57, 0.19, 0.19, 6, device=dev)
+
+    with ClockSampler(ctx["gpu"]) as clocks:
+        ctx["dist"].barrier()
+        ms = time_device(fn, args.steps, args.warmup)
+    ms_max = ctx["dist"].max(ms)
+    off, col = holder.pop("g")
+    nnz = col.numel()
+    offs_h, col_h = off.cpu().numpy(), col.cpu().numpy()
+    maxdeg = int((np.diff(offs_h) + np.bincount(col_h, minlength=1 << S)).max())
+    p_edges, p_vert, p_lower = (2 * S + 1 + 7) // 8, (S + maxdeg.bit_length() + 7) // 8, (2 * S + 7) // 8
+    # the dominant work: three LSD radix sorts, each 8-bit pass reading every
+    # 8-byte key twice (histogram, scatter) and writing it once
+    algo = 24 * (p_edges * m + p_vert * (1 << S) + p_lower * nnz)
+    launches = 1 + 5 * p_edges + 1 + 3 + 1 + 1 + 1 + 5 * p_vert + 1 + 1 + 5 * p_lower + 2
+    out = {"metric": "G input edges/s building the degree-ordered lower CSR (R-MAT scale 22) on the device",
+           "value": round(job_rate(m, ms_max / 1e3, ctx["dist"].world) / 1e9, 4), "unit": "G edges/s",
+           "ms_per_step": round(ms_max, 3), "nnz": nnz,
+           "roofline": roofline(ctx, "graph", algo, ms / 1e3,
+                                "the build's radix sorts (hist + scatter per 8-bit pass) and graph steps",
+                                note="algorithmic bytes: 24 B per key per 8-bit pass over the m edge keys "
+                                     "(45 bits), the 2^22 vertex keys and the nnz lower keys (44 bits); the "
+                                     "generation, dedup and CSR steps are not counted"),
+           "clocks": clocks.summary(), "gpu_launches": launches * args.steps,
+           "config": {"workload": "R-MAT scale 22, edge factor 16, (0.57,0.19,0.19,0.05): 67,108,864 generated "
+                                  "edges -> symmetrised, deduplicated, degree-ordered strictly lower CSR",
+                      "edges": m, "nnz": nnz}}
+    if ctx["cpu"]:
+        t0 = time.perf_counter()
+        L = bale.gen_rmat(S, ef, 0.57, 0.19, 0.19, 6)
+        secs = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": round(m / secs / 1e9, 5), "unit": "G edges/s",
+                               "cores": _oracle().num_cpus(), "kind": "port",
+                               "sample": "1 x the same build on the host (bale_gen_rmat: parallel radix sort, "
+                                         "counting-sort relabel, per-row sort)", "seconds": round(secs, 2)}
+        out["parity_ok"] = bool(np.array_equal(offs_h, L.offset) and np.array_equal(col_h, L.nonzero))
+    del off, col
+    torch.cuda.empty_cache()
+    return out
+
+
 def run_batch(ctx, small: bool = False) -> dict:
     import torch
 
@@ -663,12 +716,12 @@ def run_gb300(args, dist: Dist) -> dict | None:
     runners = {"ig": lambda: run_ig(ctx, False), "ig_zipf": lambda: run_ig(ctx, True),
                "histo": lambda: run_histo(ctx), "triangles": lambda: run_triangles(ctx),
                "batch": lambda: run_batch(ctx), "batch_small": lambda: run_batch(ctx, small=True),
-               "serve": lambda: run_serve(ctx)}
+               "serve": lambda: run_serve(ctx), "graph": lambda: run_graph(ctx)}
     head = runners[args.workload]()
     torch.cuda.empty_cache()
     if not args.only:
         others = {}
-        for wl in ("ig_zipf", "histo", "triangles", "batch", "batch_small", "serve", "ig"):
+        for wl in ("ig_zipf", "histo", "triangles", "graph", "batch", "batch_small", "serve", "ig"):
             if wl != args.workload:
                 others[wl] = runners[wl]()
                 torch.cuda.empty_cache()
@@ -718,7 +771,7 @@ def main(argv=None) -> int:
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="ig", choices=["ig", "ig_zipf", "histo", "triangles", "batch", "batch_small", "serve"])
+    ap.add_argument("--workload", default="ig", choices=["ig", "ig_zipf", "histo", "triangles", "graph", "batch", "batch_small", "serve"])
     ap.add_argument("--only", action="store_true", help="measure the selected workload only")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=8.0, help="seconds of CPU baseline per workload")

@@ -177,6 +177,26 @@ BALE_API bale_tri_prepared_t *bale_triangle_prepare(const int64_t *d_offset, con
 BALE_API int bale_triangle_count_prepared(bale_tri_prepared_t *g, int64_t *d_count, int64_t *d_work, void *stream);
 BALE_API void bale_triangle_release(bale_tri_prepared_t *g);
 
+/* ======================= graph building on the device ================== */
+/* The triangle kernels' input built in HBM: from an undirected edge list   */
+/* (d_u[e], d_v[e] in [0,n); duplicates, both orientations and self loops   */
+/* allowed) the strictly lower CSR of the simple graph, vertices relabelled */
+/* by descending degree (ties by ascending label), columns ascending -- the */
+/* reference's tidy lower matrix (spmat/spmat_utils.upc:455-473 tril,       */
+/* :1055-1062 sort_nonzeros).  d_offset[n+1]; d_nonzero needs room for m    */
+/* entries; *nnz receives the count.  Synchronous; BALE_EINPUT if an        */
+/* endpoint is outside [0,n).  n <= 2^31, m < 2^32 - 1.  New entry points.   */
+BALE_API int bale_graph_build_dev(const int64_t *d_u, const int64_t *d_v, int64_t m, int64_t n,
+                                  int64_t *d_offset, int64_t *d_nonzero, int64_t *nnz, void *stream);
+/* Device scratch a build of m edges on n vertices takes (bytes). */
+BALE_API int64_t bale_graph_build_workspace(int64_t m, int64_t n);
+/* bale_gen_rmat's graph (include/bale_inputs.h) generated and built on the */
+/* device, bit-identical: d_offset[2^scale + 1], d_nonzero room for          */
+/* edgefactor * 2^scale entries.                                            */
+BALE_API int bale_gen_rmat_dev(int64_t scale, int64_t edgefactor, double a, double b, double c,
+                               uint64_t seed, int64_t *d_offset, int64_t *d_nonzero, int64_t *nnz,
+                               void *stream);
+
 /* ======================= batched execution ============================== */
 /* Many instances of uneven size in one CUDA graph: a persistent work-queue  */
 /* kernel takes tiles of every instance (tile sizes per kind and size class  */

@@ -326,6 +326,44 @@ def gen_rmat_dev(scale: int, edgefactor: int, a: float, b: float, c: float, seed
     return off, nz[: nnz.value]
 
 
+def transpose_dev(offset, nonzero, numcols: int, stream=None):
+    """spmat's transpose_matrix_agi on the device: returns At's (offset, nonzero)."""
+    import torch
+
+    n, nnz = offset.numel() - 1, nonzero.numel()
+    toff = torch.empty(numcols + 1, dtype=torch.int64, device=offset.device)
+    tcol = torch.empty(max(nnz, 1), dtype=torch.int64, device=offset.device)
+    _status(_lib.bale_transpose_dev(_dptr(offset, "offset"), _dptr(nonzero, "nonzero") if nnz else None, n,
+                                    int(numcols), nnz, _dptr(toff, "toffset"), _dptr(tcol, "tnonzero"),
+                                    _stream(stream)), "bale_transpose_dev")
+    return toff, tcol[:nnz]
+
+
+def permute_dev(offset, nonzero, numcols: int, rperminv, cperminv, stream=None):
+    """spmat's permute_matrix_agi on the device: returns (offset, nonzero)."""
+    import torch
+
+    n, nnz = offset.numel() - 1, nonzero.numel()
+    poff = torch.empty(n + 1, dtype=torch.int64, device=offset.device)
+    pcol = torch.empty(max(nnz, 1), dtype=torch.int64, device=offset.device)
+    _status(_lib.bale_permute_dev(_dptr(offset, "offset"), _dptr(nonzero, "nonzero") if nnz else None, n,
+                                  int(numcols), nnz, _dptr(rperminv, "rperminv"), _dptr(cperminv, "cperminv"),
+                                  _dptr(poff, "poffset"), _dptr(pcol, "pnonzero"), _stream(stream)),
+            "bale_permute_dev")
+    return poff, pcol[:nnz]
+
+
+def rand_perm_dev(n: int, seed: int, device=None, stream=None):
+    """spmat's rand_permp_agi(n, seed) on the device (a device int64 tensor)."""
+    import torch
+
+    dev = device if device is not None else torch.device("cuda", torch.cuda.current_device())
+    out = torch.empty(max(n, 1), dtype=torch.int64, device=dev)
+    _status(_lib.bale_rand_perm_dev(int(n), seed & (2**64 - 1), _dptr(out, "perm"), _stream(stream)),
+            "bale_rand_perm_dev")
+    return out[:n]
+
+
 class TrianglePrepared:
     """A device CSR counted repeatedly (bale_triangle_prepare): validation,
     the 32-bit column copy and the transpose are built once; count() adds

@@ -86,6 +86,9 @@ SIGNATURES: dict[str, tuple[object, list[object]]] = {
     "bale_graph_build_dev": (C.c_int, [VP, VP, i64, i64, VP, VP, P64, VP]),
     "bale_graph_build_workspace": (i64, [i64, i64]),
     "bale_gen_rmat_dev": (C.c_int, [i64, i64, C.c_double, C.c_double, C.c_double, C.c_uint64, VP, VP, P64, VP]),
+    "bale_transpose_dev": (C.c_int, [VP, VP, i64, i64, i64, VP, VP, VP]),
+    "bale_permute_dev": (C.c_int, [VP, VP, i64, i64, i64, VP, VP, VP, VP, VP]),
+    "bale_rand_perm_dev": (C.c_int, [i64, C.c_uint64, VP, VP]),
     "bale_triangle_prepare": (VP, [VP, VP, i64, i64, VP, VP]),
     "bale_triangle_count_prepared": (C.c_int, [VP, VP, VP, VP]),
     "bale_triangle_release": (None, [VP]),

@@ -435,6 +435,166 @@ int build_from_keys(Ws &w, int64_t m, int64_t n, int S, int64_t *d_offset, int64
   return BALE_OK;
 }
 
+// ---------------------------------------------------------------- spmat ops
+// CSR checks shared by transpose and permute: offsets ascending inside
+// [0, nnz] with offset[numrows] == nnz, columns inside [0, numcols).
+__global__ void __launch_bounds__(256)
+    csr_check_kernel(const int64_t *__restrict__ off, const int64_t *__restrict__ col, int64_t numrows,
+                     int64_t numcols, int64_t nnz, unsigned long long *__restrict__ bad) {
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  unsigned long long nb = 0;
+  for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i <= numrows; i += stride) {
+    const int64_t o = off[i];
+    if (o < 0 || o > nnz || (i < numrows && off[i + 1] < o) || (i == numrows && o != nnz) || (i == 0 && o != 0))
+      nb++;
+  }
+  for (int64_t k = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; k < nnz; k += stride)
+    if (col[k] < 0 || col[k] >= numcols) nb++;
+  nb = warp_sum_u64(nb);
+  if (lane_id() == 0 && nb) atomicAdd(bad, nb);
+}
+
+// keys[k] = col << rb | row, the row of nonzero k found by a binary search
+// over the (checked) offsets.
+__global__ void __launch_bounds__(256)
+    transpose_keys_kernel(const int64_t *__restrict__ off, const int64_t *__restrict__ col, int64_t numrows,
+                          int64_t nnz, int rb, uint64_t *__restrict__ keys) {
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  for (int64_t k = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; k < nnz; k += stride) {
+    int64_t lo = 0, hi = numrows;  // the last row i with off[i] <= k
+    while (hi - lo > 1) {
+      const int64_t mid = (lo + hi) >> 1;
+      if (off[mid] <= k) lo = mid; else hi = mid;
+    }
+    keys[k] = (static_cast<uint64_t>(col[k]) << rb) | static_cast<uint64_t>(lo);
+  }
+}
+
+// seen[p[i]]++ for a claimed permutation p of [0, n); entries outside count as bad.
+__global__ void __launch_bounds__(256)
+    perm_seen_kernel(const int64_t *__restrict__ p, int64_t n, uint32_t *__restrict__ seen,
+                     unsigned long long *__restrict__ bad) {
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  unsigned long long nb = 0;
+  for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += stride) {
+    const int64_t v = p[i];
+    if (v < 0 || v >= n) nb++;
+    else atomicAdd(seen + v, 1u);
+  }
+  nb = warp_sum_u64(nb);
+  if (lane_id() == 0 && nb) atomicAdd(bad, nb);
+}
+
+__global__ void __launch_bounds__(256)
+    perm_once_kernel(const uint32_t *__restrict__ seen, int64_t n, unsigned long long *__restrict__ bad) {
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  unsigned long long nb = 0;
+  for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += stride)
+    nb += seen[i] != 1u;
+  nb = warp_sum_u64(nb);
+  if (lane_id() == 0 && nb) atomicAdd(bad, nb);
+}
+
+// rperm[rperminv[i]] = i; len[i] = the length of row rperm[i] of A.
+__global__ void __launch_bounds__(256)
+    permute_rows_kernel(const int64_t *__restrict__ off, const int64_t *__restrict__ rperminv, int64_t n,
+                        uint32_t *__restrict__ rperm) {
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += stride)
+    rperm[rperminv[i]] = static_cast<uint32_t>(i);
+}
+
+__global__ void __launch_bounds__(256)
+    permute_len_kernel(const int64_t *__restrict__ off, const uint32_t *__restrict__ rperm, int64_t n,
+                       uint32_t *__restrict__ len) {
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += stride)
+    len[i] = static_cast<uint32_t>(off[rperm[i] + 1] - off[rperm[i]]);
+}
+
+// One warp per new row i: row rperm[i] of A, columns through cperminv.
+__global__ void __launch_bounds__(256)
+    permute_fill_kernel(const int64_t *__restrict__ off, const int64_t *__restrict__ col,
+                        const uint32_t *__restrict__ rperm, const uint32_t *__restrict__ pstart, int64_t n,
+                        int64_t nnz, const int64_t *__restrict__ cperminv, int64_t *__restrict__ poff,
+                        int64_t *__restrict__ pcol) {
+  const int64_t warps = static_cast<int64_t>(gridDim.x) * (blockDim.x / 32);
+  const unsigned lane = lane_id();
+  for (int64_t i = static_cast<int64_t>(blockIdx.x) * (blockDim.x / 32) + (threadIdx.x >> 5); i < n; i += warps) {
+    const int64_t b = off[rperm[i]], d = off[rperm[i] + 1] - b, o = pstart[i];
+    if (lane == 0) poff[i] = o;
+    for (int64_t t = lane; t < d; t += 32) pcol[o + t] = cperminv[col[b + t]];
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) poff[n] = nnz;
+}
+
+// The drand48 generator (POSIX): X' = (0x5deece66d X + 0xb) mod 2^48,
+// lrand48 = X >> 17; srand48(s) sets X = (s & 0xffffffff) << 16 | 0x330e.
+// The low 48 bits of 64-bit products are exact, so u64 arithmetic suffices.
+constexpr uint64_t kLcgA = 0x5deece66dull, kLcgC = 0xbull, kLcgMask = (1ull << 48) - 1;
+
+// X after k steps from x: the affine map raised to k by squaring.
+__device__ __forceinline__ uint64_t lcg_jump(uint64_t x, uint64_t k) {
+  uint64_t a = kLcgA, c = kLcgC, ra = 1, rc = 0;  // result map: x -> ra x + rc
+  while (k) {
+    if (k & 1) {
+      ra = (ra * a) & kLcgMask;
+      rc = (rc * a + c) & kLcgMask;
+    }
+    c = (c * a + c) & kLcgMask;  // compose the map with itself
+    a = (a * a) & kLcgMask;
+    k >>= 1;
+  }
+  return (ra * x + rc) & kLcgMask;
+}
+
+// Throw t (the (t+1)-th lrand48 output) lands in slot r_t = lrand48 % m;
+// keys[t] = r_t << tb | t.  Each thread takes a run of consecutive throws.
+constexpr int kThrowsPerThread = 64;
+
+__global__ void __launch_bounds__(256)
+    throws_kernel(uint64_t x0, int64_t nthrows, uint64_t m, int tb, uint64_t *__restrict__ keys) {
+  const int64_t first = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) * kThrowsPerThread;
+  if (first >= nthrows) return;
+  uint64_t x = lcg_jump(x0, static_cast<uint64_t>(first));
+  const int64_t last = first + kThrowsPerThread < nthrows ? first + kThrowsPerThread : nthrows;
+  for (int64_t t = first; t < last; t++) {
+    x = (kLcgA * x + kLcgC) & kLcgMask;
+    keys[t] = (((x >> 17) % m) << tb) | static_cast<uint64_t>(t);
+  }
+}
+
+// In slot order (keys sorted by slot, then throw): the first throw at each
+// slot hit it; succ[t] = 1 for those.
+__global__ void __launch_bounds__(256)
+    first_hit_kernel(const uint64_t *__restrict__ sk, int64_t nthrows, int tb, uint32_t *__restrict__ succ) {
+  const uint64_t tmask = (uint64_t(1) << tb) - 1;
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  for (int64_t j = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; j < nthrows; j += stride)
+    succ[sk[j] & tmask] = (j == 0 || (sk[j] >> tb) != (sk[j - 1] >> tb)) ? 1u : 0u;
+}
+
+// used[j] = slot-order entry j is one of the first n hits.
+__global__ void __launch_bounds__(256)
+    used_kernel(const uint64_t *__restrict__ sk, int64_t nthrows, int tb, const uint32_t *__restrict__ succ,
+                const uint32_t *__restrict__ rank, uint32_t n, uint32_t *__restrict__ used) {
+  const uint64_t tmask = (uint64_t(1) << tb) - 1;
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  for (int64_t j = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; j < nthrows; j += stride) {
+    const uint64_t t = sk[j] & tmask;
+    used[j] = succ[t] && rank[t] < n ? 1u : 0u;
+  }
+}
+
+__global__ void __launch_bounds__(256)
+    perm_out_kernel(const uint64_t *__restrict__ sk, int64_t nthrows, int tb, const uint32_t *__restrict__ used,
+                    const uint32_t *__restrict__ upos, const uint32_t *__restrict__ rank, int64_t *__restrict__ perm) {
+  const uint64_t tmask = (uint64_t(1) << tb) - 1;
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  for (int64_t j = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; j < nthrows; j += stride)
+    if (used[j]) perm[upos[j]] = rank[sk[j] & tmask];
+}
+
 uint32_t prob_threshold(double p) {
   if (p <= 0.0) return 0;
   if (p >= 1.0) return UINT32_MAX;
@@ -502,6 +662,138 @@ int bale_gen_rmat_dev(int64_t scale, int64_t edgefactor, double a, double b, dou
                                                  prob_threshold(a + b + c), seed);
   BALE_CUDA_OK(cudaGetLastError());
   return build_from_keys(w, m, n, S, d_offset, d_nonzero, nnz, st);
+}
+
+int bale_transpose_dev(const int64_t *d_offset, const int64_t *d_nonzero, int64_t numrows, int64_t numcols,
+                       int64_t nnz, int64_t *d_toffset, int64_t *d_tnonzero, void *stream) {
+  if (numrows < 1 || numcols < 1 || numrows > (int64_t(1) << 31) || numcols > (int64_t(1) << 31) || nnz < 0 ||
+      nnz >= (int64_t(1) << 32) - 1 || !d_offset || !d_toffset || (nnz > 0 && (!d_nonzero || !d_tnonzero))) {
+    set_error("bale_transpose_dev: bad arguments");
+    return BALE_EINVAL;
+  }
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const int rb = label_bits(numrows), cb = label_bits(numcols);
+  Ws w;
+  void *ws = device_workspace(ws_bytes(nnz, std::max(numrows, numcols), nullptr, nullptr), st);
+  if (!ws) return BALE_ENOMEM;
+  ws_bytes(nnz, std::max(numrows, numcols), &w, static_cast<char *>(ws));
+  unsigned long long *bad = reinterpret_cast<unsigned long long *>(w.words + 4);
+  BALE_CUDA_OK(cudaMemsetAsync(w.words, 0, 64, st));
+  csr_check_kernel<<<grid_for(std::max(numrows + 1, nnz)), 256, 0, st>>>(d_offset, d_nonzero, numrows, numcols,
+                                                                          nnz, bad);
+  unsigned long long nbad = 0;
+  BALE_CUDA_OK(cudaMemcpyAsync(&nbad, bad, 8, cudaMemcpyDeviceToHost, st));
+  BALE_CUDA_OK(cudaStreamSynchronize(st));
+  if (nbad) {
+    set_error("bale_transpose_dev: %llu malformed offsets or columns", nbad);
+    return BALE_EINPUT;
+  }
+  int rc = BALE_OK;
+  if (nnz > 0) {
+    transpose_keys_kernel<<<grid_for(nnz), 256, 0, st>>>(d_offset, d_nonzero, numrows, nnz, rb, w.ka);
+    BALE_CUDA_OK(cudaGetLastError());
+  }
+  uint64_t *sk = radix_sort(w.ka, w.kb, nnz, rb + cb, w, st, &rc);
+  if (rc != BALE_OK) return rc;
+  csr_offsets_kernel<<<grid_for(numcols + 1), 256, 0, st>>>(sk, nnz, numcols, rb, d_toffset);
+  if (nnz > 0) csr_cols_kernel<<<grid_for(nnz), 256, 0, st>>>(sk, nnz, rb, d_tnonzero);
+  BALE_CUDA_OK(cudaGetLastError());
+  BALE_CUDA_OK(cudaStreamSynchronize(st));
+  return BALE_OK;
+}
+
+int bale_permute_dev(const int64_t *d_offset, const int64_t *d_nonzero, int64_t numrows, int64_t numcols,
+                     int64_t nnz, const int64_t *d_rperminv, const int64_t *d_cperminv, int64_t *d_poffset,
+                     int64_t *d_pnonzero, void *stream) {
+  if (numrows < 1 || numcols < 1 || numrows >= (int64_t(1) << 32) - 1 || nnz < 0 ||
+      nnz >= (int64_t(1) << 32) - 1 || !d_offset || !d_rperminv || !d_cperminv || !d_poffset ||
+      (nnz > 0 && (!d_nonzero || !d_pnonzero))) {
+    set_error("bale_permute_dev: bad arguments");
+    return BALE_EINVAL;
+  }
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  Ws w;
+  const int64_t nmax = std::max(numrows, numcols);
+  void *ws = device_workspace(ws_bytes(std::max<int64_t>(nnz, nmax), nmax, nullptr, nullptr), st);
+  if (!ws) return BALE_ENOMEM;
+  ws_bytes(std::max<int64_t>(nnz, nmax), nmax, &w, static_cast<char *>(ws));
+  unsigned long long *bad = reinterpret_cast<unsigned long long *>(w.words + 4);
+  BALE_CUDA_OK(cudaMemsetAsync(w.words, 0, 64, st));
+  csr_check_kernel<<<grid_for(std::max(numrows + 1, nnz)), 256, 0, st>>>(d_offset, d_nonzero, numrows, numcols,
+                                                                          nnz, bad);
+  // both permutations: every label exactly once
+  BALE_CUDA_OK(cudaMemsetAsync(w.deg, 0, static_cast<size_t>(numrows) * 4, st));
+  perm_seen_kernel<<<grid_for(numrows), 256, 0, st>>>(d_rperminv, numrows, w.deg, bad);
+  perm_once_kernel<<<grid_for(numrows), 256, 0, st>>>(w.deg, numrows, bad);
+  BALE_CUDA_OK(cudaMemsetAsync(w.newid, 0, static_cast<size_t>(numcols) * 4, st));
+  perm_seen_kernel<<<grid_for(numcols), 256, 0, st>>>(d_cperminv, numcols, w.newid, bad);
+  perm_once_kernel<<<grid_for(numcols), 256, 0, st>>>(w.newid, numcols, bad);
+  unsigned long long nbad = 0;
+  BALE_CUDA_OK(cudaMemcpyAsync(&nbad, bad, 8, cudaMemcpyDeviceToHost, st));
+  BALE_CUDA_OK(cudaStreamSynchronize(st));
+  if (nbad) {
+    set_error("bale_permute_dev: %llu malformed offsets, columns or permutation entries", nbad);
+    return BALE_EINPUT;
+  }
+  uint32_t *rperm = w.deg, *len = w.flag, *pstart = w.pos;
+  permute_rows_kernel<<<grid_for(numrows), 256, 0, st>>>(d_offset, d_rperminv, numrows, rperm);
+  permute_len_kernel<<<grid_for(numrows), 256, 0, st>>>(d_offset, rperm, numrows, len);
+  int rc = excl_scan(len, pstart, numrows, w.bsum, w.words, st);
+  if (rc != BALE_OK) return rc;
+  permute_fill_kernel<<<grid_for(numrows * 32), 256, 0, st>>>(d_offset, d_nonzero, rperm, pstart, numrows, nnz,
+                                                              d_cperminv, d_poffset, d_pnonzero);
+  BALE_CUDA_OK(cudaGetLastError());
+  BALE_CUDA_OK(cudaStreamSynchronize(st));
+  return BALE_OK;
+}
+
+int bale_rand_perm_dev(int64_t n, uint64_t seed, int64_t *d_perm, void *stream) {
+  if (n < 0 || n >= (int64_t(1) << 30) || (n > 0 && !d_perm)) {
+    set_error("bale_rand_perm_dev: bad arguments (n=%lld)", static_cast<long long>(n));
+    return BALE_EINVAL;
+  }
+  if (n == 0) return BALE_OK;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const uint64_t m = 2 * static_cast<uint64_t>(n);
+  const uint64_t x0 = ((seed & 0xffffffffull) << 16) | 0x330eull;
+  int mb = 1;
+  while ((uint64_t(1) << mb) < m) mb++;
+  // throws: about 1.39 n are needed for n distinct slots among 2n; take
+  // 1.5 n + 1024 and double until the n-th first hit is among them
+  for (int64_t nt = n + n / 2 + 1024;; nt *= 2) {
+    int tb = 1;
+    while ((int64_t(1) << tb) < nt) tb++;
+    if (mb + tb > 64) {
+      set_error("bale_rand_perm_dev: too many throws");
+      return BALE_EINVAL;
+    }
+    Ws w;
+    void *ws = device_workspace(ws_bytes(nt, nt, nullptr, nullptr), st);
+    if (!ws) return BALE_ENOMEM;
+    ws_bytes(nt, nt, &w, static_cast<char *>(ws));
+    BALE_CUDA_OK(cudaMemsetAsync(w.words, 0, 64, st));
+    const int64_t threads = (nt + kThrowsPerThread - 1) / kThrowsPerThread;
+    throws_kernel<<<static_cast<unsigned>((threads + 255) / 256), 256, 0, st>>>(x0, nt, m, tb, w.ka);
+    BALE_CUDA_OK(cudaGetLastError());
+    int rc = BALE_OK;
+    uint64_t *sk = radix_sort(w.ka, w.kb, nt, mb + tb, w, st, &rc);
+    if (rc != BALE_OK) return rc;
+    uint32_t *succ = w.flag, *rank = w.pos, *used = w.deg, *upos = w.newid;
+    first_hit_kernel<<<grid_for(nt), 256, 0, st>>>(sk, nt, tb, succ);
+    rc = excl_scan(succ, rank, nt, w.bsum, w.words, st);
+    if (rc != BALE_OK) return rc;
+    unsigned int hits = 0;
+    BALE_CUDA_OK(cudaMemcpyAsync(&hits, w.words, 4, cudaMemcpyDeviceToHost, st));
+    BALE_CUDA_OK(cudaStreamSynchronize(st));
+    if (static_cast<int64_t>(hits) < n) continue;  // the n-th hit is further on
+    used_kernel<<<grid_for(nt), 256, 0, st>>>(sk, nt, tb, succ, rank, static_cast<uint32_t>(n), used);
+    rc = excl_scan(used, upos, nt, w.bsum, w.words, st);
+    if (rc != BALE_OK) return rc;
+    perm_out_kernel<<<grid_for(nt), 256, 0, st>>>(sk, nt, tb, used, upos, rank, d_perm);
+    BALE_CUDA_OK(cudaGetLastError());
+    BALE_CUDA_OK(cudaStreamSynchronize(st));
+    return BALE_OK;
+  }
 }
 
 }  // extern "C"

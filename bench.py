@@ -469,6 +469,72 @@ def run_graph(ctx) -> dict:
     return out
 
 
+def run_spmat(ctx) -> dict:
+    """spmat's transpose, permutation and random permutation on the device
+    (the R-MAT scale-22 lower matrix, a 2^26-entry permutation), against the
+    oracle's one-thread restatements of the reference at one PE."""
+    import torch
+
+    bale, dev, args = ctx["bale"], ctx["dev"], ctx["args"]
+    S = TRI_SCALE
+    off, col = bale.gen_rmat_dev(S, 16, 0.57, 0.19, 0.19, 6, device=dev)
+    n, nnz = off.numel() - 1, col.numel()
+    rinv = bale.rand_perm_dev(n, 11, device=dev)
+    cinv = bale.rand_perm_dev(n, 12, device=dev)
+    np_ = 1 << 26
+    holder = {}
+    with ClockSampler(ctx["gpu"]) as clocks:
+        ctx["dist"].barrier()
+        t_ms = time_device(lambda: holder.__setitem__("t", bale.transpose_dev(off, col, n)), args.steps, args.warmup)
+        p_ms = time_device(lambda: holder.__setitem__("p", bale.permute_dev(off, col, n, rinv, cinv)),
+                           args.steps, args.warmup)
+        r_ms = time_device(lambda: holder.__setitem__("r", bale.rand_perm_dev(np_, 31, device=dev)),
+                           args.steps, args.warmup)
+    t_ms, p_ms, r_ms = (ctx["dist"].max(x) for x in (t_ms, p_ms, r_ms))
+    w = ctx["dist"].world
+    out = {"metric": "G nonzeros/s transposing the R-MAT scale-22 lower matrix on the device",
+           "value": round(job_rate(nnz, t_ms / 1e3, w) / 1e9, 4), "unit": "G nonzeros/s",
+           "ms_per_step": round(t_ms, 3),
+           "permute": {"value": round(job_rate(nnz, p_ms / 1e3, w) / 1e9, 4), "unit": "G nonzeros/s",
+                       "ms_per_step": round(p_ms, 3)},
+           "rand_perm": {"value": round(job_rate(np_, r_ms / 1e3, w) / 1e9, 4), "unit": "G elements/s",
+                         "ms_per_step": round(r_ms, 3), "n": np_},
+           # transpose: the sort's passes dominate -- 24 B per key per 8-bit pass
+           "roofline": roofline(ctx, "spmat", 24 * ((2 * S + 7) // 8) * nnz, t_ms / 1e3,
+                                "transpose: radix sort of (column, row) keys",
+                                note="algorithmic bytes: 24 B per key per 8-bit pass (44-bit keys); the "
+                                     "check, key and CSR kernels are not counted"),
+           "clocks": clocks.summary(), "gpu_launches": None,
+           "config": {"workload": "transpose_matrix / permute_matrix of the R-MAT scale-22 degree-ordered lower "
+                                  "matrix (n = 2^22, 64,155,075 nonzeros); rand_permp of 2^26 elements",
+                      "nnz": nnz}}
+    if ctx["cpu"]:
+        orc = _oracle()
+        offh, colh = off.cpu().numpy(), col.cpu().numpy()
+        t0 = time.perf_counter()
+        to, tc = orc.transpose(offh, colh, n)
+        t_cpu = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        orc.permute(offh, colh, rinv.cpu().numpy(), cinv.cpu().numpy())
+        p_cpu = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        rp = orc.rand_perm(1 << 22, 31)
+        r_cpu = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": round(nnz / t_cpu / 1e9, 5), "unit": "G nonzeros/s", "cores": 1,
+                               "kind": "port",
+                               "sample": "transpose_matrix_agi at one PE (oracle restatement) of the same matrix",
+                               "permute_G_nonzeros_s": round(nnz / p_cpu / 1e9, 5),
+                               "rand_perm_G_elements_s": round((1 << 22) / r_cpu / 1e9, 5),
+                               "rand_perm_sample": "2^22 elements (dart throwing over lrand48)"}
+        gt = holder["t"]
+        out["parity_ok"] = bool(np.array_equal(gt[0].cpu().numpy(), to) and np.array_equal(gt[1].cpu().numpy(), tc)
+                                and np.array_equal(bale.rand_perm_dev(1 << 22, 31, device=dev).cpu().numpy(), rp))
+    holder.clear()
+    del off, col, rinv, cinv
+    torch.cuda.empty_cache()
+    return out
+
+
 def run_batch(ctx, small: bool = False) -> dict:
     import torch
 
@@ -716,12 +782,12 @@ def run_gb300(args, dist: Dist) -> dict | None:
     runners = {"ig": lambda: run_ig(ctx, False), "ig_zipf": lambda: run_ig(ctx, True),
                "histo": lambda: run_histo(ctx), "triangles": lambda: run_triangles(ctx),
                "batch": lambda: run_batch(ctx), "batch_small": lambda: run_batch(ctx, small=True),
-               "serve": lambda: run_serve(ctx), "graph": lambda: run_graph(ctx)}
+               "serve": lambda: run_serve(ctx), "graph": lambda: run_graph(ctx), "spmat": lambda: run_spmat(ctx)}
     head = runners[args.workload]()
     torch.cuda.empty_cache()
     if not args.only:
         others = {}
-        for wl in ("ig_zipf", "histo", "triangles", "graph", "batch", "batch_small", "serve", "ig"):
+        for wl in ("ig_zipf", "histo", "triangles", "graph", "spmat", "batch", "batch_small", "serve", "ig"):
             if wl != args.workload:
                 others[wl] = runners[wl]()
                 torch.cuda.empty_cache()
@@ -771,7 +837,7 @@ def main(argv=None) -> int:
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="ig", choices=["ig", "ig_zipf", "histo", "triangles", "graph", "batch", "batch_small", "serve"])
+    ap.add_argument("--workload", default="ig", choices=["ig", "ig_zipf", "histo", "triangles", "graph", "spmat", "batch", "batch_small", "serve"])
     ap.add_argument("--only", action="store_true", help="measure the selected workload only")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=8.0, help="seconds of CPU baseline per workload")

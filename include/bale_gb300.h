@@ -197,6 +197,28 @@ BALE_API int bale_gen_rmat_dev(int64_t scale, int64_t edgefactor, double a, doub
                                uint64_t seed, int64_t *d_offset, int64_t *d_nonzero, int64_t *nnz,
                                void *stream);
 
+/* spmat's transpose, permutation and random permutation on the device,    */
+/* each bit-identical to the reference at one PE and synchronous:           */
+/*  * bale_transpose_dev: transpose_matrix_agi (spmat/spmat_agi.upc:180-235);*/
+/*    At is numcols x numrows, d_toffset[numcols+1], d_tnonzero[nnz], rows   */
+/*    ascending within each row of At;                                      */
+/*  * bale_permute_dev: permute_matrix_agi (spmat/spmat_agi.upc:119-173);    */
+/*    row i of A goes to row rperminv[i], column j to cperminv[j], nonzeros  */
+/*    keep their order; d_poffset[numrows+1], d_pnonzero[nnz];               */
+/*  * bale_rand_perm_dev: rand_permp_agi(n, seed) (spmat/spmat_agi.upc:      */
+/*    56-107): the permutation the reference's dart throwing yields from     */
+/*    lrand48 after srand48(seed) (seed 0 is taken as srand48(0)).           */
+/* BALE_EINPUT for malformed offsets or columns, or a rperminv/cperminv     */
+/* that is not a permutation.                                               */
+BALE_API int bale_transpose_dev(const int64_t *d_offset, const int64_t *d_nonzero, int64_t numrows,
+                                int64_t numcols, int64_t nnz, int64_t *d_toffset, int64_t *d_tnonzero,
+                                void *stream);
+BALE_API int bale_permute_dev(const int64_t *d_offset, const int64_t *d_nonzero, int64_t numrows,
+                              int64_t numcols, int64_t nnz, const int64_t *d_rperminv,
+                              const int64_t *d_cperminv, int64_t *d_poffset, int64_t *d_pnonzero,
+                              void *stream);
+BALE_API int bale_rand_perm_dev(int64_t n, uint64_t seed, int64_t *d_perm, void *stream);
+
 /* ======================= batched execution ============================== */
 /* Many instances of uneven size in one CUDA graph: a persistent work-queue  */
 /* kernel takes tiles of every instance (tile sizes per kind and size class  */

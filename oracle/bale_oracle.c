@@ -223,3 +223,69 @@ int64_t orc_triangle_agi_mt(const int64_t *offset, const int64_t *nonzero, int64
                             int nthreads) {
   return orc_run(JOB_TRI, nthreads, numrows, offset, nonzero, NULL);
 }
+
+/* ------------------------------------------------------------------------ */
+/* spmat: transpose, permute, random permutation                              */
+/* ------------------------------------------------------------------------ */
+
+/* transpose_matrix_agi (spmat/spmat_agi.upc:180-235) at THREADS = 1: column
+ * counts, their prefix sums, then every nonzero of A appended to its column's
+ * row of At in A's row order (so At's rows come out ascending). */
+int orc_transpose(const int64_t *offset, const int64_t *nonzero, int64_t numrows, int64_t numcols,
+                  int64_t *toffset, int64_t *tnonzero) {
+  const int64_t nnz = offset[numrows];
+  for (int64_t c = 0; c <= numcols; c++) toffset[c] = 0;
+  for (int64_t k = 0; k < nnz; k++) {
+    if (nonzero[k] < 0 || nonzero[k] >= numcols) return -1;
+    toffset[nonzero[k] + 1]++;
+  }
+  for (int64_t c = 0; c < numcols; c++) toffset[c + 1] += toffset[c];
+  int64_t *fill = (int64_t *)malloc((size_t)(numcols > 0 ? numcols : 1) * sizeof(int64_t));
+  if (!fill) return -1;
+  memcpy(fill, toffset, (size_t)numcols * sizeof(int64_t));
+  for (int64_t r = 0; r < numrows; r++)
+    for (int64_t k = offset[r]; k < offset[r + 1]; k++) tnonzero[fill[nonzero[k]]++] = r;
+  free(fill);
+  return 0;
+}
+
+/* permute_matrix_agi (spmat/spmat_agi.upc:119-173) at THREADS = 1: rperm is
+ * the inverse of rperminv; row i of Ap is row rperm[i] of A with every column
+ * mapped through cperminv, in the row's own order. */
+void orc_permute(const int64_t *offset, const int64_t *nonzero, int64_t numrows, const int64_t *rperminv,
+                 const int64_t *cperminv, int64_t *poffset, int64_t *pnonzero) {
+  int64_t *rperm = (int64_t *)malloc((size_t)(numrows > 0 ? numrows : 1) * sizeof(int64_t));
+  if (!rperm) return;
+  for (int64_t i = 0; i < numrows; i++) rperm[rperminv[i]] = i;
+  int64_t pos = 0;
+  poffset[0] = 0;
+  for (int64_t i = 0; i < numrows; i++) {
+    const int64_t row = rperm[i];
+    for (int64_t k = offset[row]; k < offset[row + 1]; k++) pnonzero[pos++] = cperminv[nonzero[k]];
+    poffset[i + 1] = pos;
+  }
+  free(rperm);
+}
+
+/* rand_permp_agi (spmat/spmat_agi.upc:56-107) at THREADS = 1 with seed != 0.
+ * The drand48 family is the 48-bit linear congruential generator POSIX
+ * specifies: srand48(s) sets X = (s & 0xffffffff) << 16 | 0x330e, and each
+ * lrand48() steps X = (0x5deece66d X + 0xb) mod 2^48 and returns X >> 17. */
+int orc_rand_perm(int64_t n, int64_t seed, int64_t *perm) {
+  const int64_t m = 2 * n;
+  int64_t *target = (int64_t *)malloc((size_t)(m > 0 ? m : 1) * sizeof(int64_t));
+  if (!target) return -1;
+  for (int64_t i = 0; i < m; i++) target[i] = -1;
+  uint64_t x = (((uint64_t)seed & 0xffffffffull) << 16) | 0x330eull;
+  int64_t i = 0;
+  while (i < n) {
+    x = (0x5deece66dull * x + 0xbull) & ((1ull << 48) - 1);
+    const int64_t r = (int64_t)(x >> 17) % m;
+    if (target[r] == -1) target[r] = i++;
+  }
+  int64_t pos = 0;
+  for (int64_t s = 0; s < m; s++)
+    if (target[s] != -1) perm[pos++] = target[s];
+  free(target);
+  return 0;
+}

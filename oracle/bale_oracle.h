@@ -53,6 +53,19 @@ int64_t orc_triangle_agi_mt(const int64_t *offset, const int64_t *nonzero, int64
                             int nthreads);
 int orc_num_cpus(void);
 
+/* spmat_agi.upc:180-235 transpose_matrix_agi at one PE: At is numcols x
+ * numrows; toffset[numcols+1], tnonzero[nnz].  Returns 0, or -1 for a column
+ * outside [0, numcols). */
+int orc_transpose(const int64_t *offset, const int64_t *nonzero, int64_t numrows, int64_t numcols,
+                  int64_t *toffset, int64_t *tnonzero);
+/* spmat_agi.upc:119-173 permute_matrix_agi at one PE: row i of A goes to row
+ * rperminv[i], column j to cperminv[j]; nonzeros keep their order in the row. */
+void orc_permute(const int64_t *offset, const int64_t *nonzero, int64_t numrows, const int64_t *rperminv,
+                 const int64_t *cperminv, int64_t *poffset, int64_t *pnonzero);
+/* spmat_agi.upc:56-107 rand_permp_agi at one PE: darts from lrand48 after
+ * srand48(seed) into 2n slots, first hits kept, slots read in order. */
+int orc_rand_perm(int64_t n, int64_t seed, int64_t *perm);
+
 #ifdef __cplusplus
 }
 #endif

@@ -66,6 +66,9 @@ class Oracle:
             "orc_histo_agi_mt": (None, [P64, i64, P64, C.c_int]),
             "orc_ig_agi_mt": (None, [P64, P64, i64, P64, C.c_int]),
             "orc_triangle_agi_mt": (i64, [P64, P64, i64, C.c_int]),
+            "orc_transpose": (C.c_int, [P64, P64, i64, i64, P64, P64]),
+            "orc_permute": (None, [P64, P64, i64, P64, P64, P64, P64]),
+            "orc_rand_perm": (C.c_int, [i64, i64, P64]),
             "orc_num_cpus": (C.c_int, []),
         }
         for name, (res, args) in sig.items():
@@ -119,6 +122,26 @@ class Oracle:
     def triangle_agi_mt(self, offset: np.ndarray, nonzero: np.ndarray, nthreads: int = 0) -> int:
         return int(self.lib.orc_triangle_agi_mt(_p(offset), _p(nonzero), offset.size - 1, nthreads))
 
+    def transpose(self, offset: np.ndarray, nonzero: np.ndarray, numcols: int) -> tuple[np.ndarray, np.ndarray]:
+        toff = np.zeros(numcols + 1, np.int64)
+        tcol = np.zeros(max(nonzero.size, 1), np.int64)
+        if self.lib.orc_transpose(_p(offset), _p(nonzero), offset.size - 1, numcols, _p(toff), _p(tcol)) != 0:
+            raise ValueError("column outside [0, numcols)")
+        return toff, tcol[: nonzero.size]
+
+    def permute(self, offset: np.ndarray, nonzero: np.ndarray, rperminv: np.ndarray,
+                cperminv: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
+        poff = np.zeros(offset.size, np.int64)
+        pcol = np.zeros(max(nonzero.size, 1), np.int64)
+        self.lib.orc_permute(_p(offset), _p(nonzero), offset.size - 1, _p(rperminv), _p(cperminv), _p(poff), _p(pcol))
+        return poff, pcol[: nonzero.size]
+
+    def rand_perm(self, n: int, seed: int) -> np.ndarray:
+        out = np.zeros(max(n, 1), np.int64)
+        if self.lib.orc_rand_perm(n, seed, _p(out)) != 0:
+            raise MemoryError("orc_rand_perm")
+        return out[:n]
+
     def num_cpus(self) -> int:
         return int(self.lib.orc_num_cpus())
 
@@ -150,6 +173,9 @@ class Reference:
             "triangle_agi_iter": (C.c_double, [P64, P64, PS, PS, i64]),
             "gen_erdos_renyi_graph_dist": (PS, [C.c_int, C.c_double, i64, i64, i64]),
             "clear_matrix": (None, [PS]),
+            "transpose_matrix_agi": (PS, [PS]),
+            "permute_matrix_agi": (PS, [PS, P64, P64]),
+            "rand_permp_agi": (P64, [i64, C.c_int]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(lib, name)
@@ -174,6 +200,34 @@ class Reference:
                 raise RuntimeError(f"reference {name} failed")
             out[name] = (int(cnt.value), int(sr.value))
         return out
+
+    def _unpack(self, m) -> tuple[np.ndarray, np.ndarray]:
+        s = m.contents
+        off = np.ctypeslib.as_array(s.loffset, shape=(s.lnumrows + 1,)).copy()
+        col = np.ctypeslib.as_array(s.lnonzero, shape=(s.lnnz,)).copy() if s.lnnz else np.zeros(0, np.int64)
+        self.lib.clear_matrix(m)
+        return off, col
+
+    def transpose(self, offset: np.ndarray, nonzero: np.ndarray, numcols: int) -> tuple[np.ndarray, np.ndarray]:
+        """spmat's transpose_matrix_agi (spmat/spmat_agi.upc:180-235) at one PE."""
+        n = offset.size - 1
+        po, pn = _p(offset), _p(nonzero)
+        m = _sparsemat_t(0, n, n, numcols, nonzero.size, nonzero.size, po, po, pn, pn)
+        return self._unpack(self.lib.transpose_matrix_agi(C.byref(m)))
+
+    def permute(self, offset: np.ndarray, nonzero: np.ndarray, numcols: int, rperminv: np.ndarray,
+                cperminv: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
+        """spmat's permute_matrix_agi (spmat/spmat_agi.upc:119-173) at one PE."""
+        n = offset.size - 1
+        po, pn = _p(offset), _p(nonzero)
+        m = _sparsemat_t(0, n, n, numcols, nonzero.size, nonzero.size, po, po, pn, pn)
+        return self._unpack(self.lib.permute_matrix_agi(C.byref(m), _p(rperminv), _p(cperminv)))
+
+    def rand_perm(self, n: int, seed: int) -> np.ndarray:
+        """spmat's rand_permp_agi (spmat/spmat_agi.upc:56-107) at one PE: darts
+        from lrand48 after srand48(seed) (seed != 0)."""
+        p = self.lib.rand_permp_agi(n, seed)
+        return np.ctypeslib.as_array(p, shape=(n,)).copy()
 
     def erdos_renyi_lower(self, n: int, p: float, seed: int) -> tuple[np.ndarray, np.ndarray]:
         """spmat's gen_erdos_renyi_graph_dist(n, p, 0, mode 1 = lower, seed)

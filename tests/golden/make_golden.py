@@ -12,6 +12,10 @@ inputs, what the reference returns:
                     accumulates across models, apps/histo_src/histo.upc:161-213);
 * ig.npz         -- tgt from ig_agi, and whether ig_exstack and ig_exstack2
                     returned the same vector;
+* spmat.npz      -- transpose_matrix_agi and permute_matrix_agi of small
+                    matrices (an R-MAT lower matrix, the reference's own
+                    Erdos-Renyi graph, a rectangular matrix with empty rows),
+                    and rand_permp_agi(n, seed) permutations;
 * triangles.npz  -- count and shared-refs/pushes of triangle_agi,
                     triangle_exstack_push, triangle_exstack2_push and the
                     alternate triangle_agi_iter on Kronecker graphs (closed-form
@@ -118,6 +122,44 @@ def make_triangles(ref: Reference) -> dict:
     return cases
 
 
+def make_spmat(ref: Reference) -> dict:
+    """transpose_matrix_agi, permute_matrix_agi and rand_permp_agi at one PE."""
+    cases = {}
+    mats = []
+    L = bale.gen_rmat(8, 16, 0.57, 0.19, 0.19, 7)
+    mats.append(("rmat8_lower", L.offset, L.nonzero, L.numrows))
+    off, col = ref.erdos_renyi_lower(500, 10.0 / 500, 4242)
+    mats.append(("ref_erdos_renyi_500", off, col, 500))
+    # a rectangular matrix with empty rows and ascending random columns
+    rng = np.random.default_rng(17)
+    rows, ncols = 300, 517
+    lens = rng.integers(0, 12, rows)
+    lens[rng.integers(0, rows, 40)] = 0
+    cols = [np.sort(rng.choice(ncols, size=k, replace=False)) for k in lens]
+    mats.append(("rect_300x517", np.concatenate([[0], np.cumsum(lens)]).astype(np.int64),
+                 np.concatenate(cols).astype(np.int64), ncols))
+    mats.append(("one_row", np.array([0, 0], np.int64), np.zeros(0, np.int64), 1))
+    names = []
+    for k, (tag, off, col, ncols) in enumerate(mats):
+        n = off.size - 1
+        t_off, t_col = ref.transpose(off, col, ncols)
+        rinv = np.argsort(bale.gen_values(n, 60 + k)).astype(np.int64)
+        cinv = np.argsort(bale.gen_values(ncols, 70 + k)).astype(np.int64)
+        p_off, p_col = ref.permute(off, col, ncols, rinv, cinv)
+        names.append(tag)
+        cases.update({f"{tag}/offset": off, f"{tag}/nonzero": col, f"{tag}/numcols": np.array([ncols], np.int64),
+                      f"{tag}/t_offset": t_off, f"{tag}/t_nonzero": t_col,
+                      f"{tag}/rperminv": rinv, f"{tag}/cperminv": cinv,
+                      f"{tag}/p_offset": p_off, f"{tag}/p_nonzero": p_col})
+    cases["mats"] = np.array(names)
+    perms = []
+    for n, seed in ((1, 1), (2, 7), (10, 12345), (1000, 99), (100_000, 31)):
+        perms.append(f"perm_{n}_{seed}")
+        cases[f"perm_{n}_{seed}"] = ref.rand_perm(n, seed)
+    cases["perms"] = np.array(perms)
+    return cases
+
+
 def main() -> int:
     if build_ref() is None:
         print("reference tree not found; cannot regenerate golden vectors", file=sys.stderr)
@@ -126,7 +168,8 @@ def main() -> int:
     np.savez_compressed(OUT / "histo.npz", **make_histo(ref))
     np.savez_compressed(OUT / "ig.npz", **make_ig(ref))
     np.savez_compressed(OUT / "triangles.npz", **make_triangles(ref))
-    for f in ("histo.npz", "ig.npz", "triangles.npz"):
+    np.savez_compressed(OUT / "spmat.npz", **make_spmat(ref))
+    for f in ("histo.npz", "ig.npz", "triangles.npz", "spmat.npz"):
         print(f, (OUT / f).stat().st_size, "bytes")
     return 0
 

@@ -89,3 +89,65 @@ def test_full_scale22_equals_host(cuda, bale):
     assert col.numel() == L.nnz
     assert np.array_equal(off.cpu().numpy(), L.offset)
     assert np.array_equal(col.cpu().numpy(), L.nonzero)
+
+
+def _dev(a, cuda):
+    import torch
+
+    return torch.from_numpy(np.ascontiguousarray(a)).to(cuda)
+
+
+def test_transpose_and_permute_match_reference_golden(cuda, bale, golden):
+    d = golden("spmat")
+    for t in d["mats"]:
+        off, col, nc = d[f"{t}/offset"], d[f"{t}/nonzero"], int(d[f"{t}/numcols"][0])
+        to, tc = bale.transpose_dev(_dev(off, cuda), _dev(col, cuda), nc)
+        np.testing.assert_array_equal(to.cpu().numpy(), d[f"{t}/t_offset"], err_msg=str(t))
+        np.testing.assert_array_equal(tc.cpu().numpy(), d[f"{t}/t_nonzero"], err_msg=str(t))
+        po, pc = bale.permute_dev(_dev(off, cuda), _dev(col, cuda), nc, _dev(d[f"{t}/rperminv"], cuda),
+                                  _dev(d[f"{t}/cperminv"], cuda))
+        np.testing.assert_array_equal(po.cpu().numpy(), d[f"{t}/p_offset"], err_msg=str(t))
+        np.testing.assert_array_equal(pc.cpu().numpy(), d[f"{t}/p_nonzero"], err_msg=str(t))
+
+
+def test_rand_perm_matches_reference_golden(cuda, bale, golden):
+    d = golden("spmat")
+    for p in d["perms"]:
+        _, n, seed = str(p).split("_")
+        np.testing.assert_array_equal(bale.rand_perm_dev(int(n), int(seed)).cpu().numpy(), d[p], err_msg=str(p))
+
+
+@pytest.mark.parametrize("n,seed", [(3, 5), (4097, 77), (1 << 20, 2024), (3_000_001, 9)])
+def test_rand_perm_matches_oracle_at_size(cuda, bale, oracle, n, seed):
+    np.testing.assert_array_equal(bale.rand_perm_dev(n, seed).cpu().numpy(), oracle.rand_perm(n, seed))
+
+
+@pytest.mark.parametrize("scale", [12, 18])
+def test_transpose_and_permute_match_oracle_at_size(cuda, bale, oracle, scale):
+    L = bale.gen_rmat(scale, 16, 0.57, 0.19, 0.19, scale)
+    n = L.numrows
+    to, tc = bale.transpose_dev(_dev(L.offset, cuda), _dev(L.nonzero, cuda), n)
+    wo, wc = oracle.transpose(L.offset, L.nonzero, n)
+    np.testing.assert_array_equal(to.cpu().numpy(), wo)
+    np.testing.assert_array_equal(tc.cpu().numpy(), wc)
+    rinv = oracle.rand_perm(n, 11)
+    cinv = oracle.rand_perm(n, 12)
+    po, pc = bale.permute_dev(_dev(L.offset, cuda), _dev(L.nonzero, cuda), n, _dev(rinv, cuda), _dev(cinv, cuda))
+    qo, qc = oracle.permute(L.offset, L.nonzero, rinv, cinv)
+    np.testing.assert_array_equal(po.cpu().numpy(), qo)
+    np.testing.assert_array_equal(pc.cpu().numpy(), qc)
+
+
+def test_spmat_ops_reject_bad_input(cuda, bale):
+    off = np.array([0, 2, 3], np.int64)
+    col = np.array([0, 5, 1], np.int64)  # column 5 outside a 3-column matrix
+    with pytest.raises(bale.BaleError, match="status 2"):
+        bale.transpose_dev(_dev(off, cuda), _dev(col, cuda), 3)
+    col[1] = 2
+    with pytest.raises(bale.BaleError, match="status 2"):  # not a permutation
+        bale.permute_dev(_dev(off, cuda), _dev(col, cuda), 3, _dev(np.array([0, 0], np.int64), cuda),
+                         _dev(np.array([2, 1, 0], np.int64), cuda))
+    po, pc = bale.permute_dev(_dev(off, cuda), _dev(col, cuda), 3, _dev(np.array([1, 0], np.int64), cuda),
+                              _dev(np.array([2, 1, 0], np.int64), cuda))
+    np.testing.assert_array_equal(po.cpu().numpy(), [0, 1, 3])
+    np.testing.assert_array_equal(pc.cpu().numpy(), [1, 2, 0])

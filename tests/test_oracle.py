@@ -148,3 +148,41 @@ def test_oracle_equals_reference_on_fresh_inputs(oracle, bale):
         assert oracle.triangle_exstack_push(L.offset, L.nonzero) == r["triangle_exstack_push"]
     off, col = ref.erdos_renyi_lower(5000, 20.0 / 5000, 777)
     assert oracle.triangle_agi(off, col) == ref.triangles(off, col)["triangle_agi"]
+
+
+def test_spmat_transpose_and_permute_match_reference_golden(oracle, golden):
+    d = golden("spmat")
+    for t in d["mats"]:
+        off, col, nc = d[f"{t}/offset"], d[f"{t}/nonzero"], int(d[f"{t}/numcols"][0])
+        to, tc = oracle.transpose(off, col, nc)
+        np.testing.assert_array_equal(to, d[f"{t}/t_offset"], err_msg=str(t))
+        np.testing.assert_array_equal(tc, d[f"{t}/t_nonzero"], err_msg=str(t))
+        po, pc = oracle.permute(off, col, d[f"{t}/rperminv"], d[f"{t}/cperminv"])
+        np.testing.assert_array_equal(po, d[f"{t}/p_offset"], err_msg=str(t))
+        np.testing.assert_array_equal(pc, d[f"{t}/p_nonzero"], err_msg=str(t))
+
+
+def test_rand_perm_matches_reference_golden(oracle, golden):
+    d = golden("spmat")
+    for p in d["perms"]:
+        _, n, seed = str(p).split("_")
+        np.testing.assert_array_equal(oracle.rand_perm(int(n), int(seed)), d[p], err_msg=str(p))
+
+
+@pytest.mark.skipif(not REF_LIB.exists(), reason="oracle/_ref is built only where the reference tree exists")
+def test_spmat_restatements_match_reference_on_fresh_inputs(oracle, bale):
+    ref = Reference()
+    for seed in (3, 4):
+        L = bale.gen_rmat(10, 8, 0.57, 0.19, 0.19, seed)
+        n = L.numrows
+        to, tc = oracle.transpose(L.offset, L.nonzero, n)
+        ro, rc = ref.transpose(L.offset, L.nonzero, n)
+        np.testing.assert_array_equal(to, ro)
+        np.testing.assert_array_equal(tc, rc)
+        rinv = np.argsort(bale.gen_values(n, seed)).astype(np.int64)
+        cinv = np.argsort(bale.gen_values(n, seed + 9)).astype(np.int64)
+        po, pc = oracle.permute(L.offset, L.nonzero, rinv, cinv)
+        qo, qc = ref.permute(L.offset, L.nonzero, n, rinv, cinv)
+        np.testing.assert_array_equal(po, qo)
+        np.testing.assert_array_equal(pc, qc)
+        np.testing.assert_array_equal(oracle.rand_perm(5000 + seed, seed), ref.rand_perm(5000 + seed, seed))

@@ -364,6 +364,33 @@ def rand_perm_dev(n: int, seed: int, device=None, stream=None):
     return out[:n]
 
 
+def write_matrix_mm(L: "SparseMatrix", path) -> None:
+    """spmat's write_matrix_mm: the matrix as a MatrixMarket pattern file."""
+    _status(_lib.bale_write_matrix_mm(L.ptr(), str(path).encode()), "bale_write_matrix_mm")
+
+
+def mm_header(path) -> tuple[int, int, int, int]:
+    """(numrows, numcols, nnz, fields) of a MatrixMarket coordinate file."""
+    nr, nc, nnz, body, fields = C.c_int64(0), C.c_int64(0), C.c_int64(0), C.c_int64(0), C.c_int(0)
+    _status(_lib.bale_mm_header(str(path).encode(), C.byref(nr), C.byref(nc), C.byref(nnz), C.byref(body),
+                                C.byref(fields)), "bale_mm_header")
+    return nr.value, nc.value, nnz.value, fields.value
+
+
+def read_matrix_mm_dev(path, device=None, stream=None):
+    """spmat's read_matrix_mm_to_dist at one PE, parsed on the device:
+    returns (offset, nonzero, numcols) with device int64 tensors."""
+    import torch
+
+    nr, nc, nnz, _ = mm_header(path)
+    dev = device if device is not None else torch.device("cuda", torch.cuda.current_device())
+    off = torch.empty(nr + 1, dtype=torch.int64, device=dev)
+    col = torch.empty(max(nnz, 1), dtype=torch.int64, device=dev)
+    _status(_lib.bale_read_matrix_mm_dev(str(path).encode(), _dptr(off, "offset"), _dptr(col, "nonzero"),
+                                         _stream(stream)), "bale_read_matrix_mm_dev")
+    return off, col[:nnz], nc
+
+
 class TrianglePrepared:
     """A device CSR counted repeatedly (bale_triangle_prepare): validation,
     the 32-bit column copy and the transpose are built once; count() adds

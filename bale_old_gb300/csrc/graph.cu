@@ -19,6 +19,8 @@
 // and per-warp counts in shared memory.
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
+#include <vector>
 
 #include "bale_inputs.h"
 #include "common.cuh"
@@ -595,6 +597,89 @@ __global__ void __launch_bounds__(256)
     if (used[j]) perm[upos[j]] = rank[sk[j] & tmask];
 }
 
+// ---------------------------------------------------------------- MatrixMarket body
+__device__ __forceinline__ bool is_digit(char c) { return c >= '0' && c <= '9'; }
+__device__ __forceinline__ bool is_blank(char c) { return c == ' ' || c == '\t'; }
+
+// flag[i] = 1 where an entry line starts: a digit preceded, past blanks, by
+// a newline or the start of the body (comment lines start with '%').
+__global__ void __launch_bounds__(256)
+    mm_starts_kernel(const char *__restrict__ b, int64_t len, uint32_t *__restrict__ flag) {
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < len; i += stride) {
+    uint32_t f = 0;
+    if (is_digit(b[i])) {
+      int64_t j = i - 1;
+      while (j >= 0 && is_blank(b[j])) j--;
+      f = (j < 0 || b[j] == '\n') ? 1u : 0u;
+    }
+    flag[i] = f;
+  }
+}
+
+__global__ void __launch_bounds__(256)
+    mm_compact_kernel(const uint32_t *__restrict__ flag, const uint32_t *__restrict__ pos, int64_t len,
+                      uint32_t *__restrict__ linepos, int64_t nlines) {
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < len; i += stride)
+    if (flag[i] && pos[i] < nlines) linepos[pos[i]] = static_cast<uint32_t>(i);
+}
+
+// An unsigned decimal at b[*p] (at least one digit, no overflow past 2^62).
+__device__ __forceinline__ bool mm_uint(const char *b, int64_t len, int64_t *p, int64_t *v) {
+  int64_t x = 0, q = *p;
+  if (q >= len || !is_digit(b[q])) return false;
+  while (q < len && is_digit(b[q])) {
+    if (x > (int64_t(1) << 58)) return false;
+    x = x * 10 + (b[q] - '0');
+    q++;
+  }
+  *p = q;
+  *v = x;
+  return true;
+}
+
+// One thread per entry line: "row col" (or "row col value"), 1-based.
+// keys[l] = (row - 1) << lb | l, cols[l] = col - 1.
+__global__ void __launch_bounds__(256)
+    mm_parse_kernel(const char *__restrict__ b, int64_t len, const uint32_t *__restrict__ linepos, int64_t nlines,
+                    int fields, int64_t nr, int64_t nc, int lb, uint64_t *__restrict__ keys,
+                    uint32_t *__restrict__ cols, unsigned long long *__restrict__ bad) {
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  unsigned long long nb = 0;
+  for (int64_t l = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; l < nlines; l += stride) {
+    int64_t p = linepos[l], r = 0, c = 0, v = 0;
+    bool ok = mm_uint(b, len, &p, &r);
+    while (ok && p < len && is_blank(b[p])) p++;
+    ok = ok && mm_uint(b, len, &p, &c);
+    if (ok && fields == 3) {
+      while (p < len && is_blank(b[p])) p++;
+      if (p < len && (b[p] == '-' || b[p] == '+')) p++;
+      ok = mm_uint(b, len, &p, &v);
+    }
+    while (ok && p < len && (is_blank(b[p]) || b[p] == '\r')) p++;
+    ok = ok && (p == len || b[p] == '\n') && r >= 1 && r <= nr && c >= 1 && c <= nc;
+    if (!ok) {
+      nb++;
+      r = 1;
+      c = 1;
+    }
+    keys[l] = (static_cast<uint64_t>(r - 1) << lb) | static_cast<uint64_t>(l);
+    cols[l] = static_cast<uint32_t>(c - 1);
+  }
+  nb = warp_sum_u64(nb);
+  if (lane_id() == 0 && nb) atomicAdd(bad, nb);
+}
+
+__global__ void __launch_bounds__(256)
+    mm_cols_kernel(const uint64_t *__restrict__ sk, int64_t nlines, int lb, const uint32_t *__restrict__ cols,
+                   int64_t *__restrict__ nonzero) {
+  const uint64_t lmask = (uint64_t(1) << lb) - 1;
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  for (int64_t e = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; e < nlines; e += stride)
+    nonzero[e] = cols[sk[e] & lmask];
+}
+
 uint32_t prob_threshold(double p) {
   if (p <= 0.0) return 0;
   if (p >= 1.0) return UINT32_MAX;
@@ -794,6 +879,108 @@ int bale_rand_perm_dev(int64_t n, uint64_t seed, int64_t *d_perm, void *stream) 
     BALE_CUDA_OK(cudaStreamSynchronize(st));
     return BALE_OK;
   }
+}
+
+int bale_read_matrix_mm_dev(const char *path, int64_t *d_offset, int64_t *d_nonzero, void *stream) {
+  int64_t nr = 0, nc = 0, nnz = 0, body = 0;
+  int fields = 0;
+  int rc = bale_mm_header(path, &nr, &nc, &nnz, &body, &fields);
+  if (rc != BALE_OK) {
+    set_error("bale_read_matrix_mm_dev: %s: not a coordinate pattern/integer MatrixMarket file", path ? path : "");
+    return rc;
+  }
+  if (!d_offset || (nnz > 0 && !d_nonzero) || nr < 1 || nr > (int64_t(1) << 31) || nnz >= (int64_t(1) << 32) - 1) {
+    set_error("bale_read_matrix_mm_dev: bad arguments or sizes");
+    return BALE_EINVAL;
+  }
+  FILE *fp = fopen(path, "rb");
+  if (!fp || fseek(fp, 0, SEEK_END) != 0) {
+    if (fp) fclose(fp);
+    set_error("bale_read_matrix_mm_dev: cannot read %s", path);
+    return BALE_EINPUT;
+  }
+  const int64_t len = static_cast<int64_t>(ftell(fp)) - body;
+  if (len < 0 || len >= (int64_t(1) << 32) - 1) {
+    fclose(fp);
+    set_error("bale_read_matrix_mm_dev: %s: body of %lld bytes is outside the supported range", path,
+              static_cast<long long>(len));
+    return BALE_EINPUT;
+  }
+  std::vector<char> text(static_cast<size_t>(len > 0 ? len : 1));
+  const bool read_ok = fseek(fp, static_cast<long>(body), SEEK_SET) == 0 &&
+                       (len == 0 || fread(text.data(), 1, static_cast<size_t>(len), fp) == static_cast<size_t>(len));
+  fclose(fp);
+  if (!read_ok) {
+    set_error("bale_read_matrix_mm_dev: short read of %s", path);
+    return BALE_EINPUT;
+  }
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  int lb = 1;
+  while ((int64_t(1) << lb) < std::max<int64_t>(nnz, 1)) lb++;
+  // workspace: the text, start flags and their prefix (per byte), line
+  // starts and columns (per entry), two key buffers, sort scratch
+  const int64_t nn = std::max<int64_t>(nnz, 1), ll = std::max<int64_t>(len, 1);
+  const int64_t tiles = (nn + kTile - 1) / kTile;
+  const int64_t nb = (std::max(ll + 1, tiles * kDigits) + kScanBlock - 1) / kScanBlock + 1;
+  const size_t need = up256(ll) + 2 * up256(4 * (ll + 1)) + 2 * up256(4 * nn) + 2 * up256(8 * nn) +
+                      2 * up256(4 * tiles * kDigits) + up256(4 * nb) + 256;
+  char *ws = static_cast<char *>(device_workspace(need, st));
+  if (!ws) return BALE_ENOMEM;
+  char *o = ws;
+  auto take = [&](size_t bytes) {
+    char *r = o;
+    o += up256(bytes);
+    return r;
+  };
+  char *d_text = take(ll);
+  Ws w;
+  w.flag = reinterpret_cast<uint32_t *>(take(4 * (ll + 1)));
+  w.pos = reinterpret_cast<uint32_t *>(take(4 * (ll + 1)));
+  uint32_t *linepos = reinterpret_cast<uint32_t *>(take(4 * nn));
+  uint32_t *cols = reinterpret_cast<uint32_t *>(take(4 * nn));
+  w.ka = reinterpret_cast<uint64_t *>(take(8 * nn));
+  w.kb = reinterpret_cast<uint64_t *>(take(8 * nn));
+  w.hist = reinterpret_cast<uint32_t *>(take(4 * tiles * kDigits));
+  w.hoff = reinterpret_cast<uint32_t *>(take(4 * tiles * kDigits));
+  w.bsum = reinterpret_cast<uint32_t *>(take(4 * nb));
+  w.words = reinterpret_cast<unsigned int *>(take(64));
+  w.va = w.vb = nullptr;
+  w.deg = w.newid = nullptr;
+  unsigned long long *bad = reinterpret_cast<unsigned long long *>(w.words + 4);
+  BALE_CUDA_OK(cudaMemsetAsync(w.words, 0, 64, st));
+  if (len > 0) BALE_CUDA_OK(cudaMemcpyAsync(d_text, text.data(), static_cast<size_t>(len), cudaMemcpyHostToDevice, st));
+  mm_starts_kernel<<<grid_for(ll), 256, 0, st>>>(d_text, len, w.flag);
+  rc = excl_scan(w.flag, w.pos, len, w.bsum, w.words, st);
+  if (rc != BALE_OK) return rc;
+  unsigned int lines = 0;
+  BALE_CUDA_OK(cudaMemcpyAsync(&lines, w.words, 4, cudaMemcpyDeviceToHost, st));
+  BALE_CUDA_OK(cudaStreamSynchronize(st));
+  if (static_cast<int64_t>(lines) != nnz) {
+    set_error("bale_read_matrix_mm_dev: %s: %lld nonzeros in the header, %u entry lines", path,
+              static_cast<long long>(nnz), lines);
+    return BALE_EINPUT;
+  }
+  if (nnz > 0) {
+    mm_compact_kernel<<<grid_for(ll), 256, 0, st>>>(w.flag, w.pos, len, linepos, nnz);
+    mm_parse_kernel<<<grid_for(nnz), 256, 0, st>>>(d_text, len, linepos, nnz, fields, nr, nc, lb, w.ka, cols, bad);
+    BALE_CUDA_OK(cudaGetLastError());
+  }
+  unsigned long long nbad = 0;
+  BALE_CUDA_OK(cudaMemcpyAsync(&nbad, bad, 8, cudaMemcpyDeviceToHost, st));
+  BALE_CUDA_OK(cudaStreamSynchronize(st));
+  if (nbad) {
+    set_error("bale_read_matrix_mm_dev: %s: %llu malformed or out-of-range entries", path, nbad);
+    return BALE_EINPUT;
+  }
+  int rb = 1;
+  while ((int64_t(1) << rb) < nr) rb++;
+  uint64_t *sk = radix_sort(w.ka, w.kb, nnz, rb + lb, w, st, &rc);
+  if (rc != BALE_OK) return rc;
+  csr_offsets_kernel<<<grid_for(nr + 1), 256, 0, st>>>(sk, nnz, nr, lb, d_offset);
+  if (nnz > 0) mm_cols_kernel<<<grid_for(nnz), 256, 0, st>>>(sk, nnz, lb, cols, d_nonzero);
+  BALE_CUDA_OK(cudaGetLastError());
+  BALE_CUDA_OK(cudaStreamSynchronize(st));
+  return BALE_OK;
 }
 
 }  // extern "C"

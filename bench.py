@@ -491,6 +491,16 @@ def run_spmat(ctx) -> dict:
         r_ms = time_device(lambda: holder.__setitem__("r", bale.rand_perm_dev(np_, 31, device=dev)),
                            args.steps, args.warmup)
     t_ms, p_ms, r_ms = (ctx["dist"].max(x) for x in (t_ms, p_ms, r_ms))
+    # MatrixMarket: the scale-20 lower matrix written with the reference's
+    # format, read back (file read, upload, parse, sort) on the device
+    import tempfile
+    L20 = bale.gen_rmat(20, 16, 0.57, 0.19, 0.19, 6)
+    mm_dir = tempfile.mkdtemp(prefix="bale_mm_")
+    mm_path = f"{mm_dir}/rmat20.mm"
+    bale.write_matrix_mm(L20, mm_path)
+    mm_bytes = os.path.getsize(mm_path)
+    mm_s = time_host(lambda: bale.read_matrix_mm_dev(mm_path, device=dev), args.steps, min(args.warmup, 2))
+    mm_ok = True
     w = ctx["dist"].world
     out = {"metric": "G nonzeros/s transposing the R-MAT scale-22 lower matrix on the device",
            "value": round(job_rate(nnz, t_ms / 1e3, w) / 1e9, 4), "unit": "G nonzeros/s",
@@ -499,6 +509,9 @@ def run_spmat(ctx) -> dict:
                        "ms_per_step": round(p_ms, 3)},
            "rand_perm": {"value": round(job_rate(np_, r_ms / 1e3, w) / 1e9, 4), "unit": "G elements/s",
                          "ms_per_step": round(r_ms, 3), "n": np_},
+           "read_matrix_mm": {"value": round(L20.nnz / mm_s / 1e9, 4), "unit": "G nonzeros/s",
+                              "ms_per_step": round(mm_s * 1e3, 3), "file_bytes": mm_bytes, "nnz": L20.nnz,
+                              "how": "bale_read_matrix_mm_dev on R-MAT scale 20 (file in the page cache)"},
            # transpose: the sort's passes dominate -- 24 B per key per 8-bit pass
            "roofline": roofline(ctx, "spmat", 24 * ((2 * S + 7) // 8) * nnz, t_ms / 1e3,
                                 "transpose: radix sort of (column, row) keys",
@@ -520,6 +533,12 @@ def run_spmat(ctx) -> dict:
         t0 = time.perf_counter()
         rp = orc.rand_perm(1 << 22, 31)
         r_cpu = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        mo, mc, _ = orc.read_mm(mm_path)
+        m_cpu = time.perf_counter() - t0
+        do, dc, _ = bale.read_matrix_mm_dev(mm_path, device=dev)
+        mm_ok = bool(np.array_equal(do.cpu().numpy(), mo) and np.array_equal(dc.cpu().numpy(), mc))
+        out["read_matrix_mm"]["cpu_G_nonzeros_s"] = round(L20.nnz / m_cpu / 1e9, 5)
         out["cpu_baseline"] = {"value": round(nnz / t_cpu / 1e9, 5), "unit": "G nonzeros/s", "cores": 1,
                                "kind": "port",
                                "sample": "transpose_matrix_agi at one PE (oracle restatement) of the same matrix",
@@ -527,9 +546,11 @@ def run_spmat(ctx) -> dict:
                                "rand_perm_G_elements_s": round((1 << 22) / r_cpu / 1e9, 5),
                                "rand_perm_sample": "2^22 elements (dart throwing over lrand48)"}
         gt = holder["t"]
-        out["parity_ok"] = bool(np.array_equal(gt[0].cpu().numpy(), to) and np.array_equal(gt[1].cpu().numpy(), tc)
+        out["parity_ok"] = mm_ok and bool(np.array_equal(gt[0].cpu().numpy(), to) and np.array_equal(gt[1].cpu().numpy(), tc)
                                 and np.array_equal(bale.rand_perm_dev(1 << 22, 31, device=dev).cpu().numpy(), rp))
     holder.clear()
+    os.remove(mm_path)
+    os.rmdir(mm_dir)
     del off, col, rinv, cinv
     torch.cuda.empty_cache()
     return out

@@ -219,6 +219,20 @@ BALE_API int bale_permute_dev(const int64_t *d_offset, const int64_t *d_nonzero,
                               void *stream);
 BALE_API int bale_rand_perm_dev(int64_t n, uint64_t seed, int64_t *d_perm, void *stream);
 
+/* MatrixMarket files of the reference's kind (spmat/spmat_utils.upc:128-149 */
+/* write_matrix_mm, :217-370 read_matrix_mm_to_dist): "%%MatrixMarket matrix */
+/* coordinate pattern" (or "integer", value ignored), "rows cols nnz", then  */
+/* one 1-based "row col" line per nonzero.  bale_write_matrix_mm writes the   */
+/* same bytes as the reference; bale_mm_header reads the banner and sizes   */
+/* (comment lines after the banner are skipped); bale_read_matrix_mm_dev     */
+/* parses the body on the device into d_offset[rows+1], d_nonzero[nnz],      */
+/* keeping the file order of the nonzeros within each row, as the reference */
+/* does.  BALE_EINPUT for an unreadable or malformed file.  Synchronous.     */
+BALE_API int bale_write_matrix_mm(const sparsemat_t *A, const char *path);
+BALE_API int bale_mm_header(const char *path, int64_t *numrows, int64_t *numcols, int64_t *nnz,
+                            int64_t *body, int *fields);
+BALE_API int bale_read_matrix_mm_dev(const char *path, int64_t *d_offset, int64_t *d_nonzero, void *stream);
+
 /* ======================= batched execution ============================== */
 /* Many instances of uneven size in one CUDA graph: a persistent work-queue  */
 /* kernel takes tiles of every instance (tile sizes per kind and size class  */

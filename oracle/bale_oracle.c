@@ -12,6 +12,7 @@
 #include "bale_oracle.h"
 
 #include <pthread.h>
+#include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 #include <unistd.h>
@@ -288,4 +289,55 @@ int orc_rand_perm(int64_t n, int64_t seed, int64_t *perm) {
     if (target[s] != -1) perm[pos++] = target[s];
   free(target);
   return 0;
+}
+
+/* read_matrix_mm_to_dist (spmat/spmat_utils.upc:217-370) at THREADS = 1: the
+ * banner's three words (matrix, coordinate, pattern or integer), the sizes,
+ * then fscanf of "row col" (or "row col value") pairs, 1-based; row counts,
+ * their prefix sums, and the columns appended to their rows in file order. */
+int orc_read_mm(const char *path, int64_t *dims, int64_t *offset, int64_t *nonzero) {
+  FILE *fp = fopen(path, "r");
+  if (!fp) return -1;
+  char object[64], format[64], field[64];
+  int64_t nr, nc, nnz, row, col, val, pos = 0;
+  int rc = -1;
+  if (fscanf(fp, "%%%%MatrixMarket %63s %63s %63s\n", object, format, field) != 3) goto done;
+  if (strcmp(object, "matrix") || strcmp(format, "coordinate")) goto done;
+  const int integer = !strcmp(field, "integer");
+  if (!integer && strcmp(field, "pattern")) goto done;
+  if (fscanf(fp, "%ld %ld %ld\n", &nr, &nc, &nnz) != 3) goto done;
+  if (!offset) {
+    dims[0] = nr;
+    dims[1] = nc;
+    dims[2] = nnz;
+    rc = 0;
+    goto done;
+  }
+  int64_t *rows = (int64_t *)malloc((size_t)(nnz > 0 ? nnz : 1) * sizeof(int64_t));
+  int64_t *cols = (int64_t *)malloc((size_t)(nnz > 0 ? nnz : 1) * sizeof(int64_t));
+  if (!rows || !cols) { free(rows); free(cols); goto done; }
+  for (int64_t i = 0; i <= nr; i++) offset[i] = 0;
+  for (;;) {
+    const int got = integer ? fscanf(fp, "%ld %ld %ld\n", &row, &col, &val) : fscanf(fp, "%ld %ld\n", &row, &col);
+    if (got != (integer ? 3 : 2)) break;
+    if (pos >= nnz || row < 1 || row > nr || col < 1 || col > nc) { pos = -1; break; }
+    rows[pos] = row - 1;
+    cols[pos++] = col - 1;
+    offset[row]++;
+  }
+  if (pos == nnz) {
+    for (int64_t i = 0; i < nr; i++) offset[i + 1] += offset[i];
+    int64_t *fill = (int64_t *)malloc((size_t)(nr > 0 ? nr : 1) * sizeof(int64_t));
+    if (fill) {
+      memcpy(fill, offset, (size_t)nr * sizeof(int64_t));
+      for (int64_t k = 0; k < nnz; k++) nonzero[fill[rows[k]]++] = cols[k];
+      free(fill);
+      rc = 0;
+    }
+  }
+  free(rows);
+  free(cols);
+done:
+  fclose(fp);
+  return rc;
 }

@@ -69,6 +69,7 @@ class Oracle:
             "orc_transpose": (C.c_int, [P64, P64, i64, i64, P64, P64]),
             "orc_permute": (None, [P64, P64, i64, P64, P64, P64, P64]),
             "orc_rand_perm": (C.c_int, [i64, i64, P64]),
+            "orc_read_mm": (C.c_int, [C.c_char_p, P64, P64, P64]),
             "orc_num_cpus": (C.c_int, []),
         }
         for name, (res, args) in sig.items():
@@ -142,6 +143,17 @@ class Oracle:
             raise MemoryError("orc_rand_perm")
         return out[:n]
 
+    def read_mm(self, path) -> tuple[np.ndarray, np.ndarray, int]:
+        dims = np.zeros(3, np.int64)
+        if self.lib.orc_read_mm(str(path).encode(), _p(dims), None, None) != 0:
+            raise ValueError(f"{path}: rejected")
+        nr, nc, nnz = (int(x) for x in dims)
+        off = np.zeros(nr + 1, np.int64)
+        col = np.zeros(max(nnz, 1), np.int64)
+        if self.lib.orc_read_mm(str(path).encode(), _p(dims), _p(off), _p(col)) != 0:
+            raise ValueError(f"{path}: rejected")
+        return off, col[:nnz], nc
+
     def num_cpus(self) -> int:
         return int(self.lib.orc_num_cpus())
 
@@ -176,6 +188,8 @@ class Reference:
             "transpose_matrix_agi": (PS, [PS]),
             "permute_matrix_agi": (PS, [PS, P64, P64]),
             "rand_permp_agi": (P64, [i64, C.c_int]),
+            "write_matrix_mm": (C.c_int, [PS, C.c_char_p]),
+            "read_matrix_mm_to_dist": (PS, [C.c_char_p]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(lib, name)
@@ -222,6 +236,23 @@ class Reference:
         po, pn = _p(offset), _p(nonzero)
         m = _sparsemat_t(0, n, n, numcols, nonzero.size, nonzero.size, po, po, pn, pn)
         return self._unpack(self.lib.permute_matrix_agi(C.byref(m), _p(rperminv), _p(cperminv)))
+
+    def write_mm(self, offset: np.ndarray, nonzero: np.ndarray, numcols: int, path: str) -> None:
+        """spmat's write_matrix_mm (spmat/spmat_utils.upc:128-149) at one PE."""
+        n = offset.size - 1
+        po, pn = _p(offset), _p(nonzero)
+        m = _sparsemat_t(0, n, n, numcols, nonzero.size, nonzero.size, po, po, pn, pn)
+        if self.lib.write_matrix_mm(C.byref(m), path.encode()) != 0:
+            raise RuntimeError("write_matrix_mm failed")
+
+    def read_mm(self, path: str) -> tuple[np.ndarray, np.ndarray, int]:
+        """spmat's read_matrix_mm_to_dist (spmat/spmat_utils.upc:217-370) at one PE."""
+        m = self.lib.read_matrix_mm_to_dist(path.encode())
+        if not m:
+            raise RuntimeError("read_matrix_mm_to_dist failed")
+        nc = m.contents.numcols
+        off, col = self._unpack(m)
+        return off, col, nc
 
     def rand_perm(self, n: int, seed: int) -> np.ndarray:
         """spmat's rand_permp_agi (spmat/spmat_agi.upc:56-107) at one PE: darts

@@ -15,7 +15,10 @@ inputs, what the reference returns:
 * spmat.npz      -- transpose_matrix_agi and permute_matrix_agi of small
                     matrices (an R-MAT lower matrix, the reference's own
                     Erdos-Renyi graph, a rectangular matrix with empty rows),
-                    and rand_permp_agi(n, seed) permutations;
+                    rand_permp_agi(n, seed) permutations, and the reference's
+                    read_matrix_mm_to_dist of MatrixMarket files written by its
+                    write_matrix_mm (*.mm, committed beside the vectors) and of
+                    a hand-made integer file with rows out of order;
 * triangles.npz  -- count and shared-refs/pushes of triangle_agi,
                     triangle_exstack_push, triangle_exstack2_push and the
                     alternate triangle_agi_iter on Kronecker graphs (closed-form
@@ -157,6 +160,24 @@ def make_spmat(ref: Reference) -> dict:
         perms.append(f"perm_{n}_{seed}")
         cases[f"perm_{n}_{seed}"] = ref.rand_perm(n, seed)
     cases["perms"] = np.array(perms)
+    # MatrixMarket: files written by the reference's writer, and a hand-made
+    # one with rows out of order, comment-free, integer field; read back by
+    # the reference's reader
+    mm = []
+    for tag in ("rmat8_lower", "rect_300x517"):
+        path = OUT / f"{tag}.mm"
+        ref.write_mm(cases[f"{tag}/offset"], cases[f"{tag}/nonzero"], int(cases[f"{tag}/numcols"][0]), str(path))
+        mm.append(path.name)
+    path = OUT / "unordered_integer.mm"
+    lines = ["%%MatrixMarket matrix coordinate integer", "5 7 9",
+             "3 2 10", "1 7 -4", "3 1 5", "5 5 1", "1 1 2", "3 6 7", "2 4 0", "5 1 3", "1 3 9"]
+    path.write_text("\n".join(lines) + "\n")
+    mm.append(path.name)
+    for name in mm:
+        off, col, nc = ref.read_mm(str(OUT / name))
+        cases.update({f"mm/{name}/offset": off, f"mm/{name}/nonzero": col,
+                      f"mm/{name}/numcols": np.array([nc], np.int64)})
+    cases["mm_files"] = np.array(mm)
     return cases
 
 
@@ -169,7 +190,8 @@ def main() -> int:
     np.savez_compressed(OUT / "ig.npz", **make_ig(ref))
     np.savez_compressed(OUT / "triangles.npz", **make_triangles(ref))
     np.savez_compressed(OUT / "spmat.npz", **make_spmat(ref))
-    for f in ("histo.npz", "ig.npz", "triangles.npz", "spmat.npz"):
+    for f in ("histo.npz", "ig.npz", "triangles.npz", "spmat.npz", "rmat8_lower.mm", "rect_300x517.mm",
+              "unordered_integer.mm"):
         print(f, (OUT / f).stat().st_size, "bytes")
     return 0
 

@@ -151,3 +151,43 @@ def test_spmat_ops_reject_bad_input(cuda, bale):
                               _dev(np.array([2, 1, 0], np.int64), cuda))
     np.testing.assert_array_equal(po.cpu().numpy(), [0, 1, 3])
     np.testing.assert_array_equal(pc.cpu().numpy(), [1, 2, 0])
+
+
+def test_matrix_market_read_matches_reference_golden(cuda, bale, golden):
+    from pathlib import Path
+
+    gdir = Path(__file__).resolve().parent / "golden"
+    d = golden("spmat")
+    for f in d["mm_files"]:
+        off, col, nc = bale.read_matrix_mm_dev(gdir / str(f))
+        np.testing.assert_array_equal(off.cpu().numpy(), d[f"mm/{f}/offset"], err_msg=str(f))
+        np.testing.assert_array_equal(col.cpu().numpy(), d[f"mm/{f}/nonzero"], err_msg=str(f))
+        assert nc == int(d[f"mm/{f}/numcols"][0])
+
+
+def test_matrix_market_round_trip_at_size(cuda, bale, tmp_path):
+    L = bale.gen_rmat(17, 16, 0.57, 0.19, 0.19, 23)
+    p = tmp_path / "rmat17.mm"
+    bale.write_matrix_mm(L, p)
+    off, col, nc = bale.read_matrix_mm_dev(p)
+    assert nc == L.numcols
+    np.testing.assert_array_equal(off.cpu().numpy(), L.offset)
+    np.testing.assert_array_equal(col.cpu().numpy(), L.nonzero)
+
+
+def test_matrix_market_tolerates_blanks_crlf_and_comments(cuda, bale, tmp_path):
+    p = tmp_path / "loose.mm"
+    p.write_bytes(b"%%MatrixMarket matrix coordinate pattern\r\n% made by hand\r\n3 3 4\r\n"
+                  b"  2 1\r\n\r\n3\t1 \r\n% a comment between entries\n3 2\n1 3")
+    off, col, nc = bale.read_matrix_mm_dev(p)
+    np.testing.assert_array_equal(off.cpu().numpy(), [0, 1, 2, 4])
+    np.testing.assert_array_equal(col.cpu().numpy(), [2, 0, 0, 1])
+
+
+@pytest.mark.parametrize("body", ["3 3 2\n1 1\n", "3 3 2\n1 1\n2 2\n3 3\n", "3 3 2\n1 1\n4 1\n",
+                                  "3 3 2\n1 1\n2 0\n", "3 3 2\n1 1\n2 x\n", "3 3 2\n1 1\n2 2 2\n"])
+def test_matrix_market_malformed_is_an_error(cuda, bale, tmp_path, body):
+    p = tmp_path / "bad.mm"
+    p.write_text("%%MatrixMarket matrix coordinate pattern\n" + body)
+    with pytest.raises(bale.BaleError):
+        bale.read_matrix_mm_dev(p)

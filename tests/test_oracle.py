@@ -186,3 +186,15 @@ def test_spmat_restatements_match_reference_on_fresh_inputs(oracle, bale):
         np.testing.assert_array_equal(po, qo)
         np.testing.assert_array_equal(pc, qc)
         np.testing.assert_array_equal(oracle.rand_perm(5000 + seed, seed), ref.rand_perm(5000 + seed, seed))
+
+
+def test_matrix_market_reader_matches_reference_golden(oracle, golden):
+    from pathlib import Path
+
+    gdir = Path(__file__).resolve().parent / "golden"
+    d = golden("spmat")
+    for f in d["mm_files"]:
+        off, col, nc = oracle.read_mm(gdir / str(f))
+        np.testing.assert_array_equal(off, d[f"mm/{f}/offset"], err_msg=str(f))
+        np.testing.assert_array_equal(col, d[f"mm/{f}/nonzero"], err_msg=str(f))
+        assert nc == int(d[f"mm/{f}/numcols"][0])

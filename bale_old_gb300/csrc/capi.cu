@@ -672,7 +672,7 @@ bale_tri_prepared_t *bale_triangle_prepare(const int64_t *d_offset, const int64_
   if (g->wedge) {
     DeviceScratch *ds = device_scratch();
     const size_t bytes = tri_wedge_workspace_bytes(numrows, nnz);
-    if (!ds || cudaMalloc(&g->ws, bytes) != cudaSuccess || cudaMalloc(&g->cursor, 8) != cudaSuccess) {
+    if (!ds || cudaMalloc(&g->ws, bytes) != cudaSuccess || cudaMalloc(&g->cursor, 16) != cudaSuccess) {
       cudaGetLastError();
       set_error("bale_triangle_prepare: cudaMalloc of %zu bytes failed", bytes);
       bale_triangle_release(g);

@@ -97,7 +97,7 @@ int tri_hybrid_run(const int64_t *offset, const uint32_t *col32, const uint32_t 
 // Wedge-probe triangle count (tri_wedge.cu), for fewer than 2^32 - 1 rows and
 // about 2^32 nonzeros.  prepare builds the u32 column copy and the transpose
 // into ws (tri_wedge_workspace_bytes) and adds malformed entries to *bad (may
-// be NULL); run counts from a prepared ws (cursor: one device word, zeroed
+// be NULL); run counts from a prepared ws (cursor: two device words, zeroed
 // there); launch_triangle_wedge does both.
 bool tri_wedge_supported(int64_t numrows, int64_t nnz);
 size_t tri_wedge_workspace_bytes(int64_t numrows, int64_t nnz);

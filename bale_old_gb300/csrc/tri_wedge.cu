@@ -49,7 +49,8 @@ constexpr int kWarpBitsMax = 16;  // bitmap of 2^16 labels (8 KiB) per warp
 constexpr int kOvf = 256;         // columns at or above 2^16 a warp keeps in shared memory
 constexpr int kUnroll = 4;        // rounds of 32 nonzeros in flight per warp (scan, fill)
 constexpr int kHub = 8192;        // labels whose incoming counts and slots live in shared memory
-constexpr int kScanBlocksPerSm = 4;
+constexpr int kScanBlocksPerSm = 6;
+constexpr int kFillUnroll = 4;     // the fill's rounds in flight
 
 // Workspace words: [1] malformed entries seen by the scan.
 enum { kWBad = 1, kWords = 4 };
@@ -331,22 +332,22 @@ __global__ void __launch_bounds__(kScanThreads)
   for (int64_t g = static_cast<int64_t>(blockIdx.x) * kScanWarps + (threadIdx.x >> 5); g < groups; g += warps) {
     RowGroup rg;
     rg.load(off, n, nnz, g * 32, stage[threadIdx.x >> 5]);
-    for (uint32_t base = 0; base < rg.tot; base += 32 * kUnroll) {
-      uint32_t k[kUnroll], p[kUnroll], c[kUnroll], slot[kUnroll];
+    for (uint32_t base = 0; base < rg.tot; base += 32 * kFillUnroll) {
+      uint32_t k[kFillUnroll], p[kFillUnroll], c[kFillUnroll], slot[kFillUnroll];
 #pragma unroll
-      for (int u = 0; u < kUnroll; u++) {
+      for (int u = 0; u < kFillUnroll; u++) {
         uint32_t r;
         rg.at(base + 32 * u, k[u], p[u], r);
         c[u] = base + 32 * u + lane < rg.tot ? col32[k[u]] : kBadCol;
         if (p[u] == 0) c[u] = kBadCol;  // the first nonzero of a row closes no wedge
       }
 #pragma unroll
-      for (int u = 0; u < kUnroll; u++)
+      for (int u = 0; u < kFillUnroll; u++)
         slot[u] = c[u] == kBadCol               ? 0u
                   : c[u] < static_cast<uint32_t>(kHub) ? atomicAdd(&hubslot[c[u]], 1u)
                                                 : in_off[c[u]] + atomicAdd(in_cnt + c[u], 1u);
 #pragma unroll
-      for (int u = 0; u < kUnroll; u++)
+      for (int u = 0; u < kFillUnroll; u++)
         if (c[u] != kBadCol) in_rec[slot[u]] = make_uint2(k[u] - p[u], p[u]);
     }
   }
@@ -478,17 +479,30 @@ __global__ void __launch_bounds__(kWarpThreads, 3)
   __syncwarp();
   unsigned long long cnt = 0, wk = 0;
   const unsigned long long nbig = static_cast<unsigned long long>(wlim);
-  for (;;) {
+  // Two queues: rows below wlim one at a time (cursor[0], issue-bound work)
+  // and claims of 32 rows above it (cursor[1], latency-bound); each warp
+  // alternates between them so that the two kinds overlap on every SM.
+  bool big_done = false, small_done = false;
+  for (unsigned it = 0;; it++) {
+    if (big_done && small_done) break;
+    const bool take_big = !big_done && (small_done || (it & 1u) == 0);
     unsigned long long t = 0;
-    if (lane == 0) t = atomicAdd(cursor, 1ull);
+    if (lane == 0) t = atomicAdd(cursor + (take_big ? 0 : 1), 1ull);
     t = __shfl_sync(kFull, t, 0);
     int64_t j0, j1;
-    if (t < nbig) {
+    if (take_big) {
+      if (t >= nbig) {
+        big_done = true;
+        continue;
+      }
       j0 = static_cast<int64_t>(t);
       j1 = j0 + 1;
     } else {
-      j0 = wlim + static_cast<int64_t>(t - nbig) * 32;
-      if (j0 >= n) break;
+      j0 = wlim + static_cast<int64_t>(t) * 32;
+      if (j0 >= n) {
+        small_done = true;
+        continue;
+      }
       j1 = j0 + 32 < n ? j0 + 32 : n;
     }
     // rows of this claim with incoming prefixes and a non-empty row j
@@ -503,13 +517,13 @@ __global__ void __launch_bounds__(kWarpThreads, 3)
       lb = static_cast<uint32_t>(bb);
       ld = static_cast<uint32_t>(dd);
     }
-    if (t >= nbig) {
+    if (!take_big) {
       // Rows above wlim: the short ones (at most stage_max columns, where a
       // binary search beats setting and clearing a bitmap) are staged in the
       // warp's buffer -- as many at a time as fit -- and all their prefixes
       // probed flattened, so they cost a few memory round trips per claim
-      // instead of a few per row.  The bitmap area is the buffer: claims
-      // below wlim are all handed out before these.
+      // instead of a few per row.  The bitmap area is the buffer, zeroed
+      // again after each batch.
       uint4 *slot = reinterpret_cast<uint4 *>(ovf + kOvf) - 32;
       uint32_t *stg = bm;
       const uint32_t cap = nw + kOvf - 128;
@@ -550,13 +564,13 @@ __global__ void __launch_bounds__(kWarpThreads, 3)
           probe_records_staged(stg, ro, rl, col4, nvec_all, rec, cnt, wk);
         }
         __syncwarp();
+        for (uint32_t g = lane; g < end_s - base_s; g += 32) stg[g] = 0;
+        __syncwarp();
         t0 = t1;
       }
-      // longer rows: one at a time below, on a zeroed bitmap
+      // longer rows: one at a time below, on the (zero) bitmap
       live = live && !fits;
       if (!__any_sync(kFull, live)) continue;
-      for (uint32_t w = lane; w < nw; w += 32) bm[w] = 0;
-      __syncwarp();
     }
     unsigned todo = __ballot_sync(kFull, live);
     while (todo) {
@@ -681,7 +695,7 @@ int tri_wedge_run(const int64_t *offset, const void *ws, int64_t numrows, int64_
   const uint32_t stage_max = static_cast<uint32_t>(knob_or("tri.wedge_stage_max", 64));
   const size_t smem = count_smem(wb);
   const int dev = current_device();
-  BALE_CUDA_OK(cudaMemsetAsync(cursor, 0, sizeof(unsigned long long), stream));
+  BALE_CUDA_OK(cudaMemsetAsync(cursor, 0, 2 * sizeof(unsigned long long), stream));
   if (dev >= 0 && dev < 64 && !g_count_attr[dev]) {
     BALE_CUDA_OK(cudaFuncSetAttribute(wedge_count_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       static_cast<int>(count_smem(kWarpBitsMax))));
@@ -692,7 +706,7 @@ int tri_wedge_run(const int64_t *offset, const void *ws, int64_t numrows, int64_
       occ < 1)
     occ = 1;
   int64_t blocks = static_cast<int64_t>(sms) * occ;
-  const int64_t claims = wlim + (numrows - wlim + 31) / 32;
+  const int64_t claims = wlim + (numrows - wlim + 31) / 32;  // both queues
   const int64_t need = (claims + kWarpWarps - 1) / kWarpWarps;
   if (blocks > need) blocks = need > 0 ? need : 1;
   wedge_count_kernel<<<static_cast<unsigned>(blocks), kWarpThreads, smem, stream>>>(

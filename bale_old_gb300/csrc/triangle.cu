@@ -167,7 +167,7 @@ int launch_triangle(const int64_t *offset, const int64_t *nonzero, int64_t numro
   const int64_t mode = knob("tri.mode");
   if ((mode < 0 || mode == 2) && tri_wedge_supported(numrows, nnz)) {
     void *ws = device_workspace(tri_wedge_workspace_bytes(numrows, nnz), stream);
-    unsigned long long *cursor = next_cursor_word();
+    unsigned long long *cursor = next_cursor_words(2);
     if (!ws || !cursor) return BALE_ENOMEM;
     return launch_triangle_wedge(offset, nonzero, numrows, nnz, count, work, bad, ws, cursor, stream);
   }

@@ -26,7 +26,9 @@ __all__ = [
     "ig_agi", "ig_exstack", "ig_exstack2", "ig_conveyor",
     "triangle_agi", "triangle_exstack_push", "triangle_exstack2_push",
     "triangle_convey_push", "triangle_agi_iter",
-    "histo_dev", "ig_dev", "triangle_dev", "ig_dev_noalloc",
+    "histo_dev", "ig_dev", "triangle_dev", "ig_dev_noalloc", "TrianglePrepared", "l2_red_rate",
+    "graph_build_dev", "gen_rmat_dev", "transpose_dev", "permute_dev", "rand_perm_dev", "rand_perm_exstack_dev",
+    "write_matrix_mm", "mm_header", "read_matrix_mm_dev",
     "splitmix64", "gen_uniform", "gen_values", "gen_uniform_dev", "gen_values_dev", "gen_negative_table", "gen_zipf",
     "keyed_perm", "gen_rmat", "gen_erdos_renyi", "gen_kronecker", "kronecker_triangles",
     "set_host_threads", "release_buffers", "version", "pack_index",
@@ -361,6 +363,18 @@ def rand_perm_dev(n: int, seed: int, device=None, stream=None):
     out = torch.empty(max(n, 1), dtype=torch.int64, device=dev)
     _status(_lib.bale_rand_perm_dev(int(n), seed & (2**64 - 1), _dptr(out, "perm"), _stream(stream)),
             "bale_rand_perm_dev")
+    return out[:n]
+
+
+def rand_perm_exstack_dev(n: int, seed: int, buf_cnt: int = 1024, device=None, stream=None):
+    """spmat's rand_permp_exstack(n, seed, buf_cnt) on the device (a device
+    int64 tensor); the default buf_cnt gives rand_permp(n, seed)."""
+    import torch
+
+    dev = device if device is not None else torch.device("cuda", torch.cuda.current_device())
+    out = torch.empty(max(n, 1), dtype=torch.int64, device=dev)
+    _status(_lib.bale_rand_perm_exstack_dev(int(n), seed & (2**64 - 1), int(buf_cnt), _dptr(out, "perm"),
+                                            _stream(stream)), "bale_rand_perm_exstack_dev")
     return out[:n]
 
 

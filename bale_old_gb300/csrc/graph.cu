@@ -550,51 +550,312 @@ __device__ __forceinline__ uint64_t lcg_jump(uint64_t x, uint64_t k) {
   return (ra * x + rc) & kLcgMask;
 }
 
-// Throw t (the (t+1)-th lrand48 output) lands in slot r_t = lrand48 % m;
-// keys[t] = r_t << tb | t.  Each thread takes a run of consecutive throws.
+__device__ __forceinline__ uint64_t lcg_step(uint64_t x) { return (kLcgA * x + kLcgC) & kLcgMask; }
+
+// Dart throwing (rand_permp_agi, spmat/spmat_agi.upc:56-107; rand_permp_exstack,
+// spmat/spmat_exstack.upc:62-190).  Throw t lands in slot r_t = lrand48() % m
+// for the lrand48 output number idx(t) = t + lost(t): the exstack form loses
+// one draw each time a round of per_round throws finds its buffer full, which
+// happens in every round before round cap and in none after it, so lost(t) =
+// min(t / per_round, cap) (per_round = 0: nothing is lost).  A throw takes its
+// slot exactly when no earlier throw hit it (a slot, once taken, stays
+// taken), so owner[r] = min{t : r_t = r} decides every throw at once.  Each
+// thread takes a run of kThrowsPerThread consecutive throws.
 constexpr int kThrowsPerThread = 64;
+constexpr int kDartRoundsMax = 4096;
 
 __global__ void __launch_bounds__(256)
-    throws_kernel(uint64_t x0, int64_t nthrows, uint64_t m, int tb, uint64_t *__restrict__ keys) {
-  const int64_t first = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) * kThrowsPerThread;
-  if (first >= nthrows) return;
-  uint64_t x = lcg_jump(x0, static_cast<uint64_t>(first));
-  const int64_t last = first + kThrowsPerThread < nthrows ? first + kThrowsPerThread : nthrows;
+    dart_slots_kernel(uint64_t x0, int64_t t_begin, int64_t t_end, int64_t per_round, int64_t cap, uint32_t m,
+                      uint32_t *__restrict__ slot, uint32_t *__restrict__ owner) {
+  const int64_t first =
+      t_begin + (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) * kThrowsPerThread;
+  if (first >= t_end) return;
+  const int64_t last = first + kThrowsPerThread < t_end ? first + kThrowsPerThread : t_end;
+  int64_t lost = 0, next_full = INT64_MAX;
+  if (per_round) {
+    lost = first / per_round < cap ? first / per_round : cap;
+    next_full = (first / per_round + 1) * per_round;
+  }
+  uint64_t x = lcg_jump(x0, static_cast<uint64_t>(first + lost));
   for (int64_t t = first; t < last; t++) {
-    x = (kLcgA * x + kLcgC) & kLcgMask;
-    keys[t] = (((x >> 17) % m) << tb) | static_cast<uint64_t>(t);
-  }
-}
-
-// In slot order (keys sorted by slot, then throw): the first throw at each
-// slot hit it; succ[t] = 1 for those.
-__global__ void __launch_bounds__(256)
-    first_hit_kernel(const uint64_t *__restrict__ sk, int64_t nthrows, int tb, uint32_t *__restrict__ succ) {
-  const uint64_t tmask = (uint64_t(1) << tb) - 1;
-  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
-  for (int64_t j = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; j < nthrows; j += stride)
-    succ[sk[j] & tmask] = (j == 0 || (sk[j] >> tb) != (sk[j - 1] >> tb)) ? 1u : 0u;
-}
-
-// used[j] = slot-order entry j is one of the first n hits.
-__global__ void __launch_bounds__(256)
-    used_kernel(const uint64_t *__restrict__ sk, int64_t nthrows, int tb, const uint32_t *__restrict__ succ,
-                const uint32_t *__restrict__ rank, uint32_t n, uint32_t *__restrict__ used) {
-  const uint64_t tmask = (uint64_t(1) << tb) - 1;
-  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
-  for (int64_t j = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; j < nthrows; j += stride) {
-    const uint64_t t = sk[j] & tmask;
-    used[j] = succ[t] && rank[t] < n ? 1u : 0u;
+    if (t == next_full) {  // round t / per_round - 1 lost a draw if it was full
+      if (t / per_round <= cap) x = lcg_step(x);
+      next_full += per_round;
+    }
+    x = lcg_step(x);
+    const uint32_t r = static_cast<uint32_t>(x >> 17) % m;
+    slot[t] = r;
+    atomicMin(&owner[r], static_cast<uint32_t>(t));
   }
 }
 
 __global__ void __launch_bounds__(256)
-    perm_out_kernel(const uint64_t *__restrict__ sk, int64_t nthrows, int tb, const uint32_t *__restrict__ used,
-                    const uint32_t *__restrict__ upos, const uint32_t *__restrict__ rank, int64_t *__restrict__ perm) {
-  const uint64_t tmask = (uint64_t(1) << tb) - 1;
+    dart_hit_kernel(const uint32_t *__restrict__ slot, const uint32_t *__restrict__ owner, int64_t nthrows,
+                    uint32_t *__restrict__ hit) {
   const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
-  for (int64_t j = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; j < nthrows; j += stride)
-    if (used[j]) perm[upos[j]] = rank[sk[j] & tmask];
+  for (int64_t t = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; t < nthrows; t += stride)
+    hit[t] = owner[slot[t]] == static_cast<uint32_t>(t) ? 1u : 0u;
+}
+
+// rand_permp_agi: dart i is thrown until it hits, so the hit of throw t
+// carries dart S[t] (the hits before t); only the first n hits are thrown.
+__global__ void __launch_bounds__(256)
+    dart_place_agi_kernel(const uint32_t *__restrict__ slot, const uint32_t *__restrict__ hit,
+                          const uint32_t *__restrict__ S, int64_t nthrows, uint32_t n, uint32_t *__restrict__ target) {
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  for (int64_t t = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; t < nthrows; t += stride)
+    if (hit[t] && S[t] < n) target[slot[t]] = S[t];
+}
+
+// rand_permp_exstack throws rounds of per_round darts while more than
+// per_round are pending; the first round k* that finds at most per_round
+// pending starts at throw k* per_round: the first k with S[k per_round] >=
+// n - per_round.  words[1] = k*, or ~0u when the throws so far fall short.
+__global__ void dart_kstar_kernel(const uint32_t *__restrict__ S, int64_t nthrows, int64_t per_round, int64_t n,
+                                  unsigned int *__restrict__ words) {
+  if (threadIdx.x | blockIdx.x) return;
+  const int64_t need = n - per_round;
+  int64_t lo = 0, hi = nthrows / per_round;  // S[hi per_round] reaches need; find the first k that does
+  if (static_cast<int64_t>(S[hi * per_round]) < need) {
+    words[1] = ~0u;
+    return;
+  }
+  while (lo < hi) {
+    const int64_t mid = lo + (hi - lo) / 2;
+    if (static_cast<int64_t>(S[mid * per_round]) >= need) hi = mid;
+    else lo = mid + 1;
+  }
+  words[1] = static_cast<unsigned int>(lo);
+}
+
+// Throws from t0 on are drawn again for the rounds from k* on (no draw is
+// lost there): forget them.
+__global__ void __launch_bounds__(256) dart_forget_kernel(uint32_t *__restrict__ owner, int64_t m, uint32_t t0) {
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  for (int64_t s = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; s < m; s += stride)
+    if (owner[s] != ~0u && owner[s] >= t0) owner[s] = ~0u;
+}
+
+// The rounds from k* on throw every pending dart: round q starts at
+// rstart[q] with as many throws as darts were pending.  words[2] = the end
+// of the last round, words[3] = the round count, words[4] = 0 (done), 1
+// (more throws needed) or 2 (more than kDartRoundsMax rounds).
+__global__ void dart_rounds_kernel(const uint32_t *__restrict__ S, int64_t nthrows, int64_t t0, int64_t n,
+                                   uint32_t *__restrict__ rstart, unsigned int *__restrict__ words) {
+  if (threadIdx.x | blockIdx.x) return;
+  int64_t start = t0, size = n - static_cast<int64_t>(S[t0]);
+  int q = 0;
+  while (size > 0) {
+    if (start + size > nthrows) {
+      words[4] = 1;
+      return;
+    }
+    if (q >= kDartRoundsMax) {
+      words[4] = 2;
+      return;
+    }
+    rstart[q++] = static_cast<uint32_t>(start);
+    const int64_t hits = static_cast<int64_t>(S[start + size]) - static_cast<int64_t>(S[start]);
+    start += size;
+    size -= hits;
+  }
+  rstart[q] = static_cast<uint32_t>(start);
+  words[2] = static_cast<unsigned int>(start);
+  words[3] = static_cast<unsigned int>(q);
+  words[4] = 0;
+}
+
+// The darts of rand_permp_exstack.  A round pops its buffer in throw order
+// and sends the missed darts back in that order; they are written backwards
+// in front of the unthrown darts, so the missed dart of rank r (of ms) is
+// thrown next at position ms - 1 - r of the following round, and the rest
+// of that round throws new darts in order.  Rounds before k* are per_round
+// throws from k per_round; with Rj(k) = k per_round - S[k per_round] darts
+// sent back before round k, round k opens with Rj(k) - Rj(k-1) returned
+// darts and continues with new darts from k per_round - Rj(k-1) on.  From
+// k* on the rounds are rstart[0..nrounds].  Each thread that throws a new
+// dart follows it to its hit and records it in the slot.  words[5] counts
+// chains that ran past the last round (none, for consistent inputs).
+__global__ void __launch_bounds__(256)
+    dart_chase_kernel(const uint32_t *__restrict__ slot, const uint32_t *__restrict__ hit,
+                      const uint32_t *__restrict__ S, int64_t per_round, int64_t kstar,
+                      const uint32_t *__restrict__ rstart, int nrounds, uint32_t *__restrict__ target,
+                      unsigned int *__restrict__ words) {
+  const int64_t t0 = kstar * per_round, tend = rstart[nrounds], t1 = rstart[1];
+  auto sent_back = [&](int64_t k) -> int64_t {  // Rj(k)
+    return k <= 0 ? 0 : k * per_round - static_cast<int64_t>(S[k * per_round]);
+  };
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  for (int64_t t = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; t < tend; t += stride) {
+    int64_t k, j;
+    if (t < t0) {
+      k = t / per_round;
+      j = t - k * per_round;
+    } else if (t < t1) {
+      k = kstar;
+      j = t - t0;
+    } else {
+      continue;  // the rounds after k* throw returned darts only
+    }
+    const int64_t before = sent_back(k - 1), back = sent_back(k) - before;
+    if (j < back) continue;
+    const uint32_t dart = static_cast<uint32_t>(k * per_round - before + j - back);
+    int64_t cur = t;
+    while (!hit[cur]) {
+      int64_t s, s2;
+      if (cur < t0) {
+        s = cur / per_round * per_round;
+        s2 = s + per_round;
+      } else {
+        int lo = 0, hi = nrounds - 1;  // the last round starting at or before cur
+        while (lo < hi) {
+          const int mid = (lo + hi + 1) / 2;
+          if (rstart[mid] <= cur) lo = mid;
+          else hi = mid - 1;
+        }
+        s = rstart[lo];
+        s2 = rstart[lo + 1];
+      }
+      const int64_t ss = S[s], missed = (s2 - s) - (static_cast<int64_t>(S[s2]) - ss);
+      const int64_t rank = (cur - static_cast<int64_t>(S[cur])) - (s - ss);
+      const int64_t nc = s2 + missed - 1 - rank;  // in [s2, s2 + missed) when consistent
+      cur = nc < s2 ? tend : nc;
+      if (cur >= tend) break;
+    }
+    if (cur >= tend) {
+      atomicAdd(&words[5], 1u);
+      continue;
+    }
+    target[slot[cur]] = dart;
+  }
+}
+
+__global__ void __launch_bounds__(256)
+    dart_taken_kernel(const uint32_t *__restrict__ target, int64_t m, uint32_t *__restrict__ taken) {
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  for (int64_t s = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; s < m; s += stride)
+    taken[s] = target[s] != ~0u ? 1u : 0u;
+}
+
+// The permutation is the darts in slot order.
+__global__ void __launch_bounds__(256)
+    dart_perm_kernel(const uint32_t *__restrict__ target, const uint32_t *__restrict__ pos, int64_t m, int64_t n,
+                     int64_t *__restrict__ perm) {
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  for (int64_t s = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; s < m; s += stride)
+    if (target[s] != ~0u && pos[s] < n) perm[pos[s]] = target[s];
+}
+
+// ---------------------------------------------------------------- random permutations (host)
+struct DartWs {
+  uint32_t *owner, *target, *pos, *slot, *hit, *S, *bsum, *rstart;
+  unsigned int *words;  // [0] scan total, [1] k*, [2] last throw, [3] rounds, [4] rounds status, [5] lost chains
+};
+
+size_t dart_ws(int64_t m, int64_t cap, DartWs *w, char *base) {
+  const int64_t nb = (std::max(m, cap) + 1 + kScanBlock - 1) / kScanBlock + 1;
+  size_t o = 0;
+  auto take = [&](size_t bytes) -> uint32_t * {
+    const size_t at = o;
+    o += up256(bytes);
+    return base ? reinterpret_cast<uint32_t *>(base + at) : nullptr;
+  };
+  uint32_t *p;
+  p = take(4 * m); if (w) w->owner = p;
+  p = take(4 * m); if (w) w->target = p;
+  p = take(4 * m); if (w) w->pos = p;
+  p = take(4 * cap); if (w) w->slot = p;
+  p = take(4 * (cap + 1)); if (w) w->hit = p;
+  p = take(4 * (cap + 1)); if (w) w->S = p;
+  p = take(4 * nb); if (w) w->bsum = p;
+  p = take(4 * (kDartRoundsMax + 1)); if (w) w->rstart = p;
+  p = take(64); if (w) w->words = reinterpret_cast<unsigned int *>(p);
+  return o;
+}
+
+int read_words(const unsigned int *d_words, unsigned int *h, int count, cudaStream_t st) {
+  BALE_CUDA_OK(cudaMemcpyAsync(h, d_words, 4 * count, cudaMemcpyDeviceToHost, st));
+  BALE_CUDA_OK(cudaStreamSynchronize(st));
+  return BALE_OK;
+}
+
+void launch_dart_slots(uint64_t x0, int64_t t_begin, int64_t t_end, int64_t per_round, int64_t cap, int64_t m,
+                       const DartWs &w, cudaStream_t st) {
+  const int64_t threads = (t_end - t_begin + kThrowsPerThread - 1) / kThrowsPerThread;
+  dart_slots_kernel<<<static_cast<unsigned>((threads + 255) / 256), 256, 0, st>>>(
+      x0, t_begin, t_end, per_round, cap, static_cast<uint32_t>(m), w.slot, w.owner);
+}
+
+// hit[t] for t < nthrows and S = their exclusive prefix, S[nthrows] = total.
+int dart_hits(int64_t nthrows, const DartWs &w, cudaStream_t st) {
+  dart_hit_kernel<<<grid_for(nthrows), 256, 0, st>>>(w.slot, w.owner, nthrows, w.hit);
+  BALE_CUDA_OK(cudaMemsetAsync(w.hit + nthrows, 0, 4, st));
+  return excl_scan(w.hit, w.S, nthrows + 1, w.bsum, w.words, st);
+}
+
+// rand_permp_agi (per_round = 0) or rand_permp_exstack with buffers of
+// per_round darts (1 <= per_round <= n), for 1 <= n < 2^30.  The throws
+// needed are not known in advance: about 1.39 n hit n distinct slots of 2n.
+// Take 1.5 n + 1024 (and for the exstack rounds from k* on, which throw at
+// most per_round pending darts, 2 per_round + 1024) and double while short.
+int rand_perm_darts(int64_t n, uint64_t seed, int64_t per_round, int64_t *d_perm, cudaStream_t st,
+                    const char *who) {
+  const int64_t m = 2 * n;
+  const uint64_t x0 = ((seed & 0xffffffffull) << 16) | 0x330eull;
+  for (int grow = 0; grow < 6; grow++) {
+    int64_t nt = (n + n / 2 + 1024) << grow, tail = 0;
+    if (per_round) {
+      nt = (nt + per_round - 1) / per_round * per_round;
+      tail = (2 * per_round + 1024) << grow;
+    }
+    const int64_t cap = nt + tail;
+    if (cap >= int64_t(0xffffffff)) break;
+    DartWs w;
+    void *ws = device_workspace(dart_ws(m, cap, nullptr, nullptr), st);
+    if (!ws) return BALE_ENOMEM;
+    dart_ws(m, cap, &w, static_cast<char *>(ws));
+    BALE_CUDA_OK(cudaMemsetAsync(w.owner, 0xff, 4 * m, st));
+    BALE_CUDA_OK(cudaMemsetAsync(w.target, 0xff, 4 * m, st));
+    BALE_CUDA_OK(cudaMemsetAsync(w.words, 0, 64, st));
+    launch_dart_slots(x0, 0, nt, per_round, INT64_MAX, m, w, st);
+    int rc = dart_hits(nt, w, st);
+    if (rc != BALE_OK) return rc;
+    unsigned int h[6] = {0, 0, 0, 0, 0, 0};
+    if (!per_round) {
+      if ((rc = read_words(w.words, h, 1, st)) != BALE_OK) return rc;
+      if (static_cast<int64_t>(h[0]) < n) continue;
+      dart_place_agi_kernel<<<grid_for(nt), 256, 0, st>>>(w.slot, w.hit, w.S, nt, static_cast<uint32_t>(n), w.target);
+    } else {
+      dart_kstar_kernel<<<1, 32, 0, st>>>(w.S, nt, per_round, n, w.words);
+      if ((rc = read_words(w.words, h, 2, st)) != BALE_OK) return rc;
+      if (h[1] == ~0u) continue;
+      const int64_t kstar = h[1], t0 = kstar * per_round, t2 = t0 + tail;
+      dart_forget_kernel<<<grid_for(m), 256, 0, st>>>(w.owner, m, static_cast<uint32_t>(t0));
+      launch_dart_slots(x0, t0, t2, per_round, kstar, m, w, st);
+      if ((rc = dart_hits(t2, w, st)) != BALE_OK) return rc;
+      dart_rounds_kernel<<<1, 32, 0, st>>>(w.S, t2, t0, n, w.rstart, w.words);
+      if ((rc = read_words(w.words, h, 5, st)) != BALE_OK) return rc;
+      if (h[4] == 1) continue;
+      if (h[4] != 0) {
+        set_error("%s: more than %d rounds of returned darts", who, kDartRoundsMax);
+        return BALE_EINVAL;
+      }
+      dart_chase_kernel<<<grid_for(h[2]), 256, 0, st>>>(w.slot, w.hit, w.S, per_round, kstar, w.rstart,
+                                                        static_cast<int>(h[3]), w.target, w.words);
+    }
+    dart_taken_kernel<<<grid_for(m), 256, 0, st>>>(w.target, m, w.owner);
+    if ((rc = excl_scan(w.owner, w.pos, m, w.bsum, w.words, st)) != BALE_OK) return rc;
+    dart_perm_kernel<<<grid_for(m), 256, 0, st>>>(w.target, w.pos, m, n, d_perm);
+    BALE_CUDA_OK(cudaGetLastError());
+    if ((rc = read_words(w.words, h, 6, st)) != BALE_OK) return rc;
+    if (static_cast<int64_t>(h[0]) != n || h[5] != 0) {
+      set_error("%s: %u darts placed of %lld (%u lost)", who, h[0], static_cast<long long>(n), h[5]);
+      return BALE_EINVAL;
+    }
+    return BALE_OK;
+  }
+  set_error("%s: too many throws for n = %lld", who, static_cast<long long>(n));
+  return BALE_EINVAL;
 }
 
 // ---------------------------------------------------------------- MatrixMarket body
@@ -838,47 +1099,19 @@ int bale_rand_perm_dev(int64_t n, uint64_t seed, int64_t *d_perm, void *stream) 
     return BALE_EINVAL;
   }
   if (n == 0) return BALE_OK;
-  cudaStream_t st = static_cast<cudaStream_t>(stream);
-  const uint64_t m = 2 * static_cast<uint64_t>(n);
-  const uint64_t x0 = ((seed & 0xffffffffull) << 16) | 0x330eull;
-  int mb = 1;
-  while ((uint64_t(1) << mb) < m) mb++;
-  // throws: about 1.39 n are needed for n distinct slots among 2n; take
-  // 1.5 n + 1024 and double until the n-th first hit is among them
-  for (int64_t nt = n + n / 2 + 1024;; nt *= 2) {
-    int tb = 1;
-    while ((int64_t(1) << tb) < nt) tb++;
-    if (mb + tb > 64) {
-      set_error("bale_rand_perm_dev: too many throws");
-      return BALE_EINVAL;
-    }
-    Ws w;
-    void *ws = device_workspace(ws_bytes(nt, nt, nullptr, nullptr), st);
-    if (!ws) return BALE_ENOMEM;
-    ws_bytes(nt, nt, &w, static_cast<char *>(ws));
-    BALE_CUDA_OK(cudaMemsetAsync(w.words, 0, 64, st));
-    const int64_t threads = (nt + kThrowsPerThread - 1) / kThrowsPerThread;
-    throws_kernel<<<static_cast<unsigned>((threads + 255) / 256), 256, 0, st>>>(x0, nt, m, tb, w.ka);
-    BALE_CUDA_OK(cudaGetLastError());
-    int rc = BALE_OK;
-    uint64_t *sk = radix_sort(w.ka, w.kb, nt, mb + tb, w, st, &rc);
-    if (rc != BALE_OK) return rc;
-    uint32_t *succ = w.flag, *rank = w.pos, *used = w.deg, *upos = w.newid;
-    first_hit_kernel<<<grid_for(nt), 256, 0, st>>>(sk, nt, tb, succ);
-    rc = excl_scan(succ, rank, nt, w.bsum, w.words, st);
-    if (rc != BALE_OK) return rc;
-    unsigned int hits = 0;
-    BALE_CUDA_OK(cudaMemcpyAsync(&hits, w.words, 4, cudaMemcpyDeviceToHost, st));
-    BALE_CUDA_OK(cudaStreamSynchronize(st));
-    if (static_cast<int64_t>(hits) < n) continue;  // the n-th hit is further on
-    used_kernel<<<grid_for(nt), 256, 0, st>>>(sk, nt, tb, succ, rank, static_cast<uint32_t>(n), used);
-    rc = excl_scan(used, upos, nt, w.bsum, w.words, st);
-    if (rc != BALE_OK) return rc;
-    perm_out_kernel<<<grid_for(nt), 256, 0, st>>>(sk, nt, tb, used, upos, rank, d_perm);
-    BALE_CUDA_OK(cudaGetLastError());
-    BALE_CUDA_OK(cudaStreamSynchronize(st));
-    return BALE_OK;
+  return rand_perm_darts(n, seed, 0, d_perm, static_cast<cudaStream_t>(stream), "bale_rand_perm_dev");
+}
+
+int bale_rand_perm_exstack_dev(int64_t n, uint64_t seed, int64_t buf_cnt, int64_t *d_perm, void *stream) {
+  if (n < 0 || n >= (int64_t(1) << 30) || buf_cnt < 1 || (n > 0 && !d_perm)) {
+    set_error("bale_rand_perm_exstack_dev: bad arguments (n=%lld, buf_cnt=%lld)", static_cast<long long>(n),
+              static_cast<long long>(buf_cnt));
+    return BALE_EINVAL;
   }
+  if (n == 0) return BALE_OK;
+  // a buffer that holds every dart never fills: the same as one of n
+  return rand_perm_darts(n, seed, std::min(buf_cnt, n), d_perm, static_cast<cudaStream_t>(stream),
+                         "bale_rand_perm_exstack_dev");
 }
 
 int bale_read_matrix_mm_dev(const char *path, int64_t *d_offset, int64_t *d_nonzero, void *stream) {

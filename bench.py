@@ -490,7 +490,9 @@ def run_spmat(ctx) -> dict:
                            args.steps, args.warmup)
         r_ms = time_device(lambda: holder.__setitem__("r", bale.rand_perm_dev(np_, 31, device=dev)),
                            args.steps, args.warmup)
-    t_ms, p_ms, r_ms = (ctx["dist"].max(x) for x in (t_ms, p_ms, r_ms))
+        x_ms = time_device(lambda: holder.__setitem__("x", bale.rand_perm_exstack_dev(np_, 31, 1024, device=dev)),
+                           args.steps, args.warmup)
+    t_ms, p_ms, r_ms, x_ms = (ctx["dist"].max(x) for x in (t_ms, p_ms, r_ms, x_ms))
     # MatrixMarket: the scale-20 lower matrix written with the reference's
     # format, read back (file read, upload, parse, sort) on the device
     import tempfile
@@ -508,7 +510,10 @@ def run_spmat(ctx) -> dict:
            "permute": {"value": round(job_rate(nnz, p_ms / 1e3, w) / 1e9, 4), "unit": "G nonzeros/s",
                        "ms_per_step": round(p_ms, 3)},
            "rand_perm": {"value": round(job_rate(np_, r_ms / 1e3, w) / 1e9, 4), "unit": "G elements/s",
-                         "ms_per_step": round(r_ms, 3), "n": np_},
+                         "ms_per_step": round(r_ms, 3), "n": np_, "how": "rand_permp_agi"},
+           "rand_permp": {"value": round(job_rate(np_, x_ms / 1e3, w) / 1e9, 4), "unit": "G elements/s",
+                          "ms_per_step": round(x_ms, 3), "n": np_,
+                          "how": "rand_permp = rand_permp_exstack with buffers of 1024"},
            "read_matrix_mm": {"value": round(L20.nnz / mm_s / 1e9, 4), "unit": "G nonzeros/s",
                               "ms_per_step": round(mm_s * 1e3, 3), "file_bytes": mm_bytes, "nnz": L20.nnz,
                               "how": "bale_read_matrix_mm_dev on R-MAT scale 20 (file in the page cache)"},
@@ -519,7 +524,8 @@ def run_spmat(ctx) -> dict:
                                      "check, key and CSR kernels are not counted"),
            "clocks": clocks.summary(), "gpu_launches": None,
            "config": {"workload": "transpose_matrix / permute_matrix of the R-MAT scale-22 degree-ordered lower "
-                                  "matrix (n = 2^22, 64,155,075 nonzeros); rand_permp of 2^26 elements",
+                                  "matrix (n = 2^22, 64,155,075 nonzeros); rand_permp_agi and rand_permp of 2^26 "
+                                  "elements",
                       "nnz": nnz}}
     if ctx["cpu"]:
         orc = _oracle()
@@ -534,6 +540,9 @@ def run_spmat(ctx) -> dict:
         rp = orc.rand_perm(1 << 22, 31)
         r_cpu = time.perf_counter() - t0
         t0 = time.perf_counter()
+        xp = orc.rand_perm_exstack(1 << 22, 31, 1024)
+        x_cpu = time.perf_counter() - t0
+        t0 = time.perf_counter()
         mo, mc, _ = orc.read_mm(mm_path)
         m_cpu = time.perf_counter() - t0
         do, dc, _ = bale.read_matrix_mm_dev(mm_path, device=dev)
@@ -544,10 +553,13 @@ def run_spmat(ctx) -> dict:
                                "sample": "transpose_matrix_agi at one PE (oracle restatement) of the same matrix",
                                "permute_G_nonzeros_s": round(nnz / p_cpu / 1e9, 5),
                                "rand_perm_G_elements_s": round((1 << 22) / r_cpu / 1e9, 5),
+                               "rand_permp_G_elements_s": round((1 << 22) / x_cpu / 1e9, 5),
                                "rand_perm_sample": "2^22 elements (dart throwing over lrand48)"}
         gt = holder["t"]
         out["parity_ok"] = mm_ok and bool(np.array_equal(gt[0].cpu().numpy(), to) and np.array_equal(gt[1].cpu().numpy(), tc)
-                                and np.array_equal(bale.rand_perm_dev(1 << 22, 31, device=dev).cpu().numpy(), rp))
+                                and np.array_equal(bale.rand_perm_dev(1 << 22, 31, device=dev).cpu().numpy(), rp)
+                                and np.array_equal(bale.rand_perm_exstack_dev(1 << 22, 31, 1024,
+                                                                              device=dev).cpu().numpy(), xp))
     holder.clear()
     os.remove(mm_path)
     os.rmdir(mm_dir)

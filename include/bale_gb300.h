@@ -207,7 +207,12 @@ BALE_API int bale_gen_rmat_dev(int64_t scale, int64_t edgefactor, double a, doub
 /*    keep their order; d_poffset[numrows+1], d_pnonzero[nnz];               */
 /*  * bale_rand_perm_dev: rand_permp_agi(n, seed) (spmat/spmat_agi.upc:      */
 /*    56-107): the permutation the reference's dart throwing yields from     */
-/*    lrand48 after srand48(seed) (seed 0 is taken as srand48(0)).           */
+/*    lrand48 after srand48(seed) (seed 0 is taken as srand48(0));           */
+/*  * bale_rand_perm_exstack_dev: rand_permp_exstack(n, seed, buf_cnt)        */
+/*    (spmat/spmat_exstack.upc:62-190), whose darts fly in rounds of buf_cnt; */
+/*    rand_permp(n, seed) (spmat/spmat_utils.upc:63-74) is buf_cnt = 1024.    */
+/*    A different permutation from rand_permp_agi's for the same seed.       */
+/* Both random permutations take 0 <= n < 2^30.                             */
 /* BALE_EINPUT for malformed offsets or columns, or a rperminv/cperminv     */
 /* that is not a permutation.                                               */
 BALE_API int bale_transpose_dev(const int64_t *d_offset, const int64_t *d_nonzero, int64_t numrows,
@@ -218,6 +223,8 @@ BALE_API int bale_permute_dev(const int64_t *d_offset, const int64_t *d_nonzero,
                               const int64_t *d_cperminv, int64_t *d_poffset, int64_t *d_pnonzero,
                               void *stream);
 BALE_API int bale_rand_perm_dev(int64_t n, uint64_t seed, int64_t *d_perm, void *stream);
+BALE_API int bale_rand_perm_exstack_dev(int64_t n, uint64_t seed, int64_t buf_cnt, int64_t *d_perm,
+                                        void *stream);
 
 /* MatrixMarket files of the reference's kind (spmat/spmat_utils.upc:128-149 */
 /* write_matrix_mm, :217-370 read_matrix_mm_to_dist): "%%MatrixMarket matrix */

@@ -291,6 +291,58 @@ int orc_rand_perm(int64_t n, int64_t seed, int64_t *perm) {
   return 0;
 }
 
+/* rand_permp_exstack (spmat/spmat_exstack.upc:62-190) at THREADS = 1 with
+ * seed != 0; rand_permp (spmat/spmat_utils.upc:63-74) is this with
+ * buf_cnt = 1024.  Darts wait in a list, initially 0..n-1.  Each round
+ * throws the pending darts in list order into a buffer of buf_cnt packages
+ * {slot = lrand48() % 2n, dart}; the draw that finds the buffer full is lost
+ * (exstack_push returns 0 and the loop breaks before the dart advances).
+ * The buffer is then popped in push order: a free slot takes the dart, a
+ * taken one sends it back, and the returned darts, popped in the order they
+ * were sent, are written backwards in front of the unthrown rest of the list.
+ * The permutation is the darts in slot order. */
+int orc_rand_perm_exstack(int64_t n, int64_t seed, int64_t buf_cnt, int64_t *perm) {
+  if (buf_cnt < 1) return -1;
+  const int64_t m = 2 * n;
+  int64_t *target = (int64_t *)malloc((size_t)(m > 0 ? m : 1) * sizeof(int64_t));
+  int64_t *list = (int64_t *)malloc((size_t)(n > 0 ? n : 1) * sizeof(int64_t));
+  int64_t *slot = (int64_t *)malloc((size_t)buf_cnt * sizeof(int64_t));
+  int64_t *dart = (int64_t *)malloc((size_t)buf_cnt * sizeof(int64_t));
+  int rc = -1;
+  if (!target || !list || !slot || !dart) goto done;
+  for (int64_t i = 0; i < m; i++) target[i] = -1;
+  for (int64_t i = 0; i < n; i++) list[i] = i;
+  uint64_t x = (((uint64_t)seed & 0xffffffffull) << 16) | 0x330eull;
+  int64_t iend = 0;
+  while (iend != n) {
+    int64_t i = iend, cnt = 0;
+    while (i < n) {
+      x = (0x5deece66dull * x + 0xbull) & ((1ull << 48) - 1);
+      const int64_t r = (int64_t)(x >> 17) % m;
+      if (cnt == buf_cnt) break;
+      slot[cnt] = r;
+      dart[cnt++] = list[i++];
+    }
+    iend = i;
+    int64_t back = 0;
+    for (int64_t k = 0; k < cnt; k++) {
+      if (target[slot[k]] == -1) target[slot[k]] = dart[k];
+      else dart[back++] = dart[k];  /* back <= k: the returned darts, in order */
+    }
+    for (int64_t k = 0; k < back; k++) list[--iend] = dart[k];
+  }
+  int64_t pos = 0;
+  for (int64_t s = 0; s < m; s++)
+    if (target[s] != -1) perm[pos++] = target[s];
+  rc = 0;
+done:
+  free(target);
+  free(list);
+  free(slot);
+  free(dart);
+  return rc;
+}
+
 /* read_matrix_mm_to_dist (spmat/spmat_utils.upc:217-370) at THREADS = 1: the
  * banner's three words (matrix, coordinate, pattern or integer), the sizes,
  * then fscanf of "row col" (or "row col value") pairs, 1-based; row counts,

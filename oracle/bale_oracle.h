@@ -65,6 +65,9 @@ void orc_permute(const int64_t *offset, const int64_t *nonzero, int64_t numrows,
 /* spmat_agi.upc:56-107 rand_permp_agi at one PE: darts from lrand48 after
  * srand48(seed) into 2n slots, first hits kept, slots read in order. */
 int orc_rand_perm(int64_t n, int64_t seed, int64_t *perm);
+/* spmat_exstack.upc:62-190 rand_permp_exstack at one PE with buf_cnt-package
+ * buffers (rand_permp, spmat_utils.upc:63-74, uses 1024). */
+int orc_rand_perm_exstack(int64_t n, int64_t seed, int64_t buf_cnt, int64_t *perm);
 /* spmat_utils.upc:217-370 read_matrix_mm_to_dist at one PE: header sizes into
  * dims[3] (rows, cols, nnz) when offset is NULL; otherwise the CSR (file
  * order kept within each row).  Returns 0, or -1 for a file it rejects. */

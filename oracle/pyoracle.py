@@ -69,6 +69,7 @@ class Oracle:
             "orc_transpose": (C.c_int, [P64, P64, i64, i64, P64, P64]),
             "orc_permute": (None, [P64, P64, i64, P64, P64, P64, P64]),
             "orc_rand_perm": (C.c_int, [i64, i64, P64]),
+            "orc_rand_perm_exstack": (C.c_int, [i64, i64, i64, P64]),
             "orc_read_mm": (C.c_int, [C.c_char_p, P64, P64, P64]),
             "orc_num_cpus": (C.c_int, []),
         }
@@ -143,6 +144,12 @@ class Oracle:
             raise MemoryError("orc_rand_perm")
         return out[:n]
 
+    def rand_perm_exstack(self, n: int, seed: int, buf_cnt: int = 1024) -> np.ndarray:
+        out = np.zeros(max(n, 1), np.int64)
+        if self.lib.orc_rand_perm_exstack(n, seed, buf_cnt, _p(out)) != 0:
+            raise MemoryError("orc_rand_perm_exstack")
+        return out[:n]
+
     def read_mm(self, path) -> tuple[np.ndarray, np.ndarray, int]:
         dims = np.zeros(3, np.int64)
         if self.lib.orc_read_mm(str(path).encode(), _p(dims), None, None) != 0:
@@ -188,6 +195,8 @@ class Reference:
             "transpose_matrix_agi": (PS, [PS]),
             "permute_matrix_agi": (PS, [PS, P64, P64]),
             "rand_permp_agi": (P64, [i64, C.c_int]),
+            "rand_permp_exstack": (P64, [i64, C.c_int, i64]),
+            "rand_permp": (P64, [i64, C.c_int]),
             "write_matrix_mm": (C.c_int, [PS, C.c_char_p]),
             "read_matrix_mm_to_dist": (PS, [C.c_char_p]),
         }
@@ -258,6 +267,17 @@ class Reference:
         """spmat's rand_permp_agi (spmat/spmat_agi.upc:56-107) at one PE: darts
         from lrand48 after srand48(seed) (seed != 0)."""
         p = self.lib.rand_permp_agi(n, seed)
+        return np.ctypeslib.as_array(p, shape=(n,)).copy()
+
+    def rand_perm_exstack(self, n: int, seed: int, buf_cnt: int = 1024) -> np.ndarray:
+        """spmat's rand_permp_exstack (spmat/spmat_exstack.upc:62-190) at one
+        PE; rand_permp (spmat/spmat_utils.upc:63-74) calls it with 1024."""
+        p = self.lib.rand_permp_exstack(n, seed, buf_cnt)
+        return np.ctypeslib.as_array(p, shape=(n,)).copy()
+
+    def rand_permp(self, n: int, seed: int) -> np.ndarray:
+        """spmat's rand_permp (spmat/spmat_utils.upc:63-74) at one PE."""
+        p = self.lib.rand_permp(n, seed)
         return np.ctypeslib.as_array(p, shape=(n,)).copy()
 
     def erdos_renyi_lower(self, n: int, p: float, seed: int) -> tuple[np.ndarray, np.ndarray]:

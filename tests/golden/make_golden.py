@@ -15,7 +15,8 @@ inputs, what the reference returns:
 * spmat.npz      -- transpose_matrix_agi and permute_matrix_agi of small
                     matrices (an R-MAT lower matrix, the reference's own
                     Erdos-Renyi graph, a rectangular matrix with empty rows),
-                    rand_permp_agi(n, seed) permutations, and the reference's
+                    rand_permp_agi(n, seed) and rand_permp_exstack(n, seed,
+                    buf_cnt) permutations, one rand_permp, and the reference's
                     read_matrix_mm_to_dist of MatrixMarket files written by its
                     write_matrix_mm (*.mm, committed beside the vectors) and of
                     a hand-made integer file with rows out of order;
@@ -160,6 +161,16 @@ def make_spmat(ref: Reference) -> dict:
         perms.append(f"perm_{n}_{seed}")
         cases[f"perm_{n}_{seed}"] = ref.rand_perm(n, seed)
     cases["perms"] = np.array(perms)
+    # rand_permp_exstack(n, seed, buf_cnt): rounds that fill the buffer
+    # (buf_cnt < n), the rounds after (buf_cnt near n), and one round
+    # (buf_cnt >= n); rand_permp is buf_cnt = 1024
+    xperms = []
+    for n, seed, b in ((1, 1, 1024), (5, 3, 1), (40, 9, 2), (1000, 99, 7), (1023, 5, 1024), (1024, 5, 1024),
+                       (1025, 5, 1024), (3000, 2, 4096), (5000, 8, 64), (100_000, 31, 1024)):
+        xperms.append(f"xperm_{n}_{seed}_{b}")
+        cases[f"xperm_{n}_{seed}_{b}"] = ref.rand_perm_exstack(n, seed, b)
+    cases["xperms"] = np.array(xperms)
+    cases["permp_100000_31"] = ref.rand_permp(100_000, 31)
     # MatrixMarket: files written by the reference's writer, and a hand-made
     # one with rows out of order, comment-free, integer field; read back by
     # the reference's reader

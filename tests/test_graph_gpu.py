@@ -122,6 +122,32 @@ def test_rand_perm_matches_oracle_at_size(cuda, bale, oracle, n, seed):
     np.testing.assert_array_equal(bale.rand_perm_dev(n, seed).cpu().numpy(), oracle.rand_perm(n, seed))
 
 
+def test_rand_perm_exstack_matches_reference_golden(cuda, bale, golden):
+    d = golden("spmat")
+    for p in d["xperms"]:
+        _, n, seed, b = str(p).split("_")
+        got = bale.rand_perm_exstack_dev(int(n), int(seed), int(b)).cpu().numpy()
+        np.testing.assert_array_equal(got, d[p], err_msg=str(p))
+    np.testing.assert_array_equal(bale.rand_perm_exstack_dev(100_000, 31).cpu().numpy(), d["permp_100000_31"])
+
+
+# buffers far below n (most rounds full), of one dart, near n, and above n
+@pytest.mark.parametrize("n,seed,b", [(4097, 77, 1024), (1 << 20, 2024, 1024), (3_000_001, 9, 1024),
+                                      (200_000, 4, 1), (300_000, 6, 299_999), (50_000, 12, 1 << 40),
+                                      (1 << 20, 5, 65_536)])
+def test_rand_perm_exstack_matches_oracle_at_size(cuda, bale, oracle, n, seed, b):
+    got = bale.rand_perm_exstack_dev(n, seed, b).cpu().numpy()
+    np.testing.assert_array_equal(got, oracle.rand_perm_exstack(n, seed, b))
+
+
+def test_rand_perm_exstack_rejects_bad_arguments(cuda, bale):
+    with pytest.raises(bale.BaleError):
+        bale.rand_perm_exstack_dev(100, 1, 0)
+    with pytest.raises(bale.BaleError):
+        bale.rand_perm_exstack_dev(-1, 1, 1024)
+    assert bale.rand_perm_exstack_dev(0, 1, 1024).numel() == 0
+
+
 @pytest.mark.parametrize("scale", [12, 18])
 def test_transpose_and_permute_match_oracle_at_size(cuda, bale, oracle, scale):
     L = bale.gen_rmat(scale, 16, 0.57, 0.19, 0.19, scale)

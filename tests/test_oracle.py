@@ -169,6 +169,16 @@ def test_rand_perm_matches_reference_golden(oracle, golden):
         np.testing.assert_array_equal(oracle.rand_perm(int(n), int(seed)), d[p], err_msg=str(p))
 
 
+def test_rand_perm_exstack_matches_reference_golden(oracle, golden):
+    d = golden("spmat")
+    for p in d["xperms"]:
+        _, n, seed, b = str(p).split("_")
+        np.testing.assert_array_equal(oracle.rand_perm_exstack(int(n), int(seed), int(b)), d[p], err_msg=str(p))
+    # rand_permp is the exstack form with buffers of 1024, not rand_permp_agi
+    np.testing.assert_array_equal(d["permp_100000_31"], d["xperm_100000_31_1024"])
+    assert not np.array_equal(d["permp_100000_31"], d["perm_100000_31"])
+
+
 @pytest.mark.skipif(not REF_LIB.exists(), reason="oracle/_ref is built only where the reference tree exists")
 def test_spmat_restatements_match_reference_on_fresh_inputs(oracle, bale):
     ref = Reference()
@@ -186,6 +196,9 @@ def test_spmat_restatements_match_reference_on_fresh_inputs(oracle, bale):
         np.testing.assert_array_equal(po, qo)
         np.testing.assert_array_equal(pc, qc)
         np.testing.assert_array_equal(oracle.rand_perm(5000 + seed, seed), ref.rand_perm(5000 + seed, seed))
+        for b in (1, 3, 1000, 5003, 10_000):
+            np.testing.assert_array_equal(oracle.rand_perm_exstack(5000 + seed, seed, b),
+                                          ref.rand_perm_exstack(5000 + seed, seed, b), err_msg=str(b))
 
 
 def test_matrix_market_reader_matches_reference_golden(oracle, golden):

@@ -29,6 +29,7 @@ __all__ = [
     "histo_dev", "ig_dev", "triangle_dev", "ig_dev_noalloc", "TrianglePrepared", "l2_red_rate",
     "graph_build_dev", "gen_rmat_dev", "transpose_dev", "permute_dev", "rand_perm_dev", "rand_perm_exstack_dev",
     "write_matrix_mm", "mm_header", "read_matrix_mm_dev",
+    "write_sparse_matrix", "write_sparse_matrix_dev", "sparse_matrix_header", "read_sparse_matrix_dev",
     "splitmix64", "gen_uniform", "gen_values", "gen_uniform_dev", "gen_values_dev", "gen_negative_table", "gen_zipf",
     "keyed_perm", "gen_rmat", "gen_erdos_renyi", "gen_kronecker", "kronecker_triangles",
     "set_host_threads", "release_buffers", "version", "pack_index",
@@ -402,6 +403,44 @@ def read_matrix_mm_dev(path, device=None, stream=None):
     col = torch.empty(max(nnz, 1), dtype=torch.int64, device=dev)
     _status(_lib.bale_read_matrix_mm_dev(str(path).encode(), _dptr(off, "offset"), _dptr(col, "nonzero"),
                                          _stream(stream)), "bale_read_matrix_mm_dev")
+    return off, col[:nnz], nc
+
+
+def write_sparse_matrix(L: "SparseMatrix", dirname) -> None:
+    """spmat's write_sparse_matrix_agi at one PE: the matrix as a binary
+    dataset directory (metadata, rowcnt_0, nonzero_0)."""
+    _status(_lib.bale_write_sparse_matrix(str(dirname).encode(), L.ptr()), "bale_write_sparse_matrix")
+
+
+def write_sparse_matrix_dev(dirname, offset, nonzero, numcols: int, nwriters: int = 1, stream=None) -> None:
+    """A device CSR written as a binary dataset with nwriters row blocks (the
+    layout the reference writes at nwriters PEs)."""
+    nnz = nonzero.numel()
+    _status(_lib.bale_write_sparse_matrix_dev(str(dirname).encode(), _dptr(offset, "offset"),
+                                              _dptr(nonzero, "nonzero") if nnz else None, offset.numel() - 1,
+                                              int(numcols), nnz, int(nwriters), _stream(stream)),
+            "bale_write_sparse_matrix_dev")
+
+
+def sparse_matrix_header(dirname) -> tuple[int, int, int, int]:
+    """(numrows, numcols, nnz, nwriters) of a binary dataset."""
+    v = [C.c_int64(0) for _ in range(4)]
+    _status(_lib.bale_sparse_matrix_header(str(dirname).encode(), *(C.byref(x) for x in v)),
+            "bale_sparse_matrix_header")
+    return tuple(x.value for x in v)
+
+
+def read_sparse_matrix_dev(dirname, device=None, stream=None):
+    """A binary dataset (any number of writers) read into device int64
+    tensors: returns (offset, nonzero, numcols)."""
+    import torch
+
+    nr, nc, nnz, _ = sparse_matrix_header(dirname)
+    dev = device if device is not None else torch.device("cuda", torch.cuda.current_device())
+    off = torch.empty(nr + 1, dtype=torch.int64, device=dev)
+    col = torch.empty(max(nnz, 1), dtype=torch.int64, device=dev)
+    _status(_lib.bale_read_sparse_matrix_dev(str(dirname).encode(), _dptr(off, "offset"), _dptr(col, "nonzero"),
+                                             _stream(stream)), "bale_read_sparse_matrix_dev")
     return off, col[:nnz], nc
 
 

@@ -93,6 +93,10 @@ SIGNATURES: dict[str, tuple[object, list[object]]] = {
     "bale_write_matrix_mm": (C.c_int, [C.POINTER(sparsemat_t), C.c_char_p]),
     "bale_mm_header": (C.c_int, [C.c_char_p, P64, P64, P64, P64, C.POINTER(C.c_int)]),
     "bale_read_matrix_mm_dev": (C.c_int, [C.c_char_p, VP, VP, VP]),
+    "bale_write_sparse_matrix": (C.c_int, [C.c_char_p, C.POINTER(sparsemat_t)]),
+    "bale_write_sparse_matrix_dev": (C.c_int, [C.c_char_p, VP, VP, i64, i64, i64, i64, VP]),
+    "bale_sparse_matrix_header": (C.c_int, [C.c_char_p, P64, P64, P64, P64]),
+    "bale_read_sparse_matrix_dev": (C.c_int, [C.c_char_p, VP, VP, VP]),
     "bale_triangle_prepare": (VP, [VP, VP, i64, i64, VP, VP]),
     "bale_triangle_count_prepared": (C.c_int, [VP, VP, VP, VP]),
     "bale_triangle_release": (None, [VP]),

@@ -1,4 +1,5 @@
-/* mmio.c -- MatrixMarket files of the reference's kind: the host side.
+/* mmio.c -- MatrixMarket files and binary sparse matrix datasets of the
+ * reference's kinds: the host side.
  *
  * spmat's write_matrix_mm (spmat/spmat_utils.upc:128-149) writes
  *   %%MatrixMarket matrix coordinate pattern
@@ -13,6 +14,7 @@
 #include <inttypes.h>
 #include <stdio.h>
 #include <string.h>
+#include <sys/stat.h>
 
 #include "bale_gb300.h"
 
@@ -60,4 +62,51 @@ int bale_mm_header(const char *path, int64_t *numrows, int64_t *numcols, int64_t
 done:
   fclose(fp);
   return rc;
+}
+
+/* Binary datasets (spmat/spmat_agi.upc:245-335 write_rowcounts and
+ * write_sparse_matrix_agi, spmat/spmat_exstack.upc:494-686
+ * write_sparse_matrix_exstack, spmat/spmat_utils.upc:159-206 the metadata
+ * file): a directory holding "metadata" (numrows, numcols, nnz and the
+ * number of writers, one decimal per line), and per writer w "rowcnt_<w>"
+ * (its rows' lengths) and "nonzero_<w>" (their columns, row after row), both
+ * raw int64.  Writer w of W takes the w-th block of (numrows + W - w - 1) / W
+ * consecutive rows.  This writes the one-writer dataset the reference writes
+ * at one PE. */
+int bale_write_sparse_matrix(const char *dirname, const sparsemat_t *A) {
+  if (!dirname || !A || A->numrows < 0 || !A->loffset || (A->nnz > 0 && !A->lnonzero)) return BALE_EINVAL;
+  char name[4096];
+  mkdir(dirname, 0770);  /* may exist already, as in the reference */
+  if (snprintf(name, sizeof name, "%s/metadata", dirname) >= (int)sizeof name) return BALE_EINVAL;
+  FILE *fp = fopen(name, "w");
+  if (!fp) return BALE_EINPUT;
+  int ok = fprintf(fp, "%" PRId64 "\n%" PRId64 "\n%" PRId64 "\n%d\n", A->numrows, A->numcols, A->nnz, 1) > 0;
+  if (fclose(fp) != 0) ok = 0;
+  snprintf(name, sizeof name, "%s/rowcnt_0", dirname);
+  if (!ok || !(fp = fopen(name, "wb"))) return BALE_EINPUT;
+  for (int64_t i = 0; ok && i < A->numrows; i++) {
+    const int64_t rc = A->loffset[i + 1] - A->loffset[i];
+    ok = fwrite(&rc, sizeof rc, 1, fp) == 1;
+  }
+  if (fclose(fp) != 0) ok = 0;
+  snprintf(name, sizeof name, "%s/nonzero_0", dirname);
+  if (!ok || !(fp = fopen(name, "wb"))) return BALE_EINPUT;
+  const size_t nnz = (size_t)(A->numrows > 0 ? A->loffset[A->numrows] : 0);
+  ok = nnz == 0 || fwrite(A->lnonzero, sizeof(int64_t), nnz, fp) == nnz;
+  if (fclose(fp) != 0) ok = 0;
+  return ok ? BALE_OK : BALE_EINPUT;
+}
+
+/* The metadata file, read as read_sparse_matrix_metadata does (four "%ld"). */
+int bale_sparse_matrix_header(const char *dirname, int64_t *numrows, int64_t *numcols, int64_t *nnz,
+                              int64_t *nwriters) {
+  if (!dirname || !numrows || !numcols || !nnz || !nwriters) return BALE_EINVAL;
+  char name[4096];
+  if (snprintf(name, sizeof name, "%s/metadata", dirname) >= (int)sizeof name) return BALE_EINVAL;
+  FILE *fp = fopen(name, "r");
+  if (!fp) return BALE_EINPUT;
+  const int got = fscanf(fp, "%" SCNd64 " %" SCNd64 " %" SCNd64 " %" SCNd64, numrows, numcols, nnz, nwriters);
+  fclose(fp);
+  if (got != 4 || *numrows < 0 || *numcols < 0 || *nnz < 0 || *nwriters < 1) return BALE_EINPUT;
+  return BALE_OK;
 }

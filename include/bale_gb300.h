@@ -240,6 +240,33 @@ BALE_API int bale_mm_header(const char *path, int64_t *numrows, int64_t *numcols
                             int64_t *body, int *fields);
 BALE_API int bale_read_matrix_mm_dev(const char *path, int64_t *d_offset, int64_t *d_nonzero, void *stream);
 
+/* Binary sparse matrix datasets (spmat/spmat_agi.upc:245-335               */
+/* write_rowcounts / write_sparse_matrix_agi, spmat/spmat_exstack.upc:       */
+/* 494-686 write_sparse_matrix_exstack, spmat/spmat_utils.upc:159-206 the    */
+/* metadata file): a directory with "metadata" (numrows, numcols, nnz, the  */
+/* number of writers W; one decimal per line) and per writer w "rowcnt_<w>"  */
+/* and "nonzero_<w>" (raw int64 row lengths and columns of the w-th block of */
+/* (numrows + W - w - 1) / W consecutive rows).  The reference at THREADS PEs */
+/* writes W = THREADS.                                                      */
+/*  * bale_write_sparse_matrix: the host matrix, W = 1: the same bytes as    */
+/*    write_sparse_matrix_agi / _exstack at one PE;                         */
+/*  * bale_write_sparse_matrix_dev: a device CSR (checked first), W writers;  */
+/*    the copies overlap the file writes;                                   */
+/*  * bale_sparse_matrix_header: the metadata file;                         */
+/*  * bale_read_sparse_matrix_dev: any W, into d_offset[numrows+1] and       */
+/*    d_nonzero[nnz] (the reference's reader is unfinished and compiled     */
+/*    out); BALE_EINPUT unless the files, lengths and columns agree.         */
+/*    numrows < 2^31, nnz < 2^32 - 1.                                       */
+/* W <= 65536.  Synchronous.                                                */
+BALE_API int bale_write_sparse_matrix(const char *dirname, const sparsemat_t *A);
+BALE_API int bale_write_sparse_matrix_dev(const char *dirname, const int64_t *d_offset, const int64_t *d_nonzero,
+                                          int64_t numrows, int64_t numcols, int64_t nnz, int64_t nwriters,
+                                          void *stream);
+BALE_API int bale_sparse_matrix_header(const char *dirname, int64_t *numrows, int64_t *numcols, int64_t *nnz,
+                                       int64_t *nwriters);
+BALE_API int bale_read_sparse_matrix_dev(const char *dirname, int64_t *d_offset, int64_t *d_nonzero,
+                                         void *stream);
+
 /* ======================= batched execution ============================== */
 /* Many instances of uneven size in one CUDA graph: a persistent work-queue  */
 /* kernel takes tiles of every instance (tile sizes per kind and size class  */

@@ -13,6 +13,7 @@
 
 #include <pthread.h>
 #include <stdio.h>
+#include <sys/stat.h>
 #include <stdlib.h>
 #include <string.h>
 #include <unistd.h>
@@ -341,6 +342,36 @@ done:
   free(slot);
   free(dart);
   return rc;
+}
+
+/* write_sparse_matrix_agi (spmat/spmat_agi.upc:286-335) at THREADS = 1: the
+ * directory, its "metadata" file (write_sparse_matrix_metadata,
+ * spmat/spmat_utils.upc:196-206: numrows, numcols, nnz and the writer count,
+ * one "%ld" per line), "rowcnt_0" (write_rowcounts, spmat_agi.upc:250-277:
+ * each row's length as a binary int64) and "nonzero_0" (the rows' columns as
+ * binary int64, row after row). */
+int orc_write_dataset(const char *dirname, const int64_t *offset, const int64_t *nonzero, int64_t numrows,
+                      int64_t numcols) {
+  char fname[4096];
+  mkdir(dirname, 0770);
+  snprintf(fname, sizeof fname, "%s/metadata", dirname);
+  FILE *fp = fopen(fname, "w");
+  if (!fp) return -1;
+  fprintf(fp, "%ld\n%ld\n%ld\n%ld\n", (long)numrows, (long)numcols, (long)offset[numrows], 1L);
+  fclose(fp);
+  snprintf(fname, sizeof fname, "%s/rowcnt_0", dirname);
+  if (!(fp = fopen(fname, "wb"))) return -1;
+  for (int64_t i = 0; i < numrows; i++) {
+    const int64_t rc = offset[i + 1] - offset[i];
+    if (fwrite(&rc, sizeof rc, 1, fp) != 1) { fclose(fp); return -1; }
+  }
+  fclose(fp);
+  snprintf(fname, sizeof fname, "%s/nonzero_0", dirname);
+  if (!(fp = fopen(fname, "wb"))) return -1;
+  const size_t nnz = (size_t)offset[numrows];
+  const int ok = nnz == 0 || fwrite(nonzero, sizeof(int64_t), nnz, fp) == nnz;
+  fclose(fp);
+  return ok ? 0 : -1;
 }
 
 /* read_matrix_mm_to_dist (spmat/spmat_utils.upc:217-370) at THREADS = 1: the

@@ -68,6 +68,10 @@ int orc_rand_perm(int64_t n, int64_t seed, int64_t *perm);
 /* spmat_exstack.upc:62-190 rand_permp_exstack at one PE with buf_cnt-package
  * buffers (rand_permp, spmat_utils.upc:63-74, uses 1024). */
 int orc_rand_perm_exstack(int64_t n, int64_t seed, int64_t buf_cnt, int64_t *perm);
+/* spmat_agi.upc:286-335 write_sparse_matrix_agi at one PE: dirname/metadata,
+ * rowcnt_0 and nonzero_0. */
+int orc_write_dataset(const char *dirname, const int64_t *offset, const int64_t *nonzero, int64_t numrows,
+                      int64_t numcols);
 /* spmat_utils.upc:217-370 read_matrix_mm_to_dist at one PE: header sizes into
  * dims[3] (rows, cols, nnz) when offset is NULL; otherwise the CSR (file
  * order kept within each row).  Returns 0, or -1 for a file it rejects. */

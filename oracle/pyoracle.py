@@ -70,6 +70,7 @@ class Oracle:
             "orc_permute": (None, [P64, P64, i64, P64, P64, P64, P64]),
             "orc_rand_perm": (C.c_int, [i64, i64, P64]),
             "orc_rand_perm_exstack": (C.c_int, [i64, i64, i64, P64]),
+            "orc_write_dataset": (C.c_int, [C.c_char_p, P64, P64, i64, i64]),
             "orc_read_mm": (C.c_int, [C.c_char_p, P64, P64, P64]),
             "orc_num_cpus": (C.c_int, []),
         }
@@ -150,6 +151,11 @@ class Oracle:
             raise MemoryError("orc_rand_perm_exstack")
         return out[:n]
 
+    def write_dataset(self, offset: np.ndarray, nonzero: np.ndarray, numcols: int, dirname) -> None:
+        if self.lib.orc_write_dataset(str(dirname).encode(), _p(offset), _p(nonzero), offset.size - 1,
+                                      numcols) != 0:
+            raise OSError(f"orc_write_dataset: {dirname}")
+
     def read_mm(self, path) -> tuple[np.ndarray, np.ndarray, int]:
         dims = np.zeros(3, np.int64)
         if self.lib.orc_read_mm(str(path).encode(), _p(dims), None, None) != 0:
@@ -199,6 +205,8 @@ class Reference:
             "rand_permp": (P64, [i64, C.c_int]),
             "write_matrix_mm": (C.c_int, [PS, C.c_char_p]),
             "read_matrix_mm_to_dist": (PS, [C.c_char_p]),
+            "write_sparse_matrix_agi": (i64, [C.c_char_p, PS]),
+            "write_sparse_matrix_exstack": (i64, [C.c_char_p, PS, i64]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(lib, name)
@@ -253,6 +261,27 @@ class Reference:
         m = _sparsemat_t(0, n, n, numcols, nonzero.size, nonzero.size, po, po, pn, pn)
         if self.lib.write_matrix_mm(C.byref(m), path.encode()) != 0:
             raise RuntimeError("write_matrix_mm failed")
+
+    def write_dataset(self, offset: np.ndarray, nonzero: np.ndarray, numcols: int, dirname: str,
+                      buf_cnt: int | None = None) -> None:
+        """spmat's write_sparse_matrix_agi (spmat/spmat_agi.upc:286-335), or
+        with buf_cnt write_sparse_matrix_exstack (spmat/spmat_exstack.upc:
+        494-686), at one PE.  Its file names live in 64-byte buffers: keep
+        dirname short."""
+        n = offset.size - 1
+        po, pn = _p(offset), _p(nonzero)
+        m = _sparsemat_t(0, n, n, numcols, nonzero.size, nonzero.size, po, po, pn, pn)
+        if len(dirname) > 40:
+            raise ValueError("dirname too long for the reference's 64-byte file names")
+        if buf_cnt is None:
+            rc = self.lib.write_sparse_matrix_agi(dirname.encode(), C.byref(m))
+        else:
+            rc = self.lib.write_sparse_matrix_exstack(dirname.encode(), C.byref(m), buf_cnt)
+            # it leaves rowcnt_0 and nonzero_0 open (no fclose): the bytes sit
+            # in stdio buffers until exit, so flush every open stream
+            C.CDLL(None).fflush(None)
+        if rc != 0:
+            raise RuntimeError("write_sparse_matrix failed")
 
     def read_mm(self, path: str) -> tuple[np.ndarray, np.ndarray, int]:
         """spmat's read_matrix_mm_to_dist (spmat/spmat_utils.upc:217-370) at one PE."""

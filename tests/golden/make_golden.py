@@ -20,6 +20,9 @@ inputs, what the reference returns:
                     read_matrix_mm_to_dist of MatrixMarket files written by its
                     write_matrix_mm (*.mm, committed beside the vectors) and of
                     a hand-made integer file with rows out of order;
+* ds_<tag>/      -- binary datasets (metadata, rowcnt_0, nonzero_0) that
+                    write_sparse_matrix_agi writes for two of those matrices
+                    (write_sparse_matrix_exstack writes the same bytes);
 * triangles.npz  -- count and shared-refs/pushes of triangle_agi,
                     triangle_exstack_push, triangle_exstack2_push and the
                     alternate triangle_agi_iter on Kronecker graphs (closed-form
@@ -192,6 +195,39 @@ def make_spmat(ref: Reference) -> dict:
     return cases
 
 
+def make_datasets(ref: Reference, spmat: dict) -> list[str]:
+    """Binary sparse matrix datasets: write_sparse_matrix_agi of two of the
+    spmat matrices at one PE, copied to ds_<tag>/ (metadata, rowcnt_0,
+    nonzero_0); write_sparse_matrix_exstack (buffers of 1024 and of 16
+    packages) must write the same bytes."""
+    import filecmp
+    import os
+    import shutil
+    import tempfile
+
+    made = []
+    for tag in ("rmat8_lower", "rect_300x517"):
+        off, col = spmat[f"{tag}/offset"], spmat[f"{tag}/nonzero"]
+        nc = int(spmat[f"{tag}/numcols"][0])
+        tmp = tempfile.mkdtemp(prefix="bds")
+        cwd = os.getcwd()
+        try:
+            os.chdir(tmp)  # the reference builds file names in 64-byte buffers
+            ref.write_dataset(off, col, nc, "agi")
+            for b in (1024, 16):
+                ref.write_dataset(off, col, nc, f"ex{b}", buf_cnt=b)
+                for f in ("metadata", "rowcnt_0", "nonzero_0"):
+                    assert filecmp.cmp(f"agi/{f}", f"ex{b}/{f}", shallow=False), (tag, b, f)
+            dst = OUT / f"ds_{tag}"
+            shutil.rmtree(dst, ignore_errors=True)
+            shutil.copytree("agi", dst)
+        finally:
+            os.chdir(cwd)
+            shutil.rmtree(tmp)
+        made.append(f"ds_{tag}")
+    return made
+
+
 def main() -> int:
     if build_ref() is None:
         print("reference tree not found; cannot regenerate golden vectors", file=sys.stderr)
@@ -200,7 +236,10 @@ def main() -> int:
     np.savez_compressed(OUT / "histo.npz", **make_histo(ref))
     np.savez_compressed(OUT / "ig.npz", **make_ig(ref))
     np.savez_compressed(OUT / "triangles.npz", **make_triangles(ref))
-    np.savez_compressed(OUT / "spmat.npz", **make_spmat(ref))
+    spmat = make_spmat(ref)
+    np.savez_compressed(OUT / "spmat.npz", **spmat)
+    for d in make_datasets(ref, spmat):
+        print(d, sum(f.stat().st_size for f in (OUT / d).iterdir()), "bytes")
     for f in ("histo.npz", "ig.npz", "triangles.npz", "spmat.npz", "rmat8_lower.mm", "rect_300x517.mm",
               "unordered_integer.mm"):
         print(f, (OUT / f).stat().st_size, "bytes")

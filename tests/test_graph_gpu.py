@@ -217,3 +217,117 @@ def test_matrix_market_malformed_is_an_error(cuda, bale, tmp_path, body):
     p.write_text("%%MatrixMarket matrix coordinate pattern\n" + body)
     with pytest.raises(bale.BaleError):
         bale.read_matrix_mm_dev(p)
+
+
+# ---------------------------------------------------------------- binary datasets
+DS_FILES = ("metadata", "rowcnt_0", "nonzero_0")
+
+
+def _golden_dir():
+    from pathlib import Path
+
+    return Path(__file__).resolve().parent / "golden"
+
+
+@pytest.mark.parametrize("tag", ["rmat8_lower", "rect_300x517"])
+def test_dataset_device_writer_matches_reference_bytes(cuda, bale, golden, tmp_path, tag):
+    d = golden("spmat")
+    off, col, nc = d[f"{tag}/offset"], d[f"{tag}/nonzero"], int(d[f"{tag}/numcols"][0])
+    bale.write_sparse_matrix_dev(tmp_path / "ds", _dev(off, cuda), _dev(col, cuda), nc)
+    for f in DS_FILES:
+        assert (tmp_path / "ds" / f).read_bytes() == (_golden_dir() / f"ds_{tag}" / f).read_bytes(), f
+
+
+@pytest.mark.parametrize("tag", ["rmat8_lower", "rect_300x517"])
+def test_dataset_reader_reads_reference_files(cuda, bale, golden, tag):
+    d = golden("spmat")
+    off, col, nc = bale.read_sparse_matrix_dev(_golden_dir() / f"ds_{tag}")
+    assert nc == int(d[f"{tag}/numcols"][0])
+    np.testing.assert_array_equal(off.cpu().numpy(), d[f"{tag}/offset"])
+    np.testing.assert_array_equal(col.cpu().numpy(), d[f"{tag}/nonzero"])
+
+
+@pytest.mark.parametrize("writers", [2, 3, 7, 301, 1000])
+def test_dataset_writer_blocks(cuda, bale, golden, tmp_path, writers):
+    """W writers: the w-th block of (n + W - w - 1) / W rows; the files put
+    together are the one-writer files."""
+    d = golden("spmat")
+    tag = "rect_300x517"
+    off, col, nc = d[f"{tag}/offset"], d[f"{tag}/nonzero"], int(d[f"{tag}/numcols"][0])
+    n = off.size - 1
+    out = tmp_path / "ds"
+    bale.write_sparse_matrix_dev(out, _dev(off, cuda), _dev(col, cuda), nc, nwriters=writers)
+    assert (out / "metadata").read_text().split() == [str(n), str(nc), str(col.size), str(writers)]
+    rc = [np.fromfile(out / f"rowcnt_{w}", np.int64) for w in range(writers)]
+    assert [r.size for r in rc] == [(n + writers - w - 1) // writers for w in range(writers)]
+    g = _golden_dir() / f"ds_{tag}"
+    assert b"".join(r.tobytes() for r in rc) == (g / "rowcnt_0").read_bytes()
+    assert b"".join((out / f"nonzero_{w}").read_bytes() for w in range(writers)) == (g / "nonzero_0").read_bytes()
+    r_off, r_col, r_nc = bale.read_sparse_matrix_dev(out)
+    assert r_nc == nc
+    np.testing.assert_array_equal(r_off.cpu().numpy(), off)
+    np.testing.assert_array_equal(r_col.cpu().numpy(), col)
+
+
+def test_dataset_round_trip_at_size(cuda, bale, tmp_path):
+    off, col = bale.gen_rmat_dev(18, 16, 0.57, 0.19, 0.19, 29)
+    n = off.numel() - 1
+    for writers in (1, 5):
+        out = tmp_path / f"ds{writers}"
+        bale.write_sparse_matrix_dev(out, off, col, n, nwriters=writers)
+        r_off, r_col, nc = bale.read_sparse_matrix_dev(out)
+        assert nc == n
+        assert torch_equal(r_off, off) and torch_equal(r_col, col)
+
+
+def torch_equal(a, b) -> bool:
+    import torch
+
+    return a.shape == b.shape and bool(torch.equal(a, b))
+
+
+def test_dataset_empty_and_tiny(cuda, bale, tmp_path):
+    off = np.zeros(4, np.int64)
+    bale.write_sparse_matrix_dev(tmp_path / "e", _dev(off, cuda), _dev(np.zeros(1, np.int64), cuda)[:0], 3,
+                                 nwriters=5)
+    r_off, r_col, nc = bale.read_sparse_matrix_dev(tmp_path / "e")
+    assert nc == 3 and r_col.numel() == 0
+    np.testing.assert_array_equal(r_off.cpu().numpy(), off)
+
+
+def _write_ds(tmp_path, meta, rowcnts, nonzeros):
+    out = tmp_path / "bad"
+    out.mkdir(exist_ok=True)
+    (out / "metadata").write_text("".join(f"{v}\n" for v in meta))
+    for w, (r, z) in enumerate(zip(rowcnts, nonzeros)):
+        np.asarray(r, np.int64).tofile(out / f"rowcnt_{w}")
+        np.asarray(z, np.int64).tofile(out / f"nonzero_{w}")
+    return out
+
+
+@pytest.mark.parametrize("case", [
+    ((3, 4, 3, 1), [[1, 1, 1]], [[0, 1]]),                # one column short
+    ((3, 4, 3, 1), [[1, 1]], [[0, 1, 2]]),                # one row length short
+    ((3, 4, 3, 1), [[1, -1, 3]], [[0, 1, 2]]),            # a negative length
+    ((3, 4, 3, 1), [[1, 1, 1]], [[0, 4, 2]]),             # a column past numcols
+    ((3, 4, 3, 1), [[1, 1, 1]], [[0, -1, 2]]),            # a negative column
+    ((4, 4, 4, 2), [[2, 1], [0, 1]], [[0, 1], [2, 3]]),   # lengths of writer 0 run into writer 1's columns
+    ((3, 4, 3, 2), [[1, 1, 1], []], [[0, 1, 2], []]),     # writer blocks of the wrong sizes
+])
+def test_dataset_malformed_is_an_error(cuda, bale, tmp_path, case):
+    out = _write_ds(tmp_path, *case)
+    with pytest.raises(bale.BaleError):
+        bale.read_sparse_matrix_dev(out)
+
+
+def test_dataset_missing_file_and_bad_csr(cuda, bale, tmp_path):
+    out = _write_ds(tmp_path, (2, 2, 1, 2), [[1], [0]], [[0], []])
+    (out / "nonzero_1").unlink()
+    with pytest.raises(bale.BaleError):
+        bale.read_sparse_matrix_dev(out)
+    with pytest.raises(bale.BaleError):
+        bale.write_sparse_matrix_dev(tmp_path / "w", _dev(np.array([0, 2, 1], np.int64), cuda),
+                                     _dev(np.array([0, 1], np.int64), cuda), 2)
+    with pytest.raises(bale.BaleError):
+        bale.write_sparse_matrix_dev(tmp_path / "w", _dev(np.array([0, 1, 2], np.int64), cuda),
+                                     _dev(np.array([0, 2], np.int64), cuda), 2)

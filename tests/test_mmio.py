@@ -1,5 +1,6 @@
-"""MatrixMarket files (host side): the writer produces the reference's bytes,
-the header reader takes what the reference's reader takes."""
+"""MatrixMarket files and binary datasets (host side): the writers produce
+the reference's bytes, the header readers take what the reference's readers
+take."""
 from __future__ import annotations
 
 from pathlib import Path
@@ -33,3 +34,39 @@ def test_header_reader(bale, tmp_path):
             bale.mm_header(p)
     with pytest.raises(bale.BaleError):
         bale.mm_header(tmp_path / "missing.mm")
+
+
+DS_FILES = ("metadata", "rowcnt_0", "nonzero_0")
+
+
+@pytest.mark.parametrize("tag", ["rmat8_lower", "rect_300x517"])
+def test_dataset_writer_matches_reference_bytes(bale, golden, tmp_path, tag):
+    d = golden("spmat")
+    L = bale.SparseMatrix(d[f"{tag}/offset"], d[f"{tag}/nonzero"], int(d[f"{tag}/numcols"][0]))
+    out = tmp_path / f"ds_{tag}"
+    bale.write_sparse_matrix(L, out)
+    assert sorted(p.name for p in out.iterdir()) == sorted(DS_FILES)
+    for f in DS_FILES:
+        assert (out / f).read_bytes() == (GOLDEN / f"ds_{tag}" / f).read_bytes(), f
+
+
+@pytest.mark.parametrize("tag", ["rmat8_lower", "rect_300x517"])
+def test_dataset_oracle_matches_reference_bytes(oracle, golden, tmp_path, tag):
+    d = golden("spmat")
+    out = tmp_path / f"ds_{tag}"
+    oracle.write_dataset(d[f"{tag}/offset"], d[f"{tag}/nonzero"], int(d[f"{tag}/numcols"][0]), out)
+    for f in DS_FILES:
+        assert (out / f).read_bytes() == (GOLDEN / f"ds_{tag}" / f).read_bytes(), f
+
+
+def test_dataset_header_reader(bale, tmp_path):
+    assert bale.sparse_matrix_header(GOLDEN / "ds_rmat8_lower") == (256, 256, 2144, 1)
+    assert bale.sparse_matrix_header(GOLDEN / "ds_rect_300x517")[3] == 1
+    (tmp_path / "metadata").write_text("7\n9\n11\n3\n")
+    assert bale.sparse_matrix_header(tmp_path) == (7, 9, 11, 3)
+    for bad in ("7\n9\n11\n", "7\n9\n11\n0\n", "-1\n9\n11\n1\n", "x\n"):
+        (tmp_path / "metadata").write_text(bad)
+        with pytest.raises(bale.BaleError):
+            bale.sparse_matrix_header(tmp_path)
+    with pytest.raises(bale.BaleError):
+        bale.sparse_matrix_header(tmp_path / "missing")

@@ -145,41 +145,79 @@ __global__ void __launch_bounds__(kThreads)
   hist[static_cast<int64_t>(threadIdx.x) * ntiles + blockIdx.x] = cnt[threadIdx.x];
 }
 
-// offs[d * ntiles + t]: where tile t's keys with digit d start in dst.
-__global__ void __launch_bounds__(kThreads)
+// offs[d * ntiles + t]: where tile t's keys with digit d start in dst.  Each
+// warp ranks a contiguous eighth of the tile in index order with warp-private
+// digit counts (no block barrier per round); the warps' counts are scanned
+// per digit, the tile is laid out in shared memory in sorted order, and the
+// threads then write consecutive sorted positions, so each digit's run leaves
+// the block as whole lines.  Stable: within a digit, tile index order.
+constexpr int kWarpSlice = static_cast<int>(kTile) / kWarps;  // 512 keys per warp
+static_assert(kWarpSlice == 32 * kPer, "a warp's slice is kPer rounds of 32");
+
+__global__ void __launch_bounds__(kThreads, 3)
     radix_scatter_kernel(const uint64_t *__restrict__ src, uint64_t *__restrict__ dst, int64_t n, int shift,
                          const uint32_t *__restrict__ offs, int64_t ntiles) {
-  __shared__ uint32_t base[kDigits];
-  __shared__ uint32_t wcnt[kWarps][kDigits];
+  __shared__ uint64_t sorted[kTile];
+  __shared__ uint32_t wcnt[kWarps][kDigits];  // counts per warp, then their exclusive prefix over warps
+  __shared__ uint32_t dstart[kDigits];        // where each digit starts in the sorted tile
+  __shared__ uint32_t gbase[kDigits];         // where it starts in dst
+  __shared__ uint32_t wsum[kWarps];
   const unsigned lane = lane_id(), warp = threadIdx.x >> 5;
-  base[threadIdx.x] = offs[static_cast<int64_t>(threadIdx.x) * ntiles + blockIdx.x];
 #pragma unroll
   for (int w = 0; w < kWarps; w++) wcnt[w][threadIdx.x] = 0;
+  gbase[threadIdx.x] = offs[static_cast<int64_t>(threadIdx.x) * ntiles + blockIdx.x];
   __syncthreads();
   const int64_t tile = static_cast<int64_t>(blockIdx.x) * kTile;
-  for (int r = 0; r < kPer; r++) {
-    const int64_t i = tile + r * kThreads + threadIdx.x;
-    const bool valid = i < n;
-    const uint64_t key = valid ? src[i] : 0ull;
-    const uint32_t d = valid ? static_cast<uint32_t>(key >> shift) & (kDigits - 1) : kDigits;  // kDigits: none
-    const unsigned peers = __match_any_sync(kFull, d);
-    const uint32_t rank = __popc(peers & ((1u << lane) - 1u));
-    if (valid && rank == 0) wcnt[warp][d] = __popc(peers);
-    __syncthreads();
-    if (valid) {
-      uint32_t pre = base[d] + rank;
-      for (unsigned w = 0; w < warp; w++) pre += wcnt[w][d];
-      dst[pre] = key;
-    }
-    __syncthreads();
-    uint32_t t = 0;
+  const int64_t first = tile + static_cast<int64_t>(warp) * kWarpSlice + lane;
+  uint64_t key[kPer];
+  uint32_t dr[kPer];  // digit << 16 | rank among the warp's keys of that digit (kDigits: no key)
 #pragma unroll
-    for (int w = 0; w < kWarps; w++) {
-      t += wcnt[w][threadIdx.x];
-      wcnt[w][threadIdx.x] = 0;
-    }
-    base[threadIdx.x] += t;
-    __syncthreads();
+  for (int r = 0; r < kPer; r++) {
+    const int64_t i = first + r * 32;
+    const bool valid = i < n;
+    key[r] = valid ? src[i] : 0ull;
+    const uint32_t d = valid ? static_cast<uint32_t>(key[r] >> shift) & (kDigits - 1) : kDigits;
+    const unsigned peers = __match_any_sync(kFull, d);
+    const uint32_t below = __popc(peers & ((1u << lane) - 1u));
+    const uint32_t prior = valid ? wcnt[warp][d] : 0u;
+    __syncwarp();
+    if (valid && below == 0) wcnt[warp][d] = prior + __popc(peers);
+    __syncwarp();
+    dr[r] = d << 16 | (prior + below);
+  }
+  __syncthreads();
+  // thread d: digit d's warp prefixes and its count in the tile, then the
+  // exclusive scan of the counts over digits
+  uint32_t cnt = 0;
+#pragma unroll
+  for (int w = 0; w < kWarps; w++) {
+    const uint32_t c = wcnt[w][threadIdx.x];
+    wcnt[w][threadIdx.x] = cnt;
+    cnt += c;
+  }
+  uint32_t inc = cnt;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(kFull, inc, o);
+    if (static_cast<int>(lane) >= o) inc += y;
+  }
+  if (lane == 31) wsum[warp] = inc;
+  __syncthreads();
+  uint32_t before = 0;
+  for (unsigned w = 0; w < warp; w++) before += wsum[w];
+  dstart[threadIdx.x] = before + inc - cnt;
+  __syncthreads();
+#pragma unroll
+  for (int r = 0; r < kPer; r++) {
+    const uint32_t d = dr[r] >> 16;
+    if (d < kDigits) sorted[dstart[d] + wcnt[warp][d] + (dr[r] & 0xffffu)] = key[r];
+  }
+  __syncthreads();
+  const int tile_n = static_cast<int>(n - tile < kTile ? n - tile : kTile);
+  for (int j = threadIdx.x; j < tile_n; j += kThreads) {
+    const uint64_t k = sorted[j];
+    const uint32_t d = static_cast<uint32_t>(k >> shift) & (kDigits - 1);
+    dst[gbase[d] + (j - dstart[d])] = k;
   }
 }
 
@@ -246,14 +284,26 @@ __global__ void __launch_bounds__(256)
   for (int h = threadIdx.x; h < kHubIds; h += 256) hub[h] = 0;
   __syncthreads();
   const uint64_t mask = (uint64_t(1) << S) - 1;
-  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
-  for (int64_t e = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; e < m; e += stride) {
-    if (!flag[e]) continue;
-    const uint64_t k = keys[e];
-    out[pos[e]] = k;
-    const uint64_t a = k >> S, b = k & mask;
-    if (a < kHubIds) atomicAdd(&hub[a], 1u); else atomicAdd(deg + a, 1u);
-    if (b < kHubIds) atomicAdd(&hub[b], 1u); else atomicAdd(deg + b, 1u);
+  const unsigned lane = lane_id();
+  const int64_t warps = static_cast<int64_t>(gridDim.x) * (blockDim.x >> 5);
+  // warp-contiguous runs of 32 sorted keys: the smaller endpoint a repeats
+  // along the run, so its lanes add once per distinct a
+  for (int64_t e0 = (static_cast<int64_t>(blockIdx.x) * (blockDim.x >> 5) + (threadIdx.x >> 5)) * 32; e0 < m;
+       e0 += warps * 32) {
+    const int64_t e = e0 + lane;
+    const bool keep = e < m && flag[e];
+    const uint64_t k = keep ? keys[e] : ~0ull;
+    if (keep) out[pos[e]] = k;
+    const uint64_t a = k >> S;
+    const unsigned peers = __match_any_sync(kFull, a);
+    if (keep && (peers & ((1u << lane) - 1u)) == 0) {
+      const uint32_t c = __popc(peers);
+      if (a < kHubIds) atomicAdd(&hub[a], c); else atomicAdd(deg + a, c);
+    }
+    if (keep) {
+      const uint64_t b = k & mask;
+      if (b < kHubIds) atomicAdd(&hub[b], 1u); else atomicAdd(deg + b, 1u);
+    }
   }
   __syncthreads();
   for (int h = threadIdx.x; h < kHubIds && h < n; h += 256)
@@ -414,7 +464,9 @@ int build_from_keys(Ws &w, int64_t m, int64_t n, int S, int64_t *d_offset, int64
   rc = excl_scan(w.flag, w.pos, m, w.bsum, w.words, st);
   if (rc != BALE_OK) return rc;
   BALE_CUDA_OK(cudaMemsetAsync(w.deg, 0, static_cast<size_t>(n) * 4, st));
-  compact_degree_kernel<<<grid_for(m), 256, 0, st>>>(sorted, m, S, n, w.flag, w.pos, other, w.deg);
+  // few blocks: each flushes its kHubIds shared counters at the end
+  compact_degree_kernel<<<std::min<unsigned>(grid_for(m), num_sms() * 4), 256, 0, st>>>(sorted, m, S, n, w.flag,
+                                                                                    w.pos, other, w.deg);
   unsigned int nu32 = 0;
   BALE_CUDA_OK(cudaMemcpyAsync(&nu32, w.words, 4, cudaMemcpyDeviceToHost, st));
   BALE_CUDA_OK(cudaMemsetAsync(w.words + 1, 0, 4, st));
@@ -556,6 +608,17 @@ __device__ __forceinline__ uint64_t lcg_jump(uint64_t x, uint64_t k) {
 
 __device__ __forceinline__ uint64_t lcg_step(uint64_t x) { return (kLcgA * x + kLcgC) & kLcgMask; }
 
+// The LCG's affine map applied 32 times, x -> kLcgA32 x + kLcgC32 (mod 2^48).
+struct LcgMap {
+  uint64_t a, c;
+};
+constexpr LcgMap lcg_power(int k) {
+  LcgMap m{1, 0};
+  for (int i = 0; i < k; i++) m = {(m.a * kLcgA) & kLcgMask, (m.c * kLcgA + kLcgC) & kLcgMask};
+  return m;
+}
+constexpr LcgMap kLcg32 = lcg_power(32);
+
 // Dart throwing (rand_permp_agi, spmat/spmat_agi.upc:56-107; rand_permp_exstack,
 // spmat/spmat_exstack.upc:62-190).  Throw t lands in slot r_t = lrand48() % m
 // for the lrand48 output number idx(t) = t + lost(t): the exstack form loses
@@ -563,33 +626,37 @@ __device__ __forceinline__ uint64_t lcg_step(uint64_t x) { return (kLcgA * x + k
 // happens in every round before round cap and in none after it, so lost(t) =
 // min(t / per_round, cap) (per_round = 0: nothing is lost).  A throw takes its
 // slot exactly when no earlier throw hit it (a slot, once taken, stays
-// taken), so owner[r] = min{t : r_t = r} decides every throw at once.  Each
-// thread takes a run of kThrowsPerThread consecutive throws.
+// taken), so owner[r] = min{t : r_t = r} decides every throw at once.  A warp
+// takes kThrowsPerThread runs of 32 consecutive throws, lane l throw l of
+// each run: one jump ahead, then the 32-step map (plus a single step per
+// draw lost in between), so the slot stores coalesce.
 constexpr int kThrowsPerThread = 64;
 constexpr int kDartRoundsMax = 4096;
+
+__device__ __forceinline__ int64_t dart_lost(int64_t t, int64_t per_round, int64_t cap) {
+  if (!per_round) return 0;
+  const int64_t k = t / per_round;
+  return k < cap ? k : cap;
+}
 
 __global__ void __launch_bounds__(256)
     dart_slots_kernel(uint64_t x0, int64_t t_begin, int64_t t_end, int64_t per_round, int64_t cap, uint32_t m,
                       uint32_t *__restrict__ slot, uint32_t *__restrict__ owner) {
-  const int64_t first =
-      t_begin + (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) * kThrowsPerThread;
-  if (first >= t_end) return;
-  const int64_t last = first + kThrowsPerThread < t_end ? first + kThrowsPerThread : t_end;
-  int64_t lost = 0, next_full = INT64_MAX;
-  if (per_round) {
-    lost = first / per_round < cap ? first / per_round : cap;
-    next_full = (first / per_round + 1) * per_round;
-  }
-  uint64_t x = lcg_jump(x0, static_cast<uint64_t>(first + lost));
-  for (int64_t t = first; t < last; t++) {
-    if (t == next_full) {  // round t / per_round - 1 lost a draw if it was full
-      if (t / per_round <= cap) x = lcg_step(x);
-      next_full += per_round;
-    }
-    x = lcg_step(x);
-    const uint32_t r = static_cast<uint32_t>(x >> 17) % m;
-    slot[t] = r;
-    atomicMin(&owner[r], static_cast<uint32_t>(t));
+  const int64_t warp = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+  int64_t t = t_begin + warp * (32 * kThrowsPerThread) + lane_id();
+  if (t >= t_end) return;
+  int64_t lost = dart_lost(t, per_round, cap);
+  uint64_t x = lcg_jump(x0, static_cast<uint64_t>(t + lost));
+  for (int r = 0; r < kThrowsPerThread && t < t_end; r++) {
+    const uint64_t y = lcg_step(x);  // output idx(t)
+    const uint32_t s = static_cast<uint32_t>(y >> 17) % m;
+    slot[t] = s;
+    atomicMin(&owner[s], static_cast<uint32_t>(t));
+    t += 32;
+    const int64_t lost2 = dart_lost(t, per_round, cap);
+    x = (kLcg32.a * x + kLcg32.c) & kLcgMask;
+    for (int64_t e = lost; e < lost2; e++) x = lcg_step(x);
+    lost = lost2;
   }
 }
 
@@ -785,8 +852,8 @@ int read_words(const unsigned int *d_words, unsigned int *h, int count, cudaStre
 
 void launch_dart_slots(uint64_t x0, int64_t t_begin, int64_t t_end, int64_t per_round, int64_t cap, int64_t m,
                        const DartWs &w, cudaStream_t st) {
-  const int64_t threads = (t_end - t_begin + kThrowsPerThread - 1) / kThrowsPerThread;
-  dart_slots_kernel<<<static_cast<unsigned>((threads + 255) / 256), 256, 0, st>>>(
+  const int64_t warps = (t_end - t_begin + 32 * kThrowsPerThread - 1) / (32 * kThrowsPerThread);
+  dart_slots_kernel<<<static_cast<unsigned>((warps + 7) / 8), 256, 0, st>>>(
       x0, t_begin, t_end, per_round, cap, static_cast<uint32_t>(m), w.slot, w.owner);
 }
 

@@ -51,6 +51,8 @@ constexpr int kUnroll = 4;        // rounds of 32 nonzeros in flight per warp (s
 constexpr int kHub = 8192;        // labels whose incoming counts and slots live in shared memory
 constexpr int kScanBlocksPerSm = 6;
 constexpr int kFillUnroll = 4;     // the fill's rounds in flight
+constexpr int kProbeInFlight = 5;  // 16-byte prefix vectors per lane in flight when probing
+constexpr int kStagedInFlight = 2; // the same for prefixes probed against staged short rows
 
 // Workspace words: [1] malformed entries seen by the scan.
 enum { kWBad = 1, kWords = 4 };
@@ -381,8 +383,8 @@ struct RowJ {
 // Probes of up to 32 prefixes (lane l holds record l; {0,0} for none; real
 // records have p >= 1) against row j: every element of each prefix
 // row_i[s, s+p) is tested.  The prefixes' 16-byte vectors are flattened over
-// the warp so every lane has a vector whatever the prefix lengths, two
-// vectors per lane in flight.
+// the warp so every lane has a vector whatever the prefix lengths,
+// kProbeInFlight vectors per lane in flight.
 template <bool OVF>
 __device__ __forceinline__ void probe_records(const RowJ<OVF> rj, const uint4 *__restrict__ col4, uint32_t nvec_all,
                                               uint2 rec, unsigned long long &cnt, unsigned long long &wk) {
@@ -394,12 +396,12 @@ __device__ __forceinline__ void probe_records(const RowJ<OVF> rj, const uint4 *_
   const uint32_t tot = __shfl_sync(kFull, inc, 31);
   const uint32_t q = v0 - (inc - nv);  // vector index = q + flattened position
   wk += p;
-  for (uint32_t base = 0; base < tot; base += 64) {
-    uint4 xv[2];
-    uint32_t vi[2], ps[2], pl[2];
-    bool act[2];
+  for (uint32_t base = 0; base < tot; base += 32 * kProbeInFlight) {
+    uint4 xv[kProbeInFlight];
+    uint32_t vi[kProbeInFlight], ps[kProbeInFlight], pl[kProbeInFlight];
+    bool act[kProbeInFlight];
 #pragma unroll
-    for (int h = 0; h < 2; h++) {
+    for (int h = 0; h < kProbeInFlight; h++) {
       const uint32_t bb = base + 32u * h;
       const int o = flat_owner(inc, bb);
       vi[h] = __shfl_sync(kFull, q, o) + bb + lane;
@@ -409,14 +411,15 @@ __device__ __forceinline__ void probe_records(const RowJ<OVF> rj, const uint4 *_
       xv[h] = act[h] ? col4[vi[h]] : make_uint4(0u, 0u, 0u, 0u);
     }
 #pragma unroll
-    for (int h = 0; h < 2; h++)
+    for (int h = 0; h < kProbeInFlight; h++)
       if (act[h]) cnt += rj.test4(xv[h], vi[h] << 2, ps[h], pl[h]);
   }
 }
 
 // Probes of up to 32 prefixes of different rows j (lane l holds record l
 // and the place of its row j in the warp's staging buffer, stg[ro, ro + rl)),
-// each element binary-searched in its staged row; flattened as above.
+// each element binary-searched in its staged row; flattened as above, with
+// kStagedInFlight vectors per lane in flight.
 __device__ __forceinline__ void probe_records_staged(const uint32_t *__restrict__ stg, uint32_t ro, uint32_t rl,
                                                      const uint4 *__restrict__ col4, uint32_t nvec_all, uint2 rec,
                                                      unsigned long long &cnt, unsigned long long &wk) {
@@ -428,19 +431,32 @@ __device__ __forceinline__ void probe_records_staged(const uint32_t *__restrict_
   const uint32_t tot = __shfl_sync(kFull, inc, 31);
   const uint32_t q = v0 - (inc - nv);
   wk += p;
-  for (uint32_t base = 0; base < tot; base += 32) {
-    const int o = flat_owner(inc, base);
-    const uint32_t vi = __shfl_sync(kFull, q, o) + base + lane;
-    const uint32_t ps = __shfl_sync(kFull, s, o), pl = __shfl_sync(kFull, p, o);
-    const uint32_t oro = __shfl_sync(kFull, ro, o), orl = __shfl_sync(kFull, rl, o);
-    if (base + lane < tot && vi < nvec_all) {
-      const uint4 x = col4[vi];
-      const uint32_t e = (vi << 2) - ps;  // wraps for elements before the prefix
-      const uint32_t *r = stg + oro;
-      if (e < pl && search_u32(r, orl, x.x)) cnt++;
-      if (e + 1u < pl && search_u32(r, orl, x.y)) cnt++;
-      if (e + 2u < pl && search_u32(r, orl, x.z)) cnt++;
-      if (e + 3u < pl && search_u32(r, orl, x.w)) cnt++;
+  for (uint32_t base = 0; base < tot; base += 32 * kStagedInFlight) {
+    uint4 xv[kStagedInFlight];
+    uint32_t vi[kStagedInFlight], ps[kStagedInFlight], pl[kStagedInFlight], oro[kStagedInFlight],
+        orl[kStagedInFlight];
+    bool act[kStagedInFlight];
+#pragma unroll
+    for (int h = 0; h < kStagedInFlight; h++) {
+      const uint32_t bb = base + 32u * h;
+      const int o = flat_owner(inc, bb);
+      vi[h] = __shfl_sync(kFull, q, o) + bb + lane;
+      ps[h] = __shfl_sync(kFull, s, o);
+      pl[h] = __shfl_sync(kFull, p, o);
+      oro[h] = __shfl_sync(kFull, ro, o);
+      orl[h] = __shfl_sync(kFull, rl, o);
+      act[h] = bb + lane < tot && vi[h] < nvec_all;
+      xv[h] = act[h] ? col4[vi[h]] : make_uint4(0u, 0u, 0u, 0u);
+    }
+#pragma unroll
+    for (int h = 0; h < kStagedInFlight; h++) {
+      if (!act[h]) continue;
+      const uint32_t e = (vi[h] << 2) - ps[h];  // wraps for elements before the prefix
+      const uint32_t *r = stg + oro[h];
+      if (e < pl[h] && search_u32(r, orl[h], xv[h].x)) cnt++;
+      if (e + 1u < pl[h] && search_u32(r, orl[h], xv[h].y)) cnt++;
+      if (e + 2u < pl[h] && search_u32(r, orl[h], xv[h].z)) cnt++;
+      if (e + 3u < pl[h] && search_u32(r, orl[h], xv[h].w)) cnt++;
     }
   }
 }

@@ -512,19 +512,65 @@ __global__ void __launch_bounds__(256)
   if (lane_id() == 0 && nb) atomicAdd(bad, nb);
 }
 
-// keys[k] = col << rb | row, the row of nonzero k found by a binary search
-// over the (checked) offsets.
+// The lane owning flattened position bb + lane, where lane r covers
+// [inc_r - len_r, inc_r), the inclusive prefixes inc_r strictly increase over
+// the lanes that cover anything and stay at the total beyond them: the lanes
+// ending at or before bb (a ballot) plus those ending inside (bb, bb + lane]
+// (bits of one OR-reduction; the ends are distinct).
+__device__ __forceinline__ int flat_owner64(int64_t inc, int64_t bb) {
+  const unsigned lane = lane_id();
+  const uint32_t a = __popc(__ballot_sync(kFull, inc <= bb));
+  const int64_t x = inc - bb;
+  const uint32_t ends = __reduce_or_sync(kFull, (x > 0 && x < 32) ? (1u << static_cast<uint32_t>(x)) : 0u);
+  const uint32_t o = a + __popc(ends & ((2u << lane) - 1u));
+  return o < 32u ? static_cast<int>(o) : 31;
+}
+
+// keys[k] = col << rb | row for every nonzero of a checked CSR.  A warp
+// takes 32 rows and flattens their nonzeros over its lanes (empty rows
+// dropped, so the prefixes strictly increase): each lane knows its
+// nonzero's row without a search, and the reads and writes coalesce.
 __global__ void __launch_bounds__(256)
     transpose_keys_kernel(const int64_t *__restrict__ off, const int64_t *__restrict__ col, int64_t numrows,
-                          int64_t nnz, int rb, uint64_t *__restrict__ keys) {
-  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
-  for (int64_t k = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; k < nnz; k += stride) {
-    int64_t lo = 0, hi = numrows;  // the last row i with off[i] <= k
-    while (hi - lo > 1) {
-      const int64_t mid = (lo + hi) >> 1;
-      if (off[mid] <= k) lo = mid; else hi = mid;
+                          int rb, uint64_t *__restrict__ keys) {
+  __shared__ longlong2 stage[8][32];
+  const unsigned lane = lane_id(), warp = threadIdx.x >> 5;
+  const int64_t groups = (numrows + 31) / 32;
+  const int64_t warps = static_cast<int64_t>(gridDim.x) * 8;
+  for (int64_t g = static_cast<int64_t>(blockIdx.x) * 8 + warp; g < groups; g += warps) {
+    const int64_t i = g * 32 + lane;
+    int64_t b = 0, d = 0;
+    if (i < numrows) {
+      b = off[i];
+      d = off[i + 1] - b;
     }
-    keys[k] = (static_cast<uint64_t>(col[k]) << rb) | static_cast<uint64_t>(lo);
+    const unsigned live = __ballot_sync(kFull, d > 0);
+    if (d > 0) stage[warp][__popc(live & ((1u << lane) - 1u))] = make_longlong2(b, (d << 5) | lane);
+    __syncwarp();
+    int64_t mb = 0, md = 0, mrow = 0;
+    if (lane < static_cast<unsigned>(__popc(live))) {
+      const longlong2 t = stage[warp][lane];
+      mb = t.x;
+      md = t.y >> 5;
+      mrow = g * 32 + (t.y & 31);
+    }
+    __syncwarp();
+    int64_t inc = md;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int64_t y = __shfl_up_sync(kFull, inc, o);
+      if (static_cast<int>(lane) >= o) inc += y;
+    }
+    const int64_t tot = __shfl_sync(kFull, inc, 31);
+    for (int64_t bb = 0; bb < tot; bb += 32) {
+      const int o = flat_owner64(inc, bb);
+      const int64_t ob = __shfl_sync(kFull, mb, o), ox = __shfl_sync(kFull, inc - md, o);
+      const int64_t orow = __shfl_sync(kFull, mrow, o);
+      if (bb + lane < tot) {
+        const int64_t k = ob + (bb + lane - ox);
+        keys[k] = (static_cast<uint64_t>(col[k]) << rb) | static_cast<uint64_t>(orow);
+      }
+    }
   }
 }
 
@@ -1157,6 +1203,14 @@ std::vector<int64_t> writer_rows(int64_t numrows, int64_t writers) {
   return first;
 }
 
+// Closes a FILE on every return path.
+struct FileGuard {
+  FILE *f;
+  ~FileGuard() {
+    if (f) fclose(f);
+  }
+};
+
 int64_t file_bytes(const char *path) {
   struct stat sb;
   if (stat(path, &sb) != 0 || !S_ISREG(sb.st_mode)) return -1;
@@ -1254,7 +1308,7 @@ int bale_transpose_dev(const int64_t *d_offset, const int64_t *d_nonzero, int64_
   }
   int rc = BALE_OK;
   if (nnz > 0) {
-    transpose_keys_kernel<<<grid_for(nnz), 256, 0, st>>>(d_offset, d_nonzero, numrows, nnz, rb, w.ka);
+    transpose_keys_kernel<<<grid_for(numrows * 32), 256, 0, st>>>(d_offset, d_nonzero, numrows, rb, w.ka);
     BALE_CUDA_OK(cudaGetLastError());
   }
   uint64_t *sk = radix_sort(w.ka, w.kb, nnz, rb + cb, w, st, &rc);
@@ -1350,19 +1404,11 @@ int bale_read_matrix_mm_dev(const char *path, int64_t *d_offset, int64_t *d_nonz
     set_error("bale_read_matrix_mm_dev: cannot read %s", path);
     return BALE_EINPUT;
   }
+  FileGuard guard{fp};
   const int64_t len = static_cast<int64_t>(ftell(fp)) - body;
   if (len < 0 || len >= (int64_t(1) << 32) - 1) {
-    fclose(fp);
     set_error("bale_read_matrix_mm_dev: %s: body of %lld bytes is outside the supported range", path,
               static_cast<long long>(len));
-    return BALE_EINPUT;
-  }
-  std::vector<char> text(static_cast<size_t>(len > 0 ? len : 1));
-  const bool read_ok = fseek(fp, static_cast<long>(body), SEEK_SET) == 0 &&
-                       (len == 0 || fread(text.data(), 1, static_cast<size_t>(len), fp) == static_cast<size_t>(len));
-  fclose(fp);
-  if (!read_ok) {
-    set_error("bale_read_matrix_mm_dev: short read of %s", path);
     return BALE_EINPUT;
   }
   cudaStream_t st = static_cast<cudaStream_t>(stream);
@@ -1399,7 +1445,17 @@ int bale_read_matrix_mm_dev(const char *path, int64_t *d_offset, int64_t *d_nonz
   w.deg = w.newid = nullptr;
   unsigned long long *bad = reinterpret_cast<unsigned long long *>(w.words + 4);
   BALE_CUDA_OK(cudaMemsetAsync(w.words, 0, 64, st));
-  if (len > 0) BALE_CUDA_OK(cudaMemcpyAsync(d_text, text.data(), static_cast<size_t>(len), cudaMemcpyHostToDevice, st));
+  if (len > 0) {  // the body, through the pinned chunks (reads overlap the copies)
+    IoStaging &io = io_staging();
+    std::lock_guard<std::mutex> lock(io.mu);
+    if (io_buffers(io) != BALE_OK) return BALE_ENOMEM;
+    rc = fseek(fp, static_cast<long>(body), SEEK_SET) == 0 ? file_to_dev(io, fp, d_text, static_cast<size_t>(len), st)
+                                                           : BALE_EINPUT;
+  }
+  if (rc != BALE_OK) {
+    set_error("bale_read_matrix_mm_dev: short read of %s", path);
+    return rc;
+  }
   mm_starts_kernel<<<grid_for(ll), 256, 0, st>>>(d_text, len, w.flag);
   rc = excl_scan(w.flag, w.pos, len, w.bsum, w.words, st);
   if (rc != BALE_OK) return rc;

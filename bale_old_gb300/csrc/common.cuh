@@ -71,9 +71,15 @@ int launch_triangle(const int64_t *offset, const int64_t *nonzero, int64_t numro
 // Region-partitioned gather for tables larger than L2 (ig_part.cu).
 size_t ig_part_workspace_bytes(int64_t n, int64_t table_len);
 bool ig_part_supported(int64_t n, int64_t table_len);
+// direct (optional): a device word from launch_ig_skew; when it reads 1 the
+// partitioned kernels return at once and the caller's direct gather runs.
 int launch_ig_partitioned(int64_t *tgt, const int64_t *index, int64_t n, const int64_t *table,
                           int64_t table_len, int shift, unsigned long long *bad, void *ws,
-                          unsigned long long *cursor, cudaStream_t stream);
+                          unsigned long long *cursor, cudaStream_t stream, const unsigned *direct = nullptr);
+// *direct = 1 when a sample of the request stream repeats its table sectors
+// at least repeat_pct percent of the time (a skewed stream).
+int launch_ig_skew(const int64_t *index, int64_t n, int shift, int64_t table_len, int repeat_pct, unsigned *direct,
+                   cudaStream_t stream);
 // Histogram over the same region partition (tables beyond L2).
 size_t histo_part_workspace_bytes(int64_t n, int64_t ncounts);
 int launch_histo_partitioned(int64_t *counts, int64_t ncounts, const int64_t *index, int64_t n, int shift,

@@ -51,11 +51,14 @@ __device__ __forceinline__ int64_t gather_one(const int64_t *__restrict__ table,
   return 0;
 }
 
+// only_if (optional): run only when *only_if is 1 (the skew test chose
+// this gather over the partitioned one).
 template <int UNROLL, int TPOL>
 __global__ void __launch_bounds__(512)
     ig_gather_kernel(int64_t *__restrict__ tgt, const int64_t *__restrict__ index, int64_t n,
                      const int64_t *__restrict__ table, uint64_t tlen, int shift,
-                     unsigned long long *__restrict__ bad) {
+                     unsigned long long *__restrict__ bad, const unsigned *__restrict__ only_if) {
+  if (only_if && !*only_if) return;
   const longlong2 *__restrict__ idx2 = reinterpret_cast<const longlong2 *>(index);
   longlong2 *__restrict__ out2 = reinterpret_cast<longlong2 *>(tgt);
   const uint64_t pol = make_policy<TPOL>();
@@ -128,7 +131,7 @@ __global__ void __launch_bounds__(256)
 }
 
 using IgKernel = void (*)(int64_t *, const int64_t *, int64_t, const int64_t *, uint64_t, int,
-                          unsigned long long *);
+                          unsigned long long *, const unsigned *);
 
 template <int U>
 IgKernel pick_policy(int pol) {
@@ -155,6 +158,33 @@ int g_l2_fetch_set[64];
 
 // Tables well beyond what L2 can hold go through the region-partitioned
 // gather (ig_part.cu) when there are enough requests to amortise its passes.
+namespace {
+
+// The skew test's threshold (knob ig.skew_repeat_pct; 0 turns the test off):
+// the share of sampled requests whose table sector repeats within the sample.
+constexpr int64_t kSkewRepeatPct = 45;
+
+// The direct gather k over n requests, as many blocks as are resident (knob
+// ig.blocks_per_sm overrides) and no more than the work needs.
+int launch_direct(IgKernel k, int threads, int unroll, int64_t *tgt, const int64_t *index, int64_t n,
+                  const int64_t *table, int64_t table_len, int shift, unsigned long long *bad,
+                  const unsigned *only_if, cudaStream_t stream) {
+  int64_t bps = knob("ig.blocks_per_sm");
+  if (bps <= 0) {
+    int occ = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, threads, 0) != cudaSuccess || occ < 1) occ = 1;
+    bps = occ;
+  }
+  const int64_t want = (n / 2 + static_cast<int64_t>(threads) * unroll - 1) / (static_cast<int64_t>(threads) * unroll);
+  const int64_t full = static_cast<int64_t>(num_sms()) * bps;
+  const int blocks = static_cast<int>(want < full ? (want > 0 ? want : 1) : full);
+  k<<<blocks, threads, 0, stream>>>(tgt, index, n, table, static_cast<uint64_t>(table_len), shift, bad, only_if);
+  BALE_CUDA_OK(cudaGetLastError());
+  return BALE_OK;
+}
+
+}  // namespace
+
 bool ig_partition_for(int64_t n, int64_t table_len, const int64_t *tgt, const int64_t *index) {
   const bool aligned = ((reinterpret_cast<uintptr_t>(tgt) | reinterpret_cast<uintptr_t>(index)) & 15) == 0;
   const int64_t mode = knob("ig.mode");
@@ -177,9 +207,20 @@ int launch_ig(int64_t *tgt, const int64_t *index, int64_t n, const int64_t *tabl
   }
   if (ig_partition_for(n, table_len, tgt, index)) {
     void *ws = device_workspace(ig_part_workspace_bytes(n, table_len), stream);
-    unsigned long long *cursor = next_cursor_word();
+    unsigned long long *cursor = next_cursor_word();  // a slot of 4 words: [0] cursor, [1] the skew choice
     if (!ws || !cursor) return BALE_ENOMEM;
-    return launch_ig_partitioned(tgt, index, n, table, table_len, shift, bad, ws, cursor, stream);
+    // Left to the size rule (ig.mode -1), a skewed stream goes to the direct
+    // gather with L1-allocating table loads instead, chosen on the device.
+    int64_t pct = knob("ig.skew_repeat_pct");
+    if (pct < 0) pct = kSkewRepeatPct;
+    if (knob("ig.mode") >= 0 || pct == 0 || pct > 100)
+      return launch_ig_partitioned(tgt, index, n, table, table_len, shift, bad, ws, cursor, stream);
+    unsigned *direct = reinterpret_cast<unsigned *>(cursor + 1);
+    int rc = launch_ig_skew(index, n, shift, table_len, static_cast<int>(pct), direct, stream);
+    if (rc == BALE_OK) rc = launch_ig_partitioned(tgt, index, n, table, table_len, shift, bad, ws, cursor, stream, direct);
+    if (rc != BALE_OK) return rc;
+    return launch_direct(ig_gather_kernel<4, kCached>, 256, 4, tgt, index, n, table, table_len, shift, bad, direct,
+                         stream);
   }
   if (!aligned) {
     int64_t want = (n + 255) / 256, full = static_cast<int64_t>(sms) * 8;
@@ -195,21 +236,8 @@ int launch_ig(int64_t *tgt, const int64_t *index, int64_t n, const int64_t *tabl
   if (pol < 0 || pol > 3) pol = kEvictLast;
   int64_t threads = knob("ig.threads");
   if (threads != 128 && threads != 256 && threads != 512) threads = 256;
-  IgKernel k = pick_kernel(static_cast<int>(unroll), static_cast<int>(pol));
-  int64_t bps = knob("ig.blocks_per_sm");
-  if (bps <= 0) {
-    int occ = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, static_cast<int>(threads), 0) != cudaSuccess || occ < 1)
-      occ = 1;
-    bps = occ;
-  }
-  int64_t want = (n / 2 + threads * unroll - 1) / (threads * unroll);
-  int64_t full = static_cast<int64_t>(sms) * bps;
-  int blocks = static_cast<int>(want < full ? (want > 0 ? want : 1) : full);
-  k<<<blocks, static_cast<int>(threads), 0, stream>>>(tgt, index, n, table,
-                                                       static_cast<uint64_t>(table_len), shift, bad);
-  BALE_CUDA_OK(cudaGetLastError());
-  return BALE_OK;
+  return launch_direct(pick_kernel(static_cast<int>(unroll), static_cast<int>(pol)), static_cast<int>(threads),
+                       static_cast<int>(unroll), tgt, index, n, table, table_len, shift, bad, nullptr, stream);
 }
 
 // One word from device memory to a mapped host word, written by the kernel:

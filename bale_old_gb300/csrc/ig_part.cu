@@ -20,7 +20,15 @@
 //
 // Per request that is ~46 bytes of streaming traffic (8 index + 4+4+4 entry
 // + 8+8 value + 8 output) and the table is read about once, instead of one
-// mostly wasted DRAM line per request.
+// mostly wasted DRAM line per request.  Table reads may allocate in L1: a
+// skewed request stream keeps its hot entries there instead of queueing on
+// their L2 slices.
+//
+// A strongly skewed stream (Zipf-like, most requests on few entries) is
+// better served by the direct gather, whose L1 and L2 keep the hot entries
+// for every request.  ig_skew_kernel samples the index stream and writes the
+// choice to a device word; the three kernels here return at once when it
+// chose the direct gather, and the direct gather returns when it did not.
 #include "common.cuh"
 
 namespace bale {
@@ -69,9 +77,11 @@ __device__ void block_exclusive_scan(uint32_t *a, int m) {
 
 __global__ void __launch_bounds__(kThreads)
     igp_partition_kernel(const int64_t *__restrict__ index, int64_t n, uint64_t tlen, int shift, int nreg,
-                         uint32_t *__restrict__ entries, uint16_t *__restrict__ starts) {
+                         uint32_t *__restrict__ entries, uint16_t *__restrict__ starts,
+                         const unsigned *__restrict__ direct) {
   __shared__ uint32_t hist[kMaxRegions + 2];
   __shared__ __align__(16) uint32_t stage[kChunk];  // read back as uint4
+  if (direct && *direct) return;
   const int64_t c = blockIdx.x;
   const int64_t base = c * kChunk;
   const int len = static_cast<int>(n - base < kChunk ? n - base : kChunk);
@@ -131,10 +141,10 @@ __global__ void __launch_bounds__(kThreads)
     igp_gather_kernel(const uint32_t *__restrict__ entries, const uint16_t *__restrict__ starts,
                       int64_t nchunks, int nreg, const int64_t *__restrict__ table,
                       int64_t *__restrict__ val, unsigned long long *__restrict__ cursor,
-                      unsigned long long *__restrict__ bad) {
+                      unsigned long long *__restrict__ bad, const unsigned *__restrict__ direct) {
+  if (direct && *direct) return;
   const unsigned lane = lane_id();
   const uint64_t ef = policy_evict_first();
-  const uint64_t el = policy_evict_last();
   const int64_t total = static_cast<int64_t>(nreg + 1) * nchunks;
   unsigned long long nbad = 0;
   for (;;) {
@@ -161,7 +171,7 @@ __global__ void __launch_bounds__(kThreads)
             kk[u] = (k + 32 * u < e) ? ld_u32_pol(ent + k + 32 * u, ef) : 0u;
 #pragma unroll
           for (int u = 0; u < 4; u++)
-            v[u] = (k + 32 * u < e) ? ld_s64_pol(reg + (kk[u] >> kCBits), el) : 0;
+            v[u] = (k + 32 * u < e) ? __ldg(reg + (kk[u] >> kCBits)) : 0;  // may allocate in L1
 #pragma unroll
           for (int u = 0; u < 4; u++)
             if (k + 32 * u < e) st_s64_pol(vo + k + 32 * u, v[u], ef);
@@ -215,8 +225,9 @@ __global__ void __launch_bounds__(kThreads)
 
 __global__ void __launch_bounds__(kThreads)
     igp_unpermute_kernel(const uint32_t *__restrict__ entries, const int64_t *__restrict__ val,
-                         int64_t *__restrict__ tgt, int64_t n) {
+                         int64_t *__restrict__ tgt, int64_t n, const unsigned *__restrict__ direct) {
   __shared__ __align__(16) int64_t tile[kChunk];
+  if (direct && *direct) return;
   const int64_t base = static_cast<int64_t>(blockIdx.x) * kChunk;
   const int len = static_cast<int>(n - base < kChunk ? n - base : kChunk);
   const uint64_t ef = policy_evict_first();
@@ -239,6 +250,48 @@ __global__ void __launch_bounds__(kThreads)
     else st_stream(tgt + base + 2 * p, tile[2 * p]);
   }
 }
+
+// Is the request stream skewed enough for the direct gather?  One block
+// samples kSkewSamples indices spread evenly over the stream, inserts their
+// 32-byte table sectors into a shared-memory hash set and counts the samples
+// whose sector was already there.  *direct = 1 when at least repeat_pct
+// percent of them were: Zipf(s) requests over 2^26 entries repeat 0.04%
+// (uniform), 36% (s = 1.01), 55% (s = 1.1) and 83% (s = 1.3) of an
+// 8192-sample, and the direct gather overtakes the partitioned one between
+// 36% and 55%.
+constexpr int kSkewSamples = 8192;
+constexpr int kSkewSlots = 2 * kSkewSamples;  // the set is never more than half full
+constexpr int kSkewThreads = 1024;
+
+__global__ void __launch_bounds__(kSkewThreads)
+    ig_skew_kernel(const int64_t *__restrict__ index, int64_t n, int shift, uint64_t tlen, int repeat_pct,
+                   unsigned *__restrict__ direct) {
+  extern __shared__ uint32_t set[];  // kSkewSlots words (dynamic: above the static limit)
+  __shared__ unsigned repeats;
+  for (int i = threadIdx.x; i < kSkewSlots; i += kSkewThreads) set[i] = 0;
+  if (threadIdx.x == 0) repeats = 0;
+  __syncthreads();
+  const int64_t step = n / kSkewSamples;  // >= 1: callers sample streams of at least kSkewSamples
+  unsigned mine = 0;
+  for (int t = threadIdx.x; t < kSkewSamples; t += kSkewThreads) {
+    const uint64_t k = static_cast<uint64_t>(index[static_cast<int64_t>(t) * step] >> shift);
+    const uint32_t key = k < tlen ? static_cast<uint32_t>(k >> 2) + 1u : 0xffffffffu;  // 0 marks a free slot
+    uint32_t h = (key * 0x9e3779b1u) >> (32 - 14);  // kSkewSlots = 2^14
+    for (int probe = 0; probe < kSkewSlots; probe++) {
+      const uint32_t old = atomicCAS(&set[h], 0u, key);
+      if (old == 0u) break;
+      if (old == key) {
+        mine++;
+        break;
+      }
+      h = (h + 1u) & (kSkewSlots - 1u);
+    }
+  }
+  if (mine) atomicAdd(&repeats, mine);
+  __syncthreads();
+  if (threadIdx.x == 0) *direct = repeats * 100u >= static_cast<unsigned>(repeat_pct) * kSkewSamples ? 1u : 0u;
+}
+static_assert(kSkewSlots == 1 << 14, "the hash takes the top 14 bits");
 
 }  // namespace
 
@@ -270,7 +323,7 @@ int launch_histo_partitioned(int64_t *counts, int64_t ncounts, const int64_t *in
                                                   static_cast<size_t>(nchunks) * kChunk * sizeof(uint32_t));
   BALE_CUDA_OK(cudaMemsetAsync(cursor, 0, sizeof(unsigned long long), stream));
   igp_partition_kernel<<<static_cast<unsigned>(nchunks), kThreads, 0, stream>>>(
-      index, n, static_cast<uint64_t>(ncounts), shift, nreg, entries, starts);
+      index, n, static_cast<uint64_t>(ncounts), shift, nreg, entries, starts, nullptr);
   BALE_CUDA_OK(cudaGetLastError());
   int occ = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, igp_histo_kernel, kThreads, 0) != cudaSuccess || occ < 1)
@@ -289,9 +342,23 @@ bool ig_part_supported(int64_t n, int64_t table_len) {
   return n > 0 && table_len > 0 && table_len <= (int64_t(kMaxRegions) << kRBits);
 }
 
+int launch_ig_skew(const int64_t *index, int64_t n, int shift, int64_t table_len, int repeat_pct, unsigned *direct,
+                   cudaStream_t stream) {
+  if (n < kSkewSamples) {
+    BALE_CUDA_OK(cudaMemsetAsync(direct, 0, sizeof(unsigned), stream));
+    return BALE_OK;
+  }
+  const int smem = kSkewSlots * static_cast<int>(sizeof(uint32_t));
+  BALE_CUDA_OK(cudaFuncSetAttribute(ig_skew_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  ig_skew_kernel<<<1, kSkewThreads, smem, stream>>>(index, n, shift, static_cast<uint64_t>(table_len), repeat_pct,
+                                                    direct);
+  BALE_CUDA_OK(cudaGetLastError());
+  return BALE_OK;
+}
+
 int launch_ig_partitioned(int64_t *tgt, const int64_t *index, int64_t n, const int64_t *table,
                           int64_t table_len, int shift, unsigned long long *bad, void *ws,
-                          unsigned long long *cursor, cudaStream_t stream) {
+                          unsigned long long *cursor, cudaStream_t stream, const unsigned *direct) {
   const int64_t nchunks = (n + kChunk - 1) / kChunk;
   const int nreg = static_cast<int>((table_len + (int64_t(1) << kRBits) - 1) >> kRBits);
   char *p = static_cast<char *>(ws);
@@ -303,7 +370,7 @@ int launch_ig_partitioned(int64_t *tgt, const int64_t *index, int64_t n, const i
 
   BALE_CUDA_OK(cudaMemsetAsync(cursor, 0, sizeof(unsigned long long), stream));
   igp_partition_kernel<<<static_cast<unsigned>(nchunks), kThreads, 0, stream>>>(
-      index, n, static_cast<uint64_t>(table_len), shift, nreg, entries, starts);
+      index, n, static_cast<uint64_t>(table_len), shift, nreg, entries, starts, direct);
   BALE_CUDA_OK(cudaGetLastError());
   int occ = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, igp_gather_kernel, kThreads, 0) != cudaSuccess || occ < 1)
@@ -313,9 +380,9 @@ int launch_ig_partitioned(int64_t *tgt, const int64_t *index, int64_t n, const i
   if (blocks * (kThreads / 32) > warps_needed) blocks = (warps_needed + (kThreads / 32) - 1) / (kThreads / 32);
   if (blocks < 1) blocks = 1;
   igp_gather_kernel<<<static_cast<unsigned>(blocks), kThreads, 0, stream>>>(entries, starts, nchunks, nreg,
-                                                                          table, val, cursor, bad);
+                                                                          table, val, cursor, bad, direct);
   BALE_CUDA_OK(cudaGetLastError());
-  igp_unpermute_kernel<<<static_cast<unsigned>(nchunks), kThreads, 0, stream>>>(entries, val, tgt, n);
+  igp_unpermute_kernel<<<static_cast<unsigned>(nchunks), kThreads, 0, stream>>>(entries, val, tgt, n, direct);
   BALE_CUDA_OK(cudaGetLastError());
   return BALE_OK;
 }

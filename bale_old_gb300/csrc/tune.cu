@@ -21,6 +21,7 @@ struct Knob {
 
 Knob g_knobs[] = {
     {"ig.mode", -1},            // 0 direct gather, 1 region-partitioned gather
+    {"ig.skew_repeat_pct", -1}, // skewed streams to the direct gather: sample repeat share in %, 0 off
     {"ig.part_min_table_bytes", -1},   // automatic partitioning above this table size (96 MiB)
     {"ig.part_min_requests", -1},      // ... with at least this many requests (2^20)
     {"ig.unroll", -1},          // pairs of requests per thread per trip: 1, 2, 4, 8

@@ -185,3 +185,36 @@ def test_pipelined_dropin_bad_index_is_an_error(cuda, bale, small_chunks):
     tgt = np.zeros(n, np.int64)
     bale.ig_agi(tgt, idx, table)
     np.testing.assert_array_equal(tgt, table[idx])
+
+
+# Tables beyond L2 with skewed requests: the skew test on the device picks
+# the direct gather (L1-allocating table loads) or the partitioned one; both
+# must give the same values and bad counts, whatever the choice and however
+# its threshold is set.
+@pytest.mark.parametrize("dist", ["uniform", "zipf1.01", "zipf1.3", "zipf1.3_bad"])
+@pytest.mark.parametrize("pct", [-1, 0, 1, 100])
+def test_skew_switch_matches_oracle(cuda, bale, oracle, dist, pct):
+    import torch
+
+    tsize, n = 1 << 24, (1 << 22) + 5
+    if dist == "uniform":
+        index = bale.gen_uniform(n, tsize, 41)
+    else:
+        index = bale.gen_zipf(n, tsize, 1.3 if dist.startswith("zipf1.3") else 1.01, 42, 43)
+    if dist.endswith("_bad"):
+        index[::4097] = tsize + 7  # out-of-range requests: value 0, counted
+    table = bale.gen_values(tsize, 44)
+    dev = torch.device("cuda:0")
+    t_index, t_table = torch.from_numpy(index).to(dev), torch.from_numpy(table).to(dev)
+    tgt = torch.full((n,), 99, dtype=torch.int64, device=dev)
+    bad = torch.zeros(1, dtype=torch.int64, device=dev)
+    bale.tune_set("ig.skew_repeat_pct", pct)
+    try:
+        bale.ig_dev(tgt, t_index, t_table, bad=bad)
+        torch.cuda.synchronize()
+    finally:
+        bale.tune_set("ig.skew_repeat_pct", -1)
+    ok = index < tsize
+    want = np.where(ok, table[np.where(ok, index, 0)], 0)
+    np.testing.assert_array_equal(tgt.cpu().numpy(), want)
+    assert int(bad.item()) == int((~ok).sum())

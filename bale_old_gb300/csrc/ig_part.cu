@@ -262,6 +262,7 @@ __global__ void __launch_bounds__(kThreads)
 constexpr int kSkewSamples = 8192;
 constexpr int kSkewSlots = 2 * kSkewSamples;  // the set is never more than half full
 constexpr int kSkewThreads = 1024;
+static_assert(kSkewSamples % kSkewThreads == 0, "whole samples per thread");
 
 __global__ void __launch_bounds__(kSkewThreads)
     ig_skew_kernel(const int64_t *__restrict__ index, int64_t n, int shift, uint64_t tlen, int repeat_pct,
@@ -272,9 +273,14 @@ __global__ void __launch_bounds__(kSkewThreads)
   if (threadIdx.x == 0) repeats = 0;
   __syncthreads();
   const int64_t step = n / kSkewSamples;  // >= 1: callers sample streams of at least kSkewSamples
+  constexpr int kPer = kSkewSamples / kSkewThreads;
+  int64_t raw[kPer];
+#pragma unroll
+  for (int r = 0; r < kPer; r++) raw[r] = index[static_cast<int64_t>(threadIdx.x + r * kSkewThreads) * step];
   unsigned mine = 0;
-  for (int t = threadIdx.x; t < kSkewSamples; t += kSkewThreads) {
-    const uint64_t k = static_cast<uint64_t>(index[static_cast<int64_t>(t) * step] >> shift);
+#pragma unroll
+  for (int r = 0; r < kPer; r++) {
+    const uint64_t k = static_cast<uint64_t>(raw[r] >> shift);
     const uint32_t key = k < tlen ? static_cast<uint32_t>(k >> 2) + 1u : 0xffffffffu;  // 0 marks a free slot
     uint32_t h = (key * 0x9e3779b1u) >> (32 - 14);  // kSkewSlots = 2^14
     for (int probe = 0; probe < kSkewSlots; probe++) {

@@ -252,9 +252,9 @@ __global__ void __launch_bounds__(kThreads)
 }
 
 // Is the request stream skewed enough for the direct gather?  One block
-// samples kSkewSamples indices spread evenly over the stream, inserts their
-// 32-byte table sectors into a shared-memory hash set and counts the samples
-// whose sector was already there.  *direct = 1 when at least repeat_pct
+// samples kSkewSamples requests (runs spread evenly over the stream),
+// inserts their 32-byte table sectors into a shared-memory hash set and
+// counts the samples whose sector was already there.  *direct = 1 when at least repeat_pct
 // percent of them were: Zipf(s) requests over 2^26 entries repeat 0.04%
 // (uniform), 36% (s = 1.01), 55% (s = 1.1) and 83% (s = 1.3) of an
 // 8192-sample, and the direct gather overtakes the partitioned one between
@@ -262,7 +262,9 @@ __global__ void __launch_bounds__(kThreads)
 constexpr int kSkewSamples = 8192;
 constexpr int kSkewSlots = 2 * kSkewSamples;  // the set is never more than half full
 constexpr int kSkewThreads = 1024;
-static_assert(kSkewSamples % kSkewThreads == 0, "whole samples per thread");
+constexpr int kSkewRun = 128;                       // consecutive requests per run (1 KiB)
+constexpr int kSkewRuns = kSkewSamples / kSkewRun;  // 64
+static_assert(kSkewSamples % kSkewThreads == 0 && kSkewSamples % kSkewRun == 0, "whole samples");
 
 __global__ void __launch_bounds__(kSkewThreads)
     ig_skew_kernel(const int64_t *__restrict__ index, int64_t n, int shift, uint64_t tlen, int repeat_pct,
@@ -272,11 +274,16 @@ __global__ void __launch_bounds__(kSkewThreads)
   for (int i = threadIdx.x; i < kSkewSlots; i += kSkewThreads) set[i] = 0;
   if (threadIdx.x == 0) repeats = 0;
   __syncthreads();
-  const int64_t step = n / kSkewSamples;  // >= 1: callers sample streams of at least kSkewSamples
+  // kSkewRuns runs of kSkewRun consecutive requests, evenly spaced: whole
+  // lines, so the one block needs few memory transactions
+  const int64_t step = n / kSkewRuns;  // >= kSkewRun: callers sample streams of at least kSkewSamples
   constexpr int kPer = kSkewSamples / kSkewThreads;
   int64_t raw[kPer];
 #pragma unroll
-  for (int r = 0; r < kPer; r++) raw[r] = index[static_cast<int64_t>(threadIdx.x + r * kSkewThreads) * step];
+  for (int r = 0; r < kPer; r++) {
+    const int t = threadIdx.x + r * kSkewThreads;
+    raw[r] = index[static_cast<int64_t>(t / kSkewRun) * step + t % kSkewRun];
+  }
   unsigned mine = 0;
 #pragma unroll
   for (int r = 0; r < kPer; r++) {

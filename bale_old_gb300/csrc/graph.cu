@@ -672,12 +672,18 @@ constexpr LcgMap kLcg32 = lcg_power(32);
 // happens in every round before round cap and in none after it, so lost(t) =
 // min(t / per_round, cap) (per_round = 0: nothing is lost).  A throw takes its
 // slot exactly when no earlier throw hit it (a slot, once taken, stays
-// taken), so owner[r] = min{t : r_t = r} decides every throw at once.  A warp
-// takes kThrowsPerThread runs of 32 consecutive throws, lane l throw l of
-// each run: one jump ahead, then the 32-step map (plus a single step per
-// draw lost in between), so the slot stores coalesce.
+// taken), so owner[r] = min{t : r_t = r} decides every throw at once.
+//
+// The owner and target arrays hold 2n words (512 MB at n = 2^26), far beyond
+// L2, and the throws land at random.  So the throws become keys slot << tb |
+// t, one stable radix pass groups them by slot region (2^kDartRegionBits
+// slots, 64 MiB of owner), and the passes that touch owner and target sweep
+// the keys in that order: at any time the GPU works on one or two regions,
+// whose slices stay in L2.  The hits are bits of a bitmap (12.5 MB at
+// 2^26, L2-resident); S(t), the hits before throw t, is a prefix count of it.
 constexpr int kThrowsPerThread = 64;
 constexpr int kDartRoundsMax = 4096;
+constexpr int kDartRegionBits = 22;
 
 __device__ __forceinline__ int64_t dart_lost(int64_t t, int64_t per_round, int64_t cap) {
   if (!per_round) return 0;
@@ -685,9 +691,19 @@ __device__ __forceinline__ int64_t dart_lost(int64_t t, int64_t per_round, int64
   return k < cap ? k : cap;
 }
 
+// The slot of throw t, alone (one jump ahead).
+__device__ __forceinline__ uint32_t dart_slot(uint64_t x0, int64_t t, int64_t per_round, int64_t cap, uint32_t m) {
+  const uint64_t x = lcg_jump(x0, static_cast<uint64_t>(t + dart_lost(t, per_round, cap)));
+  return static_cast<uint32_t>(lcg_step(x) >> 17) % m;
+}
+
+// keys[t - t_begin] = r_t << tb | t for throws [t_begin, t_end).  A warp
+// takes kThrowsPerThread runs of 32 consecutive throws, lane l throw l of
+// each run: one jump ahead, then the 32-step map (plus a single step per
+// draw lost in between), so the key stores coalesce.
 __global__ void __launch_bounds__(256)
-    dart_slots_kernel(uint64_t x0, int64_t t_begin, int64_t t_end, int64_t per_round, int64_t cap, uint32_t m,
-                      uint32_t *__restrict__ slot, uint32_t *__restrict__ owner) {
+    dart_keys_kernel(uint64_t x0, int64_t t_begin, int64_t t_end, int64_t per_round, int64_t cap, uint32_t m, int tb,
+                     uint64_t *__restrict__ keys) {
   const int64_t warp = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
   int64_t t = t_begin + warp * (32 * kThrowsPerThread) + lane_id();
   if (t >= t_end) return;
@@ -695,9 +711,7 @@ __global__ void __launch_bounds__(256)
   uint64_t x = lcg_jump(x0, static_cast<uint64_t>(t + lost));
   for (int r = 0; r < kThrowsPerThread && t < t_end; r++) {
     const uint64_t y = lcg_step(x);  // output idx(t)
-    const uint32_t s = static_cast<uint32_t>(y >> 17) % m;
-    slot[t] = s;
-    atomicMin(&owner[s], static_cast<uint32_t>(t));
+    keys[t - t_begin] = (static_cast<uint64_t>(static_cast<uint32_t>(y >> 17) % m) << tb) | static_cast<uint64_t>(t);
     t += 32;
     const int64_t lost2 = dart_lost(t, per_round, cap);
     x = (kLcg32.a * x + kLcg32.c) & kLcgMask;
@@ -706,61 +720,124 @@ __global__ void __launch_bounds__(256)
   }
 }
 
+// The passes over the region-grouped keys: each block takes kDartKeysPerBlock
+// consecutive keys and blocks start in order, so the GPU's working set moves
+// through the regions one at a time; the keys themselves stream past L2
+// (evict-first) instead of pushing the region's slices out.
+constexpr int kDartKeysPerThread = 16;
+constexpr int64_t kDartKeysPerBlock = 256 * kDartKeysPerThread;
+
+__device__ __forceinline__ uint64_t dart_key(const uint64_t *__restrict__ keys, int64_t i, uint64_t pol) {
+  return static_cast<uint64_t>(ld_s64_pol(reinterpret_cast<const int64_t *>(keys) + i, pol));
+}
+
 __global__ void __launch_bounds__(256)
-    dart_hit_kernel(const uint32_t *__restrict__ slot, const uint32_t *__restrict__ owner, int64_t nthrows,
-                    uint32_t *__restrict__ hit) {
+    dart_claim_kernel(const uint64_t *__restrict__ keys, int64_t nkeys, int tb, uint32_t *__restrict__ owner) {
+  const uint64_t tmask = (uint64_t(1) << tb) - 1, pol = policy_evict_first();
+  const int64_t base = static_cast<int64_t>(blockIdx.x) * kDartKeysPerBlock + threadIdx.x;
+#pragma unroll 4
+  for (int r = 0; r < kDartKeysPerThread; r++) {
+    const int64_t i = base + r * 256;
+    if (i >= nkeys) break;
+    const uint64_t k = dart_key(keys, i, pol);
+    atomicMin(&owner[k >> tb], static_cast<uint32_t>(k & tmask));
+  }
+}
+
+__global__ void __launch_bounds__(256)
+    dart_hitbits_kernel(const uint64_t *__restrict__ keys, int64_t nkeys, int tb, const uint32_t *__restrict__ owner,
+                        uint32_t *__restrict__ bits) {
+  const uint64_t tmask = (uint64_t(1) << tb) - 1, pol = policy_evict_first();
+  const int64_t base = static_cast<int64_t>(blockIdx.x) * kDartKeysPerBlock + threadIdx.x;
+#pragma unroll 4
+  for (int r = 0; r < kDartKeysPerThread; r++) {
+    const int64_t i = base + r * 256;
+    if (i >= nkeys) break;
+    const uint64_t k = dart_key(keys, i, pol);
+    const uint32_t t = static_cast<uint32_t>(k & tmask);
+    if (owner[k >> tb] == t) atomicOr(&bits[t >> 5], 1u << (t & 31));
+  }
+}
+
+__global__ void __launch_bounds__(256)
+    dart_popc_kernel(const uint32_t *__restrict__ bits, int64_t nwords, uint32_t *__restrict__ pc) {
   const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
-  for (int64_t t = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; t < nthrows; t += stride)
-    hit[t] = owner[slot[t]] == static_cast<uint32_t>(t) ? 1u : 0u;
+  for (int64_t w = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; w < nwords; w += stride)
+    pc[w] = __popc(bits[w]);
+}
+
+__device__ __forceinline__ bool dart_hit(const uint32_t *__restrict__ bits, int64_t t) {
+  return (bits[t >> 5] >> (t & 31)) & 1u;
+}
+
+// S(t): the hits among throws [0, t).
+__device__ __forceinline__ int64_t dart_S(const uint32_t *__restrict__ bits, const uint32_t *__restrict__ wpre,
+                                          int64_t t) {
+  return static_cast<int64_t>(wpre[t >> 5]) + __popc(bits[t >> 5] & ((1u << (t & 31)) - 1u));
 }
 
 // rand_permp_agi: dart i is thrown until it hits, so the hit of throw t
-// carries dart S[t] (the hits before t); only the first n hits are thrown.
+// carries dart S(t); only the first n hits are thrown.
 __global__ void __launch_bounds__(256)
-    dart_place_agi_kernel(const uint32_t *__restrict__ slot, const uint32_t *__restrict__ hit,
-                          const uint32_t *__restrict__ S, int64_t nthrows, uint32_t n, uint32_t *__restrict__ target) {
-  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
-  for (int64_t t = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; t < nthrows; t += stride)
-    if (hit[t] && S[t] < n) target[slot[t]] = S[t];
+    dart_place_agi_kernel(const uint64_t *__restrict__ keys, int64_t nkeys, int tb, const uint32_t *__restrict__ bits,
+                          const uint32_t *__restrict__ wpre, int64_t n, uint32_t *__restrict__ target) {
+  const uint64_t tmask = (uint64_t(1) << tb) - 1, pol = policy_evict_first();
+  const int64_t base = static_cast<int64_t>(blockIdx.x) * kDartKeysPerBlock + threadIdx.x;
+#pragma unroll 4
+  for (int r = 0; r < kDartKeysPerThread; r++) {
+    const int64_t i = base + r * 256;
+    if (i >= nkeys) break;
+    const uint64_t k = dart_key(keys, i, pol);
+    const int64_t t = static_cast<int64_t>(k & tmask);
+    if (!dart_hit(bits, t)) continue;
+    const int64_t d = dart_S(bits, wpre, t);
+    if (d < n) target[k >> tb] = static_cast<uint32_t>(d);
+  }
 }
 
 // rand_permp_exstack throws rounds of per_round darts while more than
 // per_round are pending; the first round k* that finds at most per_round
-// pending starts at throw k* per_round: the first k with S[k per_round] >=
+// pending starts at throw k* per_round: the first k with S(k per_round) >=
 // n - per_round.  words[1] = k*, or ~0u when the throws so far fall short.
-__global__ void dart_kstar_kernel(const uint32_t *__restrict__ S, int64_t nthrows, int64_t per_round, int64_t n,
-                                  unsigned int *__restrict__ words) {
+__global__ void dart_kstar_kernel(const uint32_t *__restrict__ bits, const uint32_t *__restrict__ wpre,
+                                  int64_t nthrows, int64_t per_round, int64_t n, unsigned int *__restrict__ words) {
   if (threadIdx.x | blockIdx.x) return;
   const int64_t need = n - per_round;
-  int64_t lo = 0, hi = nthrows / per_round;  // S[hi per_round] reaches need; find the first k that does
-  if (static_cast<int64_t>(S[hi * per_round]) < need) {
+  int64_t lo = 0, hi = nthrows / per_round;  // S(hi per_round) reaches need; find the first k that does
+  if (dart_S(bits, wpre, hi * per_round) < need) {
     words[1] = ~0u;
     return;
   }
   while (lo < hi) {
     const int64_t mid = lo + (hi - lo) / 2;
-    if (static_cast<int64_t>(S[mid * per_round]) >= need) hi = mid;
+    if (dart_S(bits, wpre, mid * per_round) >= need) hi = mid;
     else lo = mid + 1;
   }
   words[1] = static_cast<unsigned int>(lo);
 }
 
 // Throws from t0 on are drawn again for the rounds from k* on (no draw is
-// lost there): forget them.
-__global__ void __launch_bounds__(256) dart_forget_kernel(uint32_t *__restrict__ owner, int64_t m, uint32_t t0) {
+// lost there): forget their claims and hits.
+__global__ void __launch_bounds__(256)
+    dart_forget_kernel(uint32_t *__restrict__ owner, int64_t m, uint32_t t0, uint32_t *__restrict__ bits,
+                       int64_t nwords) {
   const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
-  for (int64_t s = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; s < m; s += stride)
-    if (owner[s] != ~0u && owner[s] >= t0) owner[s] = ~0u;
+  const int64_t w0 = t0 >> 5;
+  for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < m || i < nwords; i += stride) {
+    if (i < m && owner[i] != ~0u && owner[i] >= t0) owner[i] = ~0u;
+    if (i >= w0 && i < nwords) bits[i] &= i == w0 ? (1u << (t0 & 31)) - 1u : 0u;
+  }
 }
 
 // The rounds from k* on throw every pending dart: round q starts at
 // rstart[q] with as many throws as darts were pending.  words[2] = the end
 // of the last round, words[3] = the round count, words[4] = 0 (done), 1
 // (more throws needed) or 2 (more than kDartRoundsMax rounds).
-__global__ void dart_rounds_kernel(const uint32_t *__restrict__ S, int64_t nthrows, int64_t t0, int64_t n,
-                                   uint32_t *__restrict__ rstart, unsigned int *__restrict__ words) {
+__global__ void dart_rounds_kernel(const uint32_t *__restrict__ bits, const uint32_t *__restrict__ wpre,
+                                   int64_t nthrows, int64_t t0, int64_t n, uint32_t *__restrict__ rstart,
+                                   unsigned int *__restrict__ words) {
   if (threadIdx.x | blockIdx.x) return;
-  int64_t start = t0, size = n - static_cast<int64_t>(S[t0]);
+  int64_t start = t0, size = n - dart_S(bits, wpre, t0);
   int q = 0;
   while (size > 0) {
     if (start + size > nthrows) {
@@ -772,7 +849,7 @@ __global__ void dart_rounds_kernel(const uint32_t *__restrict__ S, int64_t nthro
       return;
     }
     rstart[q++] = static_cast<uint32_t>(start);
-    const int64_t hits = static_cast<int64_t>(S[start + size]) - static_cast<int64_t>(S[start]);
+    const int64_t hits = dart_S(bits, wpre, start + size) - dart_S(bits, wpre, start);
     start += size;
     size -= hits;
   }
@@ -787,20 +864,20 @@ __global__ void dart_rounds_kernel(const uint32_t *__restrict__ S, int64_t nthro
 // in front of the unthrown darts, so the missed dart of rank r (of ms) is
 // thrown next at position ms - 1 - r of the following round, and the rest
 // of that round throws new darts in order.  Rounds before k* are per_round
-// throws from k per_round; with Rj(k) = k per_round - S[k per_round] darts
+// throws from k per_round; with Rj(k) = k per_round - S(k per_round) darts
 // sent back before round k, round k opens with Rj(k) - Rj(k-1) returned
 // darts and continues with new darts from k per_round - Rj(k-1) on.  From
 // k* on the rounds are rstart[0..nrounds].  Each thread that throws a new
-// dart follows it to its hit and records it in the slot.  words[5] counts
-// chains that ran past the last round (none, for consistent inputs).
+// dart follows it to its hit and records it in the slot (found again from
+// the generator).  words[5] counts chains that ran past the last round
+// (none, for consistent inputs).
 __global__ void __launch_bounds__(256)
-    dart_chase_kernel(const uint32_t *__restrict__ slot, const uint32_t *__restrict__ hit,
-                      const uint32_t *__restrict__ S, int64_t per_round, int64_t kstar,
-                      const uint32_t *__restrict__ rstart, int nrounds, uint32_t *__restrict__ target,
-                      unsigned int *__restrict__ words) {
+    dart_chase_kernel(uint64_t x0, uint32_t m, const uint32_t *__restrict__ bits, const uint32_t *__restrict__ wpre,
+                      int64_t per_round, int64_t kstar, const uint32_t *__restrict__ rstart, int nrounds,
+                      uint32_t *__restrict__ target, unsigned int *__restrict__ words) {
   const int64_t t0 = kstar * per_round, tend = rstart[nrounds], t1 = rstart[1];
   auto sent_back = [&](int64_t k) -> int64_t {  // Rj(k)
-    return k <= 0 ? 0 : k * per_round - static_cast<int64_t>(S[k * per_round]);
+    return k <= 0 ? 0 : k * per_round - dart_S(bits, wpre, k * per_round);
   };
   const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
   for (int64_t t = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; t < tend; t += stride) {
@@ -818,7 +895,7 @@ __global__ void __launch_bounds__(256)
     if (j < back) continue;
     const uint32_t dart = static_cast<uint32_t>(k * per_round - before + j - back);
     int64_t cur = t;
-    while (!hit[cur]) {
+    while (!dart_hit(bits, cur)) {
       int64_t s, s2;
       if (cur < t0) {
         s = cur / per_round * per_round;
@@ -833,8 +910,8 @@ __global__ void __launch_bounds__(256)
         s = rstart[lo];
         s2 = rstart[lo + 1];
       }
-      const int64_t ss = S[s], missed = (s2 - s) - (static_cast<int64_t>(S[s2]) - ss);
-      const int64_t rank = (cur - static_cast<int64_t>(S[cur])) - (s - ss);
+      const int64_t ss = dart_S(bits, wpre, s), missed = (s2 - s) - (dart_S(bits, wpre, s2) - ss);
+      const int64_t rank = (cur - dart_S(bits, wpre, cur)) - (s - ss);
       const int64_t nc = s2 + missed - 1 - rank;  // in [s2, s2 + missed) when consistent
       cur = nc < s2 ? tend : nc;
       if (cur >= tend) break;
@@ -843,7 +920,7 @@ __global__ void __launch_bounds__(256)
       atomicAdd(&words[5], 1u);
       continue;
     }
-    target[slot[cur]] = dart;
+    target[dart_slot(x0, cur, per_round, kstar, m)] = dart;
   }
 }
 
@@ -865,27 +942,37 @@ __global__ void __launch_bounds__(256)
 
 // ---------------------------------------------------------------- random permutations (host)
 struct DartWs {
-  uint32_t *owner, *target, *pos, *slot, *hit, *S, *bsum, *rstart;
+  uint64_t *ka, *kb;                        // keys, and the region pass's output
+  uint32_t *owner, *target, *pos;           // per slot
+  uint32_t *bits, *pc, *wpre;               // hit bits per throw, popcounts and their prefix per word
+  uint32_t *hist, *hoff, *bsum, *rstart;    // radix pass, scans, rounds
   unsigned int *words;  // [0] scan total, [1] k*, [2] last throw, [3] rounds, [4] rounds status, [5] lost chains
 };
 
-size_t dart_ws(int64_t m, int64_t cap, DartWs *w, char *base) {
-  const int64_t nb = (std::max(m, cap) + 1 + kScanBlock - 1) / kScanBlock + 1;
+size_t dart_ws(int64_t m, int64_t nkeys, int64_t nbits, DartWs *w, char *base) {
+  const int64_t tiles = (nkeys + kTile - 1) / kTile;
+  const int64_t nwords = (nbits >> 5) + 2;
+  const int64_t scan_n = std::max(std::max(m, nwords), tiles * kDigits) + 1;
+  const int64_t nb = (scan_n + kScanBlock - 1) / kScanBlock + 1;
   size_t o = 0;
-  auto take = [&](size_t bytes) -> uint32_t * {
+  auto take = [&](size_t bytes) -> char * {
     const size_t at = o;
     o += up256(bytes);
-    return base ? reinterpret_cast<uint32_t *>(base + at) : nullptr;
+    return base ? base + at : nullptr;
   };
-  uint32_t *p;
-  p = take(4 * m); if (w) w->owner = p;
-  p = take(4 * m); if (w) w->target = p;
-  p = take(4 * m); if (w) w->pos = p;
-  p = take(4 * cap); if (w) w->slot = p;
-  p = take(4 * (cap + 1)); if (w) w->hit = p;
-  p = take(4 * (cap + 1)); if (w) w->S = p;
-  p = take(4 * nb); if (w) w->bsum = p;
-  p = take(4 * (kDartRoundsMax + 1)); if (w) w->rstart = p;
+  char *p;
+  p = take(8 * nkeys); if (w) w->ka = reinterpret_cast<uint64_t *>(p);
+  p = take(8 * nkeys); if (w) w->kb = reinterpret_cast<uint64_t *>(p);
+  p = take(4 * m); if (w) w->owner = reinterpret_cast<uint32_t *>(p);
+  p = take(4 * m); if (w) w->target = reinterpret_cast<uint32_t *>(p);
+  p = take(4 * m); if (w) w->pos = reinterpret_cast<uint32_t *>(p);
+  p = take(4 * nwords); if (w) w->bits = reinterpret_cast<uint32_t *>(p);
+  p = take(4 * (nwords + 1)); if (w) w->pc = reinterpret_cast<uint32_t *>(p);
+  p = take(4 * (nwords + 1)); if (w) w->wpre = reinterpret_cast<uint32_t *>(p);
+  p = take(4 * tiles * kDigits); if (w) w->hist = reinterpret_cast<uint32_t *>(p);
+  p = take(4 * tiles * kDigits); if (w) w->hoff = reinterpret_cast<uint32_t *>(p);
+  p = take(4 * nb); if (w) w->bsum = reinterpret_cast<uint32_t *>(p);
+  p = take(4 * (kDartRoundsMax + 1)); if (w) w->rstart = reinterpret_cast<uint32_t *>(p);
   p = take(64); if (w) w->words = reinterpret_cast<unsigned int *>(p);
   return o;
 }
@@ -896,18 +983,40 @@ int read_words(const unsigned int *d_words, unsigned int *h, int count, cudaStre
   return BALE_OK;
 }
 
-void launch_dart_slots(uint64_t x0, int64_t t_begin, int64_t t_end, int64_t per_round, int64_t cap, int64_t m,
-                       const DartWs &w, cudaStream_t st) {
-  const int64_t warps = (t_end - t_begin + 32 * kThrowsPerThread - 1) / (32 * kThrowsPerThread);
-  dart_slots_kernel<<<static_cast<unsigned>((warps + 7) / 8), 256, 0, st>>>(
-      x0, t_begin, t_end, per_round, cap, static_cast<uint32_t>(m), w.slot, w.owner);
+// Keys of throws [t_begin, t_end) grouped by slot region (stable); returns
+// the buffer holding them (w.ka or w.kb).
+uint64_t *dart_region_keys(uint64_t x0, int64_t t_begin, int64_t t_end, int64_t per_round, int64_t cap, int64_t m,
+                           int tb, DartWs &w, cudaStream_t st, int *rc) {
+  *rc = BALE_OK;
+  const int64_t nk = t_end - t_begin;
+  const int64_t warps = (nk + 32 * kThrowsPerThread - 1) / (32 * kThrowsPerThread);
+  dart_keys_kernel<<<static_cast<unsigned>((warps + 7) / 8), 256, 0, st>>>(x0, t_begin, t_end, per_round, cap,
+                                                                           static_cast<uint32_t>(m), tb, w.ka);
+  if (m <= (int64_t(1) << kDartRegionBits) || nk <= 1) return w.ka;  // one region: its slices fit in L2 as they are
+  Ws rw;
+  rw.hist = w.hist;
+  rw.hoff = w.hoff;
+  rw.bsum = w.bsum;
+  rw.words = w.words;
+  const int64_t tiles = (nk + kTile - 1) / kTile;
+  const int shift = tb + kDartRegionBits;  // at most 2^(31-24) regions: one 8-bit pass
+  radix_hist_kernel<<<static_cast<unsigned>(tiles), kThreads, 0, st>>>(w.ka, nk, shift, rw.hist, tiles);
+  *rc = excl_scan(rw.hist, rw.hoff, tiles * kDigits, rw.bsum, rw.words, st);
+  if (*rc != BALE_OK) return w.ka;
+  radix_scatter_kernel<<<static_cast<unsigned>(tiles), kThreads, 0, st>>>(w.ka, w.kb, nk, shift, rw.hoff, tiles);
+  if (cudaGetLastError() != cudaSuccess) *rc = BALE_ECUDA;
+  return w.kb;
 }
 
-// hit[t] for t < nthrows and S = their exclusive prefix, S[nthrows] = total.
-int dart_hits(int64_t nthrows, const DartWs &w, cudaStream_t st) {
-  dart_hit_kernel<<<grid_for(nthrows), 256, 0, st>>>(w.slot, w.owner, nthrows, w.hit);
-  BALE_CUDA_OK(cudaMemsetAsync(w.hit + nthrows, 0, 4, st));
-  return excl_scan(w.hit, w.S, nthrows + 1, w.bsum, w.words, st);
+// The hit bits of the keys' throws set in w.bits, then S: wpre[w] = hits in
+// words [0, w) (wpre[nwords] = all of them, also in words[0]).
+int dart_claims(const uint64_t *keys, int64_t nk, int tb, int64_t nwords, DartWs &w, cudaStream_t st) {
+  const unsigned blocks = static_cast<unsigned>((nk + kDartKeysPerBlock - 1) / kDartKeysPerBlock);
+  dart_claim_kernel<<<blocks, 256, 0, st>>>(keys, nk, tb, w.owner);
+  dart_hitbits_kernel<<<blocks, 256, 0, st>>>(keys, nk, tb, w.owner, w.bits);
+  dart_popc_kernel<<<grid_for(nwords), 256, 0, st>>>(w.bits, nwords, w.pc);
+  BALE_CUDA_OK(cudaMemsetAsync(w.pc + nwords, 0, 4, st));
+  return excl_scan(w.pc, w.wpre, nwords + 1, w.bsum, w.words, st);
 }
 
 // rand_permp_agi (per_round = 0) or rand_permp_exstack with buffers of
@@ -925,40 +1034,46 @@ int rand_perm_darts(int64_t n, uint64_t seed, int64_t per_round, int64_t *d_perm
       nt = (nt + per_round - 1) / per_round * per_round;
       tail = (2 * per_round + 1024) << grow;
     }
-    const int64_t cap = nt + tail;
+    const int64_t cap = nt + tail;  // throws numbered below cap
     if (cap >= int64_t(0xffffffff)) break;
+    int tb = 1;
+    while ((int64_t(1) << tb) < cap + 1) tb++;
+    const int64_t nwords = (cap >> 5) + 2;
     DartWs w;
-    void *ws = device_workspace(dart_ws(m, cap, nullptr, nullptr), st);
+    void *ws = device_workspace(dart_ws(m, std::max(nt, tail), cap, nullptr, nullptr), st);
     if (!ws) return BALE_ENOMEM;
-    dart_ws(m, cap, &w, static_cast<char *>(ws));
+    dart_ws(m, std::max(nt, tail), cap, &w, static_cast<char *>(ws));
     BALE_CUDA_OK(cudaMemsetAsync(w.owner, 0xff, 4 * m, st));
     BALE_CUDA_OK(cudaMemsetAsync(w.target, 0xff, 4 * m, st));
+    BALE_CUDA_OK(cudaMemsetAsync(w.bits, 0, 4 * nwords, st));
     BALE_CUDA_OK(cudaMemsetAsync(w.words, 0, 64, st));
-    launch_dart_slots(x0, 0, nt, per_round, INT64_MAX, m, w, st);
-    int rc = dart_hits(nt, w, st);
-    if (rc != BALE_OK) return rc;
+    int rc = BALE_OK;
+    const uint64_t *keys = dart_region_keys(x0, 0, nt, per_round, INT64_MAX, m, tb, w, st, &rc);
+    if (rc != BALE_OK || (rc = dart_claims(keys, nt, tb, nwords, w, st)) != BALE_OK) return rc;
     unsigned int h[6] = {0, 0, 0, 0, 0, 0};
     if (!per_round) {
       if ((rc = read_words(w.words, h, 1, st)) != BALE_OK) return rc;
       if (static_cast<int64_t>(h[0]) < n) continue;
-      dart_place_agi_kernel<<<grid_for(nt), 256, 0, st>>>(w.slot, w.hit, w.S, nt, static_cast<uint32_t>(n), w.target);
+      dart_place_agi_kernel<<<static_cast<unsigned>((nt + kDartKeysPerBlock - 1) / kDartKeysPerBlock), 256, 0, st>>>(
+          keys, nt, tb, w.bits, w.wpre, n, w.target);
     } else {
-      dart_kstar_kernel<<<1, 32, 0, st>>>(w.S, nt, per_round, n, w.words);
+      dart_kstar_kernel<<<1, 32, 0, st>>>(w.bits, w.wpre, nt, per_round, n, w.words);
       if ((rc = read_words(w.words, h, 2, st)) != BALE_OK) return rc;
       if (h[1] == ~0u) continue;
       const int64_t kstar = h[1], t0 = kstar * per_round, t2 = t0 + tail;
-      dart_forget_kernel<<<grid_for(m), 256, 0, st>>>(w.owner, m, static_cast<uint32_t>(t0));
-      launch_dart_slots(x0, t0, t2, per_round, kstar, m, w, st);
-      if ((rc = dart_hits(t2, w, st)) != BALE_OK) return rc;
-      dart_rounds_kernel<<<1, 32, 0, st>>>(w.S, t2, t0, n, w.rstart, w.words);
+      dart_forget_kernel<<<grid_for(std::max(m, nwords)), 256, 0, st>>>(w.owner, m, static_cast<uint32_t>(t0), w.bits,
+                                                                         nwords);
+      const uint64_t *tk = dart_region_keys(x0, t0, t2, per_round, kstar, m, tb, w, st, &rc);
+      if (rc != BALE_OK || (rc = dart_claims(tk, tail, tb, nwords, w, st)) != BALE_OK) return rc;
+      dart_rounds_kernel<<<1, 32, 0, st>>>(w.bits, w.wpre, t2, t0, n, w.rstart, w.words);
       if ((rc = read_words(w.words, h, 5, st)) != BALE_OK) return rc;
       if (h[4] == 1) continue;
       if (h[4] != 0) {
         set_error("%s: more than %d rounds of returned darts", who, kDartRoundsMax);
         return BALE_EINVAL;
       }
-      dart_chase_kernel<<<grid_for(h[2]), 256, 0, st>>>(w.slot, w.hit, w.S, per_round, kstar, w.rstart,
-                                                        static_cast<int>(h[3]), w.target, w.words);
+      dart_chase_kernel<<<grid_for(h[2]), 256, 0, st>>>(x0, static_cast<uint32_t>(m), w.bits, w.wpre, per_round,
+                                                        kstar, w.rstart, static_cast<int>(h[3]), w.target, w.words);
     }
     dart_taken_kernel<<<grid_for(m), 256, 0, st>>>(w.target, m, w.owner);
     if ((rc = excl_scan(w.owner, w.pos, m, w.bsum, w.words, st)) != BALE_OK) return rc;

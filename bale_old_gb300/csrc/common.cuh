@@ -71,6 +71,12 @@ int launch_triangle(const int64_t *offset, const int64_t *nonzero, int64_t numro
 // Region-partitioned gather for tables larger than L2 (ig_part.cu).
 size_t ig_part_workspace_bytes(int64_t n, int64_t table_len);
 bool ig_part_supported(int64_t n, int64_t table_len);
+// The region partition's layout: each request becomes one u32, its offset in
+// a region of 2^kIgRegionBits table entries above its position in a chunk
+// of 2^kIgChunkBits requests.
+constexpr int kIgChunkBits = 11;
+constexpr int kIgRegionBits = 32 - kIgChunkBits;
+constexpr int64_t kIgMaxRegions = int64_t(1) << (32 - kIgRegionBits);  // tables up to 2^32 entries
 // direct (optional): a device word from launch_ig_skew; when it reads 1 the
 // partitioned kernels return at once and the caller's direct gather runs.
 int launch_ig_partitioned(int64_t *tgt, const int64_t *index, int64_t n, const int64_t *table,

@@ -175,7 +175,7 @@ int histo_mode_for(int64_t n, int64_t ncounts, const int64_t *index) {
   }
   if (mode == 0 && ncounts > kSmemMaxCounters) mode = 2;
   if (!aligned && (mode == 0 || mode == 3)) mode = 2;
-  if (mode == 3 && ncounts > (int64_t(1024) << 22)) mode = 2;
+  if (mode == 3 && ncounts > (kIgMaxRegions << kIgRegionBits)) mode = 2;
   return static_cast<int>(mode);
 }
 

@@ -34,12 +34,12 @@ namespace bale {
 namespace {
 
 constexpr int64_t kNoAllocMaxRequests = int64_t(1) << 18;       // per call
-constexpr int64_t kNoAllocMaxTable = int64_t(1024) << 22;        // 2^32 entries (1024 regions)
-constexpr int64_t kChunk = 1024;                                  // requests per partition chunk
-constexpr int64_t kMaxChunks = kNoAllocMaxRequests / kChunk;      // 256
+constexpr int64_t kNoAllocMaxTable = kIgMaxRegions << kIgRegionBits;  // 2^32 entries
+constexpr int64_t kChunk = int64_t(1) << kIgChunkBits;            // requests per partition chunk
+constexpr int64_t kMaxChunks = kNoAllocMaxRequests / kChunk;      // 128
 constexpr size_t kEntriesBytes = kNoAllocMaxRequests * sizeof(uint32_t);
 constexpr size_t kValuesBytes = kNoAllocMaxRequests * sizeof(int64_t);
-constexpr size_t kStartsBytes = ((kMaxChunks * (1024 + 2) * sizeof(uint16_t)) + 255) & ~size_t(255);
+constexpr size_t kStartsBytes = ((kMaxChunks * (kIgMaxRegions + 2) * sizeof(uint16_t)) + 255) & ~size_t(255);
 constexpr size_t kWordsOffset = kEntriesBytes + kValuesBytes + kStartsBytes;
 constexpr size_t kScratchBytes = kWordsOffset + 256;  // [0] work cursor, [1] discarded bad count
 

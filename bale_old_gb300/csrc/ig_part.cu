@@ -8,9 +8,9 @@
 // reply back.  Here the "PEs" are L2-sized regions of the table and the
 // exchange happens through HBM in three coalesced passes:
 //
-//  1. partition: each 1024-request chunk is counting-sorted in shared memory
-//     by region (region = 2^22 entries = 32 MiB).  Each request becomes one
-//     u32 (offset in its region << 10 | position in its chunk), written back
+//  1. partition: each 2048-request chunk is counting-sorted in shared memory
+//     by region (region = 2^21 entries = 16 MiB).  Each request becomes one
+//     u32 (offset in its region << 11 | position in its chunk), written back
 //     grouped by region, plus the chunk's region boundaries (u16);
 //  2. gather: (region, chunk) segments are processed region-major, so at any
 //     time the whole GPU reads one region, which stays resident in L2; the
@@ -36,10 +36,12 @@ namespace bale {
 namespace {
 
 constexpr int kThreads = 256;
-constexpr int kCBits = 10;
-constexpr int kChunk = 1 << kCBits;       // requests per chunk
-constexpr int kRBits = 32 - kCBits;       // log2(entries per region) = 22
-constexpr int kMaxRegions = 1024;         // tables up to 2^32 entries
+constexpr int kCBits = kIgChunkBits;
+constexpr int kChunk = 1 << kCBits;       // requests per chunk: 2048
+constexpr int kRBits = kIgRegionBits;     // log2(entries per region) = 21: 16 MiB of table
+constexpr int kMaxRegions = static_cast<int>(kIgMaxRegions);
+constexpr int kPer = kChunk / kThreads;   // requests per thread in the partition and unpermute
+static_assert(kPer % 4 == 0, "whole 16-byte vectors per thread");
 constexpr int kDescPerClaim = 8;          // (region, chunk) segments a warp claims at once
 
 // Exclusive scan of a[0,m) in shared memory, in place; a[m] = total.
@@ -89,10 +91,10 @@ __global__ void __launch_bounds__(kThreads)
   for (int i = threadIdx.x; i < nreg + 2; i += kThreads) hist[i] = 0;
   __syncthreads();
 
-  uint32_t key[4], reg[4], rank[4];
+  uint32_t key[kPer], reg[kPer], rank[kPer];
   const longlong2 *src = reinterpret_cast<const longlong2 *>(index + base);
 #pragma unroll
-  for (int h = 0; h < 2; h++) {
+  for (int h = 0; h < kPer / 2; h++) {
     const int e0 = 2 * (h * kThreads + threadIdx.x);
     int64_t r[2] = {0, 0};
     if (e0 + 1 < len) {
@@ -120,7 +122,7 @@ __global__ void __launch_bounds__(kThreads)
   uint16_t *st = starts + c * (nreg + 2);
   for (int i = threadIdx.x; i < nreg + 2; i += kThreads) st[i] = static_cast<uint16_t>(hist[i]);
 #pragma unroll
-  for (int h = 0; h < 2; h++)
+  for (int h = 0; h < kPer / 2; h++)
 #pragma unroll
     for (int j = 0; j < 2; j++) {
       const int e = 2 * (h * kThreads + threadIdx.x) + j, s = 2 * h + j;
@@ -129,8 +131,11 @@ __global__ void __launch_bounds__(kThreads)
   __syncthreads();
   uint32_t *dst = entries + base;
   if (len == kChunk) {
-    const uint4 v = reinterpret_cast<const uint4 *>(stage)[threadIdx.x];
-    st_v4_u32_pol(reinterpret_cast<uint4 *>(dst) + threadIdx.x, v, pol);
+#pragma unroll
+    for (int q = 0; q < kPer / 4; q++) {
+      const uint4 v = reinterpret_cast<const uint4 *>(stage)[q * kThreads + threadIdx.x];
+      st_v4_u32_pol(reinterpret_cast<uint4 *>(dst) + q * kThreads + threadIdx.x, v, pol);
+    }
   } else {
     for (int i = threadIdx.x; i < len; i += kThreads) st_u32_pol(dst + i, stage[i], pol);
   }
@@ -232,13 +237,17 @@ __global__ void __launch_bounds__(kThreads)
   const int len = static_cast<int>(n - base < kChunk ? n - base : kChunk);
   const uint64_t ef = policy_evict_first();
   if (len == kChunk) {
-    const uint4 e = ld_v4_u32_pol(reinterpret_cast<const uint4 *>(entries + base) + threadIdx.x, ef);
-    const longlong2 *vp = reinterpret_cast<const longlong2 *>(val + base) + 2 * threadIdx.x;
-    const longlong2 v0 = ld_v2_s64_pol(vp, ef), v1 = ld_v2_s64_pol(vp + 1, ef);
-    tile[e.x & (kChunk - 1)] = v0.x;
-    tile[e.y & (kChunk - 1)] = v0.y;
-    tile[e.z & (kChunk - 1)] = v1.x;
-    tile[e.w & (kChunk - 1)] = v1.y;
+#pragma unroll
+    for (int q = 0; q < kPer / 4; q++) {
+      const int at = q * kThreads + threadIdx.x;  // entries 4 at..4 at+3
+      const uint4 e = ld_v4_u32_pol(reinterpret_cast<const uint4 *>(entries + base) + at, ef);
+      const longlong2 *vp = reinterpret_cast<const longlong2 *>(val + base) + 2 * at;
+      const longlong2 v0 = ld_v2_s64_pol(vp, ef), v1 = ld_v2_s64_pol(vp + 1, ef);
+      tile[e.x & (kChunk - 1)] = v0.x;
+      tile[e.y & (kChunk - 1)] = v0.y;
+      tile[e.z & (kChunk - 1)] = v1.x;
+      tile[e.w & (kChunk - 1)] = v1.y;
+    }
   } else {
     for (int i = threadIdx.x; i < len; i += kThreads)
       tile[entries[base + i] & (kChunk - 1)] = val[base + i];

@@ -16,7 +16,21 @@
 // The radix sort is stable, 8 bits per pass: per tile of 4096 keys a digit
 // histogram, one exclusive scan over (digit, tile), then a scatter in which
 // every key's rank among equal digits of its tile comes from a warp match
-// and per-warp counts in shared memory.
+// and per-warp counts in shared memory; the tile is laid out in shared
+// memory in sorted order and leaves run by run.
+//
+// The same machinery serves spmat's other operations at one PE, each
+// bit-identical to the reference:
+//   * transpose_matrix_agi and permute_matrix_agi (spmat/spmat_agi.upc:
+//     119-235): a key pass and a sort; a warp per permuted row;
+//   * rand_permp_agi and rand_permp_exstack (spmat/spmat_agi.upc:56-107,
+//     spmat/spmat_exstack.upc:62-190): dart throwing decided in parallel,
+//     the throws grouped by slot region so that their claims stay in L2;
+//   * read_matrix_mm_to_dist (spmat/spmat_utils.upc:217-370): the body
+//     parsed on the device, a stable sort keeping each row's file order;
+//   * binary datasets (spmat/spmat_agi.upc:245-335): row lengths and
+//     columns streamed between device memory and the files through two
+//     pinned chunks.
 #include <sys/stat.h>
 
 #include <algorithm>

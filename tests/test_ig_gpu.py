@@ -218,3 +218,39 @@ def test_skew_switch_matches_oracle(cuda, bale, oracle, dist, pct):
     want = np.where(ok, table[np.where(ok, index, 0)], 0)
     np.testing.assert_array_equal(tgt.cpu().numpy(), want)
     assert int(bad.item()) == int((~ok).sum())
+
+
+@pytest.mark.parametrize("dist", ["uniform", "zipf1.3"])
+def test_skew_switch_inside_a_captured_graph(cuda, bale, dist):
+    """The skew test, both partitioned kernels' early returns and the direct
+    gather are stream work only: a warmed-up call captures into a CUDA graph
+    and replays with fresh inputs."""
+    import torch
+
+    tsize, n = 1 << 24, 1 << 22
+    dev = torch.device("cuda:0")
+    table_h = bale.gen_values(tsize, 51)
+    t_table = torch.from_numpy(table_h).to(dev)
+    t_index = torch.empty(n, dtype=torch.int64, device=dev)
+    tgt = torch.empty(n, dtype=torch.int64, device=dev)
+    s = torch.cuda.Stream()
+
+    def fresh(seed):
+        return (bale.gen_uniform(n, tsize, seed) if dist == "uniform"
+                else bale.gen_zipf(n, tsize, 1.3, seed, seed + 1))
+
+    with torch.cuda.stream(s):  # the workspace is per stream: warm up on the capture stream
+        t_index.copy_(torch.from_numpy(fresh(1)))
+        bale.ig_dev(tgt, t_index, t_table)
+    s.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=s):
+        bale.ig_dev(tgt, t_index, t_table)
+    for seed in (5, 9):
+        index_h = fresh(seed)
+        t_index.copy_(torch.from_numpy(index_h))
+        tgt.fill_(-1)
+        torch.cuda.synchronize()
+        g.replay()
+        torch.cuda.synchronize()
+        np.testing.assert_array_equal(tgt.cpu().numpy(), table_h[index_h])

@@ -538,7 +538,9 @@ def run_spmat(ctx) -> dict:
                                 "transpose: radix sort of (column, row) keys",
                                 note="algorithmic bytes: 24 B per key per 8-bit pass (44-bit keys); the "
                                      "check, key and CSR kernels are not counted"),
-           "clocks": clocks.summary(), "gpu_launches": None,
+           # a transpose step: the CSR check, the key pass, ceil(44/8) = 6 radix passes of histogram + 3 scan
+           # kernels + scatter, then the CSR offsets and columns
+           "clocks": clocks.summary(), "gpu_launches": (2 + 6 * 5 + 2) * args.steps,
            "config": {"workload": "transpose_matrix / permute_matrix of the R-MAT scale-22 degree-ordered lower "
                                   "matrix (n = 2^22, 64,155,075 nonzeros); rand_permp_agi and rand_permp of 2^26 "
                                   "elements",

@@ -173,8 +173,7 @@ __global__ void __launch_bounds__(kThreads, 3)
                          const uint32_t *__restrict__ offs, int64_t ntiles) {
   __shared__ uint64_t sorted[kTile];
   __shared__ uint32_t wcnt[kWarps][kDigits];  // counts per warp, then their exclusive prefix over warps
-  __shared__ uint32_t dstart[kDigits];        // where each digit starts in the sorted tile
-  __shared__ uint32_t gbase[kDigits];         // where it starts in dst
+  __shared__ uint32_t gbase[kDigits];         // where each digit's run starts in dst
   __shared__ uint32_t wsum[kWarps];
   const unsigned lane = lane_id(), warp = threadIdx.x >> 5;
 #pragma unroll
@@ -219,19 +218,24 @@ __global__ void __launch_bounds__(kThreads, 3)
   __syncthreads();
   uint32_t before = 0;
   for (unsigned w = 0; w < warp; w++) before += wsum[w];
-  dstart[threadIdx.x] = before + inc - cnt;
+  const uint32_t start = before + inc - cnt;  // digit d = threadIdx.x starts here in the sorted tile
+  // one table per use: each warp's place for digit d in the sorted tile, and
+  // the shift from a sorted position to its place in dst
+#pragma unroll
+  for (int w = 0; w < kWarps; w++) wcnt[w][threadIdx.x] += start;
+  gbase[threadIdx.x] -= start;
   __syncthreads();
 #pragma unroll
   for (int r = 0; r < kPer; r++) {
     const uint32_t d = dr[r] >> 16;
-    if (d < kDigits) sorted[dstart[d] + wcnt[warp][d] + (dr[r] & 0xffffu)] = key[r];
+    if (d < kDigits) sorted[wcnt[warp][d] + (dr[r] & 0xffffu)] = key[r];
   }
   __syncthreads();
   const int tile_n = static_cast<int>(n - tile < kTile ? n - tile : kTile);
   for (int j = threadIdx.x; j < tile_n; j += kThreads) {
     const uint64_t k = sorted[j];
     const uint32_t d = static_cast<uint32_t>(k >> shift) & (kDigits - 1);
-    dst[gbase[d] + (j - dstart[d])] = k;
+    dst[gbase[d] + j] = k;  // gbase[d] - start[d] + j, modulo 2^32
   }
 }
 

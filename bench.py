@@ -882,8 +882,9 @@ def run_reference(args, dist: Dist) -> dict | None:
             "ms_per_step": round(secs * 1e3, 3),
             "cpu_baseline": {"value": round(v, 5), "unit": unit, "cores": cores, "kind": "port", "sample": desc},
             "e2e": {"value": round(v, 5), "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-            "config": {"workload": wl, "note": "oracle restatement of the reference's AGI loop "
-                                               "(the reference tree is not on this machine)"}}
+            "config": {"workload": wl, "note": "oracle restatement of the reference's AGI loop, one pthread per "
+                                               "core (the reference's own build runs one PE, single-threaded, "
+                                               "and exists only where its source tree does)"}}
 
 
 def main(argv=None) -> int:

@@ -400,7 +400,28 @@ def run_triangles(ctx) -> dict:
                                   "symmetrised, deduplicated, degree-ordered strictly lower L",
                       "n": n, "nnz": nnz, "pulls": pulls, "pushes": pushes, "generate_s": round(gen_s, 2),
                       "l2": "the 513 MiB CSR exceeds L2; a 256 MiB buffer is also rewritten between steps"}}
-    del off, col, flush
+    # the Erdos-Renyi variant (n = 2^20, average degree 32): the default path
+    # and, for comparison, the merge kernel (tri.mode 0), which suits a graph
+    # without hubs
+    E = bale.gen_erdos_renyi(1 << 20, 32.0 / (1 << 20), 7)
+    e_off, e_col = torch.from_numpy(E.offset).to(dev), torch.from_numpy(E.nonzero).to(dev)
+    e_cnt = torch.zeros(1, dtype=torch.int64, device=dev)
+    er = {}
+    for mode, name in ((-1, "default"), (0, "merge")):
+        bale.tune_set("tri.mode", mode)
+        try:
+            e_ms = ctx["dist"].max(time_device(lambda: bale.triangle_dev(e_off, e_col, e_cnt), args.steps,
+                                               args.warmup, between))
+        finally:
+            bale.tune_set("tri.mode", -1)
+        er[name] = {"value": round(job_rate(E.nnz, e_ms / 1e3, ctx["dist"].world) / 1e9, 4), "unit": "Gedges/s",
+                    "ms_per_step": round(e_ms, 4)}
+    e_cnt.zero_()
+    bale.triangle_dev(e_off, e_col, e_cnt)
+    torch.cuda.synchronize()
+    out["erdos_renyi"] = {**er, "triangles": int(e_cnt.item()), "n": E.numrows, "nnz": E.nnz,
+                          "how": "gen_erdos_renyi(2^20, 32/2^20, seed 7), lower triangle"}
+    del off, col, flush, e_off, e_col
     torch.cuda.empty_cache()
     res = {}
 

@@ -93,19 +93,24 @@ int launch_histo_partitioned(int64_t *counts, int64_t ncounts, const int64_t *in
                              cudaStream_t stream);
 // Bitmap/search hybrid triangle counting (tri_hybrid.cu); needs numrows < 2^32.
 size_t tri_hybrid_workspace_bytes(int64_t numrows, int64_t nnz);
+// run_if (optional, here and in the wedge functions below): a device word;
+// the kernels return at once unless it reads 0 (hybrid) or 1 (wedge), so a
+// choice made on the device picks one of the two paths.
 int launch_triangle_hybrid(const int64_t *offset, const int64_t *nonzero, int64_t numrows, int64_t nnz,
                            unsigned long long *count, unsigned long long *work, unsigned long long *bad,
-                           void *ws, unsigned long long *words, int rows_per_fetch, cudaStream_t stream);
+                           void *ws, unsigned long long *words, int rows_per_fetch, cudaStream_t stream,
+                           const unsigned *run_if = nullptr);
 // A public batch instance is well formed (kind, shift, sizes, pointers).
 bool instance_valid(const bale_instance_t &x);
 // The two halves of the hybrid: prepare (u32 column copy + heavy-row list,
 // once per graph) and run (heavy and light kernels; cursors[0..1] zeroed here).
 int tri_hybrid_prepare(const int64_t *offset, const int64_t *nonzero, int64_t numrows, int64_t nnz,
-                       uint32_t *col32, uint32_t *heavy, unsigned long long *nheavy, cudaStream_t stream);
+                       uint32_t *col32, uint32_t *heavy, unsigned long long *nheavy, cudaStream_t stream,
+                       const unsigned *run_if = nullptr);
 int tri_hybrid_run(const int64_t *offset, const uint32_t *col32, const uint32_t *heavy,
                    const unsigned long long *nheavy, int64_t numrows, int64_t nnz, unsigned long long *count,
                    unsigned long long *work, unsigned long long *bad, unsigned long long *cursors,
-                   int rows_per_fetch, cudaStream_t stream);
+                   int rows_per_fetch, cudaStream_t stream, const unsigned *run_if = nullptr);
 // Wedge-probe triangle count (tri_wedge.cu), for fewer than 2^32 - 1 rows and
 // about 2^32 nonzeros.  prepare builds the u32 column copy and the transpose
 // into ws (tri_wedge_workspace_bytes) and adds malformed entries to *bad (may
@@ -114,12 +119,13 @@ int tri_hybrid_run(const int64_t *offset, const uint32_t *col32, const uint32_t 
 bool tri_wedge_supported(int64_t numrows, int64_t nnz);
 size_t tri_wedge_workspace_bytes(int64_t numrows, int64_t nnz);
 int tri_wedge_prepare(const int64_t *offset, const int64_t *nonzero, int64_t numrows, int64_t nnz, void *ws,
-                      unsigned long long *bad, cudaStream_t stream);
+                      unsigned long long *bad, cudaStream_t stream, const unsigned *run_if = nullptr);
 int tri_wedge_run(const int64_t *offset, const void *ws, int64_t numrows, int64_t nnz, unsigned long long *count,
-                  unsigned long long *work, unsigned long long *cursor, cudaStream_t stream);
+                  unsigned long long *work, unsigned long long *cursor, cudaStream_t stream,
+                  const unsigned *run_if = nullptr);
 int launch_triangle_wedge(const int64_t *offset, const int64_t *nonzero, int64_t numrows, int64_t nnz,
                           unsigned long long *count, unsigned long long *work, unsigned long long *bad, void *ws,
-                          unsigned long long *cursor, cudaStream_t stream);
+                          unsigned long long *cursor, cudaStream_t stream, const unsigned *run_if = nullptr);
 // n +1 L2 reductions at hashed positions of counts (the L2 reduction-rate probe).
 int launch_l2_red_rate(int64_t *counts, int64_t ncounts, int64_t n, cudaStream_t stream);
 // *mapped_dst = *src by a one-thread kernel (mapped_dst: the device alias of

@@ -29,6 +29,12 @@ __device__ __forceinline__ bool is_heavy(int64_t i, int64_t b, int64_t e, int64_
   return i < bits && e - b >= kHeavyMinDeg;
 }
 
+// A path's kernels return at once when a device-made choice picked the
+// other one (run_if: null, or a word that must read `want`).
+__device__ __forceinline__ bool skipped(const unsigned *run_if, unsigned want) {
+  return run_if && *run_if != want;
+}
+
 // Bit w of the row-i bitmap.  The word index is masked to the power-of-two
 // bitmap size, so a malformed row j never indexes outside it; such a row is
 // itself flagged when it is processed as row i, which fails the whole count.

@@ -36,7 +36,8 @@ constexpr int kLightThreads = 256;
 constexpr int kLightWarps = kLightThreads / 32;
 
 __global__ void __launch_bounds__(256)
-    tri_convert_kernel(const int64_t *__restrict__ col, int64_t nnz, uint32_t *__restrict__ col32) {
+    tri_convert_kernel(const int64_t *__restrict__ col, int64_t nnz, uint32_t *__restrict__ col32, const unsigned *__restrict__ run_if) {
+  if (tri::skipped(run_if, 0u)) return;
   const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
   for (int64_t k = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; k < nnz; k += stride) {
     const int64_t c = ld_stream(col + k);
@@ -46,7 +47,8 @@ __global__ void __launch_bounds__(256)
 
 __global__ void __launch_bounds__(256)
     tri_classify_kernel(const int64_t *__restrict__ off, int64_t n, int64_t bits,
-                        uint32_t *__restrict__ heavy, unsigned long long *__restrict__ nheavy) {
+                        uint32_t *__restrict__ heavy, unsigned long long *__restrict__ nheavy, const unsigned *__restrict__ run_if) {
+  if (tri::skipped(run_if, 0u)) return;
   const int64_t lim = n < bits ? n : bits;
   const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
   for (int64_t base = static_cast<int64_t>(blockIdx.x) * blockDim.x; base < lim; base += stride) {
@@ -76,7 +78,8 @@ __global__ void __launch_bounds__(kHeavyThreads, 3)
     tri_heavy_kernel(const int64_t *__restrict__ off, const uint32_t *__restrict__ col, int64_t nnz,
                      const uint32_t *__restrict__ heavy, const unsigned long long *__restrict__ nheavy_p,
                      int64_t bits, unsigned long long *__restrict__ count, unsigned long long *__restrict__ work,
-                     unsigned long long *__restrict__ bad, unsigned long long *__restrict__ cursor) {
+                     unsigned long long *__restrict__ bad, unsigned long long *__restrict__ cursor, const unsigned *__restrict__ run_if) {
+  if (tri::skipped(run_if, 0u)) return;
   extern __shared__ uint32_t bm[];
   __shared__ long long sel;
   const int64_t nwords = bits >> 5;  // bits is a power of two >= 32
@@ -102,7 +105,8 @@ __global__ void __launch_bounds__(kLightThreads)
     tri_light_kernel(const int64_t *__restrict__ off, const uint32_t *__restrict__ col, int64_t n, int64_t nnz,
                      int64_t bits, unsigned long long *__restrict__ count, unsigned long long *__restrict__ work,
                      unsigned long long *__restrict__ bad, unsigned long long *__restrict__ cursor,
-                     int rows_per_fetch) {
+                     int rows_per_fetch, const unsigned *__restrict__ run_if) {
+  if (tri::skipped(run_if, 0u)) return;
   __shared__ uint32_t rowbuf[kLightWarps][tri::kLightCap];
   uint32_t *rb = rowbuf[threadIdx.x >> 5];
   tri::Tally t;
@@ -128,20 +132,22 @@ size_t tri_hybrid_workspace_bytes(int64_t numrows, int64_t nnz) {
 }
 
 int tri_hybrid_prepare(const int64_t *offset, const int64_t *nonzero, int64_t numrows, int64_t nnz,
-                       uint32_t *col32, uint32_t *heavy, unsigned long long *nheavy, cudaStream_t stream) {
+                       uint32_t *col32, uint32_t *heavy, unsigned long long *nheavy, cudaStream_t stream,
+                       const unsigned *run_if) {
   const int sms = num_sms();
   const int64_t bits = tri::bitmap_bits(numrows);
   BALE_CUDA_OK(cudaMemsetAsync(nheavy, 0, sizeof(unsigned long long), stream));
   if (nnz > 0) {
     int64_t blocks = (nnz + 255) / 256, cap = static_cast<int64_t>(sms) * 8;
-    tri_convert_kernel<<<static_cast<unsigned>(blocks < cap ? blocks : cap), 256, 0, stream>>>(nonzero, nnz, col32);
+    tri_convert_kernel<<<static_cast<unsigned>(blocks < cap ? blocks : cap), 256, 0, stream>>>(nonzero, nnz, col32,
+                                                                                           run_if);
     BALE_CUDA_OK(cudaGetLastError());
   }
   const int64_t lim = numrows < bits ? numrows : bits;
   int64_t blocks = (lim + 255) / 256, cap = static_cast<int64_t>(sms) * 8;
   if (blocks < 1) blocks = 1;
   tri_classify_kernel<<<static_cast<unsigned>(blocks < cap ? blocks : cap), 256, 0, stream>>>(
-      offset, numrows, bits, heavy, nheavy);
+      offset, numrows, bits, heavy, nheavy, run_if);
   BALE_CUDA_OK(cudaGetLastError());
   return BALE_OK;
 }
@@ -149,7 +155,7 @@ int tri_hybrid_prepare(const int64_t *offset, const int64_t *nonzero, int64_t nu
 int tri_hybrid_run(const int64_t *offset, const uint32_t *col32, const uint32_t *heavy,
                    const unsigned long long *nheavy, int64_t numrows, int64_t nnz, unsigned long long *count,
                    unsigned long long *work, unsigned long long *bad, unsigned long long *cursors,
-                   int rows_per_fetch, cudaStream_t stream) {
+                   int rows_per_fetch, cudaStream_t stream, const unsigned *run_if) {
   const int sms = num_sms();
   const int64_t bits = tri::bitmap_bits(numrows);
   BALE_CUDA_OK(cudaMemsetAsync(cursors, 0, 2 * sizeof(unsigned long long), stream));
@@ -166,7 +172,7 @@ int tri_hybrid_run(const int64_t *offset, const uint32_t *col32, const uint32_t 
         occ < 1)
       occ = 1;
     tri_heavy_kernel<<<static_cast<unsigned>(sms * occ), kHeavyThreads, smem, stream>>>(
-        offset, col32, nnz, heavy, nheavy, bits, count, work, bad, cursors);
+        offset, col32, nnz, heavy, nheavy, bits, count, work, bad, cursors, run_if);
     BALE_CUDA_OK(cudaGetLastError());
   }
   {
@@ -178,7 +184,7 @@ int tri_hybrid_run(const int64_t *offset, const uint32_t *col32, const uint32_t 
     const int64_t need = ((numrows + rows_per_fetch - 1) / rows_per_fetch + kLightWarps - 1) / kLightWarps;
     if (blocks > need) blocks = need > 0 ? need : 1;
     tri_light_kernel<<<static_cast<unsigned>(blocks), kLightThreads, 0, stream>>>(
-        offset, col32, numrows, nnz, bits, count, work, bad, cursors + 1, rows_per_fetch);
+        offset, col32, numrows, nnz, bits, count, work, bad, cursors + 1, rows_per_fetch, run_if);
     BALE_CUDA_OK(cudaGetLastError());
   }
   return BALE_OK;
@@ -186,16 +192,17 @@ int tri_hybrid_run(const int64_t *offset, const uint32_t *col32, const uint32_t 
 
 int launch_triangle_hybrid(const int64_t *offset, const int64_t *nonzero, int64_t numrows, int64_t nnz,
                            unsigned long long *count, unsigned long long *work, unsigned long long *bad,
-                           void *ws, unsigned long long *words, int rows_per_fetch, cudaStream_t stream) {
+                           void *ws, unsigned long long *words, int rows_per_fetch, cudaStream_t stream,
+                           const unsigned *run_if) {
   // words: [0] heavy-list length, [1] heavy cursor, [2] light cursor
   char *p = static_cast<char *>(ws);
   uint32_t *col32 = reinterpret_cast<uint32_t *>(p);
   p += (static_cast<size_t>(nnz > 0 ? nnz : 1) * sizeof(uint32_t) + 255) & ~size_t(255);
   uint32_t *heavy = reinterpret_cast<uint32_t *>(p);
-  int rc = tri_hybrid_prepare(offset, nonzero, numrows, nnz, col32, heavy, words, stream);
+  int rc = tri_hybrid_prepare(offset, nonzero, numrows, nnz, col32, heavy, words, stream, run_if);
   if (rc != BALE_OK) return rc;
   return tri_hybrid_run(offset, col32, heavy, words, numrows, nnz, count, work, bad, words + 1, rows_per_fetch,
-                        stream);
+                        stream, run_if);
 }
 
 }  // namespace bale

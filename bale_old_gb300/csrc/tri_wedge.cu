@@ -169,7 +169,8 @@ struct RowGroup {
 __global__ void __launch_bounds__(kScanThreads)
     wedge_scan_kernel(const int64_t *__restrict__ off, const int64_t *__restrict__ col, int64_t n, int64_t nnz,
                       uint32_t *__restrict__ col32, uint32_t *__restrict__ in_cnt, uint32_t *__restrict__ hubs,
-                      unsigned long long *__restrict__ words, unsigned long long *__restrict__ bad) {
+                      unsigned long long *__restrict__ words, unsigned long long *__restrict__ bad, const unsigned *__restrict__ run_if) {
+  if (tri::skipped(run_if, 1u)) return;
   __shared__ uint4 stage[kScanWarps][32];
   __shared__ uint32_t hub[kHub];
   for (int h = threadIdx.x; h < kHub; h += kScanThreads) hub[h] = 0;
@@ -226,7 +227,8 @@ __global__ void __launch_bounds__(kScanThreads)
 }
 
 // hubs[b][h] becomes the exclusive prefix over blocks b of the hub counts.
-__global__ void __launch_bounds__(256) wedge_hubscan_kernel(uint32_t *__restrict__ hubs, int nblocks) {
+__global__ void __launch_bounds__(256) wedge_hubscan_kernel(uint32_t *__restrict__ hubs, int nblocks, const unsigned *__restrict__ run_if) {
+  if (tri::skipped(run_if, 1u)) return;
   const int h = blockIdx.x * 256 + threadIdx.x;
   if (h >= kHub) return;
   uint32_t run = 0;
@@ -264,7 +266,8 @@ __device__ __forceinline__ void load4(const uint32_t *__restrict__ a, int64_t n,
 }
 
 __global__ void __launch_bounds__(kPsumThreads)
-    wedge_blocksum_kernel(const uint32_t *__restrict__ in_cnt, int64_t n, uint32_t *__restrict__ bsum) {
+    wedge_blocksum_kernel(const uint32_t *__restrict__ in_cnt, int64_t n, uint32_t *__restrict__ bsum, const unsigned *__restrict__ run_if) {
+  if (tri::skipped(run_if, 1u)) return;
   __shared__ uint32_t tot;
   const int64_t idx = static_cast<int64_t>(blockIdx.x) * kPsumBlock + static_cast<int64_t>(threadIdx.x) * kPsumPer;
   uint32_t v[4];
@@ -275,7 +278,8 @@ __global__ void __launch_bounds__(kPsumThreads)
 
 // One block: exclusive scan of the nb block sums in place; in_off[n] = total.
 __global__ void __launch_bounds__(kPsumThreads)
-    wedge_topscan_kernel(uint32_t *__restrict__ bsum, int64_t nb, uint32_t *__restrict__ in_off, int64_t n) {
+    wedge_topscan_kernel(uint32_t *__restrict__ bsum, int64_t nb, uint32_t *__restrict__ in_off, int64_t n, const unsigned *__restrict__ run_if) {
+  if (tri::skipped(run_if, 1u)) return;
   __shared__ uint32_t tot;
   uint32_t carry = 0;
   for (int64_t base = 0; base < nb; base += kPsumBlock) {
@@ -296,7 +300,8 @@ __global__ void __launch_bounds__(kPsumThreads)
 // in_off[j] = exclusive prefix of the counts; the counts are zeroed for the fill.
 __global__ void __launch_bounds__(kPsumThreads)
     wedge_offsets_kernel(uint32_t *__restrict__ in_cnt, int64_t n, const uint32_t *__restrict__ bsum,
-                         uint32_t *__restrict__ in_off) {
+                         uint32_t *__restrict__ in_off, const unsigned *__restrict__ run_if) {
+  if (tri::skipped(run_if, 1u)) return;
   __shared__ uint32_t tot;
   const int64_t idx = static_cast<int64_t>(blockIdx.x) * kPsumBlock + static_cast<int64_t>(threadIdx.x) * kPsumPer;
   uint32_t v[4];
@@ -319,7 +324,8 @@ __global__ void __launch_bounds__(kScanThreads)
     wedge_fill_kernel(const int64_t *__restrict__ off, const uint32_t *__restrict__ col32, int64_t n, int64_t nnz,
                       const uint32_t *__restrict__ in_off, uint32_t *__restrict__ in_cnt,
                       const uint32_t *__restrict__ hubs, uint2 *__restrict__ in_rec,
-                      const unsigned long long *__restrict__ words) {
+                      const unsigned long long *__restrict__ words, const unsigned *__restrict__ run_if) {
+  if (tri::skipped(run_if, 1u)) return;
   __shared__ uint4 stage[kScanWarps][32];
   __shared__ uint32_t hubslot[kHub];
   if (words[kWBad]) return;
@@ -482,7 +488,8 @@ __global__ void __launch_bounds__(kWarpThreads, 3)
                        const uint32_t *__restrict__ in_off, const uint2 *__restrict__ in_rec, int64_t n, int64_t wlim,
                        int wbits, uint32_t nvec_all, uint32_t stage_max, const unsigned long long *__restrict__ words,
                        unsigned long long *__restrict__ count, unsigned long long *__restrict__ work,
-                       unsigned long long *__restrict__ cursor) {
+                       unsigned long long *__restrict__ cursor, const unsigned *__restrict__ run_if) {
+  if (tri::skipped(run_if, 1u)) return;
   extern __shared__ uint32_t wsm[];
   if (words[kWBad]) return;
   const unsigned lane = lane_id();
@@ -659,7 +666,7 @@ bool tri_wedge_supported(int64_t numrows, int64_t nnz) {
 size_t tri_wedge_workspace_bytes(int64_t numrows, int64_t nnz) { return layout(numrows, nnz).total; }
 
 int tri_wedge_prepare(const int64_t *offset, const int64_t *nonzero, int64_t numrows, int64_t nnz, void *ws,
-                      unsigned long long *bad, cudaStream_t stream) {
+                      unsigned long long *bad, cudaStream_t stream, const unsigned *run_if) {
   if (!tri_wedge_supported(numrows, nnz)) return BALE_EINVAL;
   const Layout l = layout(numrows, nnz);
   char *p = static_cast<char *>(ws);
@@ -678,25 +685,26 @@ int tri_wedge_prepare(const int64_t *offset, const int64_t *nonzero, int64_t num
   const int64_t scap = static_cast<int64_t>(sms) * kScanBlocksPerSm;  // the hubs array holds this many blocks
   if (sblocks > scap) sblocks = scap;
   wedge_scan_kernel<<<static_cast<unsigned>(sblocks), kScanThreads, 0, stream>>>(offset, nonzero, numrows, nnz, col32,
-                                                                                 in_cnt, hubs, words, bad);
+                                                                                 in_cnt, hubs, words, bad, run_if);
   BALE_CUDA_OK(cudaGetLastError());
-  wedge_hubscan_kernel<<<kHub / 256, 256, 0, stream>>>(hubs, static_cast<int>(sblocks));
+  wedge_hubscan_kernel<<<kHub / 256, 256, 0, stream>>>(hubs, static_cast<int>(sblocks), run_if);
   BALE_CUDA_OK(cudaGetLastError());
   const int64_t nb = (numrows + kPsumBlock - 1) / kPsumBlock;
-  wedge_blocksum_kernel<<<static_cast<unsigned>(nb), kPsumThreads, 0, stream>>>(in_cnt, numrows, bsum);
+  wedge_blocksum_kernel<<<static_cast<unsigned>(nb), kPsumThreads, 0, stream>>>(in_cnt, numrows, bsum, run_if);
   BALE_CUDA_OK(cudaGetLastError());
-  wedge_topscan_kernel<<<1, kPsumThreads, 0, stream>>>(bsum, nb, in_off, numrows);
+  wedge_topscan_kernel<<<1, kPsumThreads, 0, stream>>>(bsum, nb, in_off, numrows, run_if);
   BALE_CUDA_OK(cudaGetLastError());
-  wedge_offsets_kernel<<<static_cast<unsigned>(nb), kPsumThreads, 0, stream>>>(in_cnt, numrows, bsum, in_off);
+  wedge_offsets_kernel<<<static_cast<unsigned>(nb), kPsumThreads, 0, stream>>>(in_cnt, numrows, bsum, in_off,
+                                                                               run_if);
   BALE_CUDA_OK(cudaGetLastError());
   wedge_fill_kernel<<<static_cast<unsigned>(sblocks), kScanThreads, 0, stream>>>(offset, col32, numrows, nnz, in_off,
-                                                                                 in_cnt, hubs, in_rec, words);
+                                                                                 in_cnt, hubs, in_rec, words, run_if);
   BALE_CUDA_OK(cudaGetLastError());
   return BALE_OK;
 }
 
 int tri_wedge_run(const int64_t *offset, const void *ws, int64_t numrows, int64_t nnz, unsigned long long *count,
-                  unsigned long long *work, unsigned long long *cursor, cudaStream_t stream) {
+                  unsigned long long *work, unsigned long long *cursor, cudaStream_t stream, const unsigned *run_if) {
   if (!tri_wedge_supported(numrows, nnz)) return BALE_EINVAL;
   const Layout l = layout(numrows, nnz);
   const char *p = static_cast<const char *>(ws);
@@ -726,17 +734,17 @@ int tri_wedge_run(const int64_t *offset, const void *ws, int64_t numrows, int64_
   const int64_t need = (claims + kWarpWarps - 1) / kWarpWarps;
   if (blocks > need) blocks = need > 0 ? need : 1;
   wedge_count_kernel<<<static_cast<unsigned>(blocks), kWarpThreads, smem, stream>>>(
-      offset, col32, in_off, in_rec, numrows, wlim, wb, nvec_all, stage_max, words, count, work, cursor);
+      offset, col32, in_off, in_rec, numrows, wlim, wb, nvec_all, stage_max, words, count, work, cursor, run_if);
   BALE_CUDA_OK(cudaGetLastError());
   return BALE_OK;
 }
 
 int launch_triangle_wedge(const int64_t *offset, const int64_t *nonzero, int64_t numrows, int64_t nnz,
                           unsigned long long *count, unsigned long long *work, unsigned long long *bad, void *ws,
-                          unsigned long long *cursor, cudaStream_t stream) {
-  const int rc = tri_wedge_prepare(offset, nonzero, numrows, nnz, ws, bad, stream);
+                          unsigned long long *cursor, cudaStream_t stream, const unsigned *run_if) {
+  const int rc = tri_wedge_prepare(offset, nonzero, numrows, nnz, ws, bad, stream, run_if);
   if (rc != BALE_OK) return rc;
-  return tri_wedge_run(offset, ws, numrows, nnz, count, work, cursor, stream);
+  return tri_wedge_run(offset, ws, numrows, nnz, count, work, cursor, stream, run_if);
 }
 
 }  // namespace bale

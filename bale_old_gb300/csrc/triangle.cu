@@ -157,14 +157,86 @@ int g_tri_blocks_per_sm[2][64] = {{0}, {0}};
 
 }  // namespace
 
+// The default path per graph, chosen on the device.  The wedge path's work
+// is the pushes, sum over rows of C(d,2); the hybrid's is close to the
+// pulls, sum over nonzeros (i,j) of d_j.  Graphs with hubs (R-MAT: pulls
+// 1.9-4x the pushes from scale 10 to 22; Kronecker products of stars, whose
+// rows average hundreds of wedges per nonzero) count fastest by wedges;
+// graphs without (Erdos-Renyi: pulls = pushes, 8-43 wedges per nonzero) by
+// the hybrid, 10-30% faster there.  The pushes are summed exactly over the
+// rows, the pulls estimated from kChooseSamples evenly spaced nonzeros; the
+// last block to finish writes choice[0] = 1 (wedge) or 0 (hybrid).
+// words: [0] pushes, [1] sampled pulls, [2] blocks done (zeroed by the caller).
+constexpr int kChooseSamples = 4096;
+constexpr int kChooseThreads = 256;
+// Below this many nonzeros the choice (a kernel, and the skipped path's
+// launches: 0.03-0.06 ms) would cost more than it can save; the wedge path
+// runs directly.
+constexpr int64_t kChooseMinNnz = int64_t(1) << 23;
+
+__global__ void __launch_bounds__(kChooseThreads)
+    tri_choose_kernel(const int64_t *__restrict__ off, const int64_t *__restrict__ col, int64_t n, int64_t nnz,
+                      unsigned long long *__restrict__ words, unsigned *__restrict__ choice) {
+  __shared__ unsigned last;
+  unsigned long long pushes = 0, pulls = 0;
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += stride) {
+    const int64_t d = off[i + 1] - off[i];
+    if (d > 1) pushes += static_cast<unsigned long long>(d) * static_cast<unsigned long long>(d - 1) / 2;
+  }
+  if (blockIdx.x == 0 && nnz > 0) {
+    for (int s = threadIdx.x; s < kChooseSamples; s += kChooseThreads) {
+      const int64_t j = col[static_cast<int64_t>((static_cast<unsigned long long>(s) * nnz) / kChooseSamples)];
+      if (j >= 0 && j < n) pulls += static_cast<unsigned long long>(off[j + 1] - off[j]);  // a bad j: the paths count it
+    }
+  }
+  pushes = warp_sum_u64(pushes);
+  pulls = warp_sum_u64(pulls);
+  if (lane_id() == 0) {
+    if (pushes) atomicAdd(&words[0], pushes);
+    if (pulls) atomicAdd(&words[1], pulls);
+  }
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) last = atomicAdd(&words[2], 1ull) == gridDim.x - 1 ? 1u : 0u;
+  __syncthreads();
+  if (!last || threadIdx.x != 0) return;
+  __threadfence();
+  const double push = static_cast<double>(atomicAdd(&words[0], 0ull));
+  const double pull = static_cast<double>(atomicAdd(&words[1], 0ull)) * static_cast<double>(nnz) / kChooseSamples;
+  const bool wedge = push == 0.0 || pull >= 1.5 * push || push >= 128.0 * static_cast<double>(nnz);
+  *choice = wedge ? 1u : 0u;
+}
+
 int launch_triangle(const int64_t *offset, const int64_t *nonzero, int64_t numrows, int64_t nnz,
                     unsigned long long *count, unsigned long long *work, unsigned long long *bad,
                     cudaStream_t stream) {
   if (numrows <= 0) return BALE_OK;
-  // Default: wedge probes at the far vertex (tri_wedge.cu); mode 1 the
-  // bitmap/search hybrid over rows i (tri_hybrid.cu); mode 0 this file's
-  // warp-per-row merge kernel for every row.
+  // Default: per graph, wedge probes at the far vertex (tri_wedge.cu) or the
+  // bitmap/search hybrid over rows i (tri_hybrid.cu), chosen on the device
+  // by tri_choose_kernel; mode 2 the wedge path, mode 1 the hybrid, mode 0
+  // this file's warp-per-row merge kernel for every row.
   const int64_t mode = knob("tri.mode");
+  if (mode < 0 && tri_wedge_supported(numrows, nnz) && nnz >= kChooseMinNnz) {
+    // both paths launched, the one not chosen returning at once; their
+    // workspaces side by side
+    const size_t wbytes = (tri_wedge_workspace_bytes(numrows, nnz) + 255) & ~size_t(255);
+    char *ws = static_cast<char *>(device_workspace(wbytes + tri_hybrid_workspace_bytes(numrows, nnz), stream));
+    unsigned long long *cursor = next_cursor_words(2), *hwords = next_cursor_words(3), *cw = next_cursor_words(4);
+    if (!ws || !cursor || !hwords || !cw) return BALE_ENOMEM;
+    unsigned *choice = reinterpret_cast<unsigned *>(cw + 3);
+    BALE_CUDA_OK(cudaMemsetAsync(cw, 0, 3 * sizeof(unsigned long long), stream));
+    const int64_t want = (numrows + kChooseThreads - 1) / kChooseThreads, cap = static_cast<int64_t>(num_sms()) * 4;
+    tri_choose_kernel<<<static_cast<unsigned>(want < cap ? want : cap), kChooseThreads, 0, stream>>>(
+        offset, nonzero, numrows, nnz, cw, choice);
+    BALE_CUDA_OK(cudaGetLastError());
+    int rc = launch_triangle_wedge(offset, nonzero, numrows, nnz, count, work, bad, ws, cursor, stream, choice);
+    if (rc != BALE_OK) return rc;
+    int64_t rpf_h = knob("tri.rows_per_fetch");
+    if (rpf_h < 1 || rpf_h > 4096) rpf_h = 8;
+    return launch_triangle_hybrid(offset, nonzero, numrows, nnz, count, work, bad, ws + wbytes, hwords,
+                                  static_cast<int>(rpf_h), stream, choice);
+  }
   if ((mode < 0 || mode == 2) && tri_wedge_supported(numrows, nnz)) {
     void *ws = device_workspace(tri_wedge_workspace_bytes(numrows, nnz), stream);
     unsigned long long *cursor = next_cursor_words(2);

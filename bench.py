@@ -401,8 +401,8 @@ def run_triangles(ctx) -> dict:
                       "n": n, "nnz": nnz, "pulls": pulls, "pushes": pushes, "generate_s": round(gen_s, 2),
                       "l2": "the 513 MiB CSR exceeds L2; a 256 MiB buffer is also rewritten between steps"}}
     # the Erdos-Renyi variant (n = 2^20, average degree 32): the default path
-    # and, for comparison, the merge kernel (tri.mode 0), which suits a graph
-    # without hubs
+    # (which picks the hybrid for a graph without hubs) and, for comparison,
+    # the merge kernel (tri.mode 0)
     E = bale.gen_erdos_renyi(1 << 20, 32.0 / (1 << 20), 7)
     e_off, e_col = torch.from_numpy(E.offset).to(dev), torch.from_numpy(E.nonzero).to(dev)
     e_cnt = torch.zeros(1, dtype=torch.int64, device=dev)

@@ -200,3 +200,31 @@ def test_prepared_graph_malformed_is_flagged(cuda, bale):
         g.count(count)
     torch.cuda.synchronize()
     assert int(bad.item()) > 0 and int(count.item()) == 0
+
+
+# The default mode picks the path per graph on the device (from 2^23
+# nonzeros; below, the wedge path): wedges for graphs with hubs (R-MAT,
+# Kronecker products of stars), the hybrid for graphs without (Erdos-Renyi).
+# The count is exact either way; the work tally shows which path ran (it
+# equals the forced mode's).
+@pytest.mark.parametrize("graph,want", [("rmat20", 2), ("er20", 1), ("er64", 1), ("kron", 2), ("er16", 2)])
+def test_default_mode_choice(cuda, bale, graph, want):
+    if graph.startswith("rmat"):
+        L = bale.gen_rmat(int(graph[4:]), 16, 0.57, 0.19, 0.19, 6)
+    elif graph == "er20":
+        L = bale.gen_erdos_renyi(1 << 20, 32.0 / (1 << 20), 7)
+    elif graph == "er64":
+        L = bale.gen_erdos_renyi(1 << 18, 128.0 / (1 << 18), 7)
+    elif graph == "er16":  # below the size where the choice is made
+        L = bale.gen_erdos_renyi(1 << 16, 32.0 / (1 << 16), 7)
+    else:  # products of stars, large enough to be chosen for
+        L = bale.gen_kronecker(1, [3, 4, 5, 9, 16, 25])
+    cnt, sr, _ = bale.triangle_agi(L)
+    bale.tune_set("tri.mode", want)
+    try:
+        fcnt, fsr, _ = bale.triangle_agi(L)
+    finally:
+        bale.tune_set("tri.mode", -1)
+    assert cnt == fcnt and sr == fsr
+    if graph == "kron":
+        assert cnt == bale.kronecker_triangles(1, [3, 4, 5, 9, 16, 25])

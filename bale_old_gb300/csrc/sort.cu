@@ -1,0 +1,304 @@
+// sort.cu -- the stable LSD radix sort of 64-bit keys and the u32 exclusive
+// scan the graph build and spmat's operations share.
+//
+// The radix sort takes 8 bits per pass: per tile of 4096 keys a digit
+// histogram, one exclusive scan over (digit, tile), then a scatter in which
+// every key's rank among equal digits of its tile comes from a warp match
+// and per-warp counts in shared memory; the tile is laid out in shared
+// memory in sorted order and leaves run by run.
+#include <algorithm>
+
+#include "sort.cuh"
+
+namespace bale {
+namespace {
+
+constexpr unsigned kFull = 0xffffffffu;
+constexpr int kThreads = kSortThreads;
+constexpr int kWarps = kThreads / 32;
+constexpr int kPer = kSortPer;
+static_assert(kDigits == kThreads, "one digit per thread");
+
+// ---------------------------------------------------------------- scan
+__device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t *total) {
+  __shared__ uint32_t warp_tot[kScanThreads / 32];
+  const unsigned lane = lane_id(), warp = threadIdx.x >> 5;
+  uint32_t inc = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(kFull, inc, o);
+    if (static_cast<int>(lane) >= o) inc += y;
+  }
+  if (lane == 31) warp_tot[warp] = inc;
+  __syncthreads();
+  if (warp == 0) {
+    const uint32_t t = warp_tot[lane];
+    uint32_t ti = t;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(kFull, ti, o);
+      if (static_cast<int>(lane) >= o) ti += y;
+    }
+    warp_tot[lane] = ti - t;
+    if (lane == 31) *total = ti;
+  }
+  __syncthreads();
+  const uint32_t r = warp_tot[warp] + inc - v;
+  __syncthreads();
+  return r;
+}
+
+__device__ __forceinline__ void load4(const uint32_t *__restrict__ a, int64_t n, int64_t idx, uint32_t v[4]) {
+#pragma unroll
+  for (int q = 0; q < 4; q++) v[q] = idx + q < n ? a[idx + q] : 0u;
+}
+
+__global__ void __launch_bounds__(kScanThreads)
+    scan_blocksum_kernel(const uint32_t *__restrict__ in, int64_t n, uint32_t *__restrict__ bsum) {
+  __shared__ uint32_t tot;
+  const int64_t idx = static_cast<int64_t>(blockIdx.x) * kScanBlock + threadIdx.x * 4;
+  uint32_t v[4];
+  load4(in, n, idx, v);
+  block_excl_scan(v[0] + v[1] + v[2] + v[3], &tot);
+  if (threadIdx.x == 0) bsum[blockIdx.x] = tot;
+}
+
+__global__ void __launch_bounds__(kScanThreads)
+    scan_top_kernel(uint32_t *__restrict__ bsum, int64_t nb, uint32_t *__restrict__ total) {
+  __shared__ uint32_t tot;
+  uint32_t carry = 0;
+  for (int64_t base = 0; base < nb; base += kScanBlock) {
+    const int64_t idx = base + threadIdx.x * 4;
+    uint32_t v[4];
+    load4(bsum, nb, idx, v);
+    uint32_t x = block_excl_scan(v[0] + v[1] + v[2] + v[3], &tot) + carry;
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      if (idx + q < nb) bsum[idx + q] = x;
+      x += v[q];
+    }
+    carry += tot;
+  }
+  if (threadIdx.x == 0) *total = carry;
+}
+
+__global__ void __launch_bounds__(kScanThreads)
+    scan_apply_kernel(const uint32_t *__restrict__ in, int64_t n, const uint32_t *__restrict__ bsum,
+                      uint32_t *__restrict__ out) {
+  __shared__ uint32_t tot;
+  const int64_t idx = static_cast<int64_t>(blockIdx.x) * kScanBlock + threadIdx.x * 4;
+  uint32_t v[4];
+  load4(in, n, idx, v);
+  uint32_t x = block_excl_scan(v[0] + v[1] + v[2] + v[3], &tot) + bsum[blockIdx.x];
+#pragma unroll
+  for (int q = 0; q < 4; q++) {
+    if (idx + q < n) out[idx + q] = x;
+    x += v[q];
+  }
+}
+
+// ---------------------------------------------------------------- radix sort
+__global__ void __launch_bounds__(kThreads)
+    radix_hist_kernel(const uint64_t *__restrict__ keys, int64_t n, int shift, uint32_t *__restrict__ hist,
+                      int64_t ntiles) {
+  __shared__ uint32_t cnt[kDigits];
+  cnt[threadIdx.x] = 0;
+  __syncthreads();
+  const int64_t base = static_cast<int64_t>(blockIdx.x) * kTile;
+#pragma unroll 4
+  for (int r = 0; r < kPer; r++) {
+    const int64_t i = base + r * kThreads + threadIdx.x;
+    if (i < n) atomicAdd(&cnt[static_cast<uint32_t>(keys[i] >> shift) & (kDigits - 1)], 1u);
+  }
+  __syncthreads();
+  hist[static_cast<int64_t>(threadIdx.x) * ntiles + blockIdx.x] = cnt[threadIdx.x];
+}
+
+// offs[d * ntiles + t]: where tile t's keys with digit d start in dst.  Each
+// warp ranks a contiguous eighth of the tile in index order with warp-private
+// digit counts (no block barrier per round); the warps' counts are scanned
+// per digit, the tile is laid out in shared memory in sorted order, and the
+// threads then write consecutive sorted positions, so each digit's run leaves
+// the block as whole lines.  Stable: within a digit, tile index order.
+constexpr int kWarpSlice = static_cast<int>(kTile) / kWarps;  // 512 keys per warp
+static_assert(kWarpSlice == 32 * kPer, "a warp's slice is kPer rounds of 32");
+
+__global__ void __launch_bounds__(kThreads, 3)
+    radix_scatter_kernel(const uint64_t *__restrict__ src, uint64_t *__restrict__ dst, int64_t n, int shift,
+                         const uint32_t *__restrict__ offs, int64_t ntiles) {
+  __shared__ uint64_t sorted[kTile];
+  __shared__ uint32_t wcnt[kWarps][kDigits];  // counts per warp, then their exclusive prefix over warps
+  __shared__ uint32_t gbase[kDigits];         // where each digit's run starts in dst
+  __shared__ uint32_t wsum[kWarps];
+  const unsigned lane = lane_id(), warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int w = 0; w < kWarps; w++) wcnt[w][threadIdx.x] = 0;
+  gbase[threadIdx.x] = offs[static_cast<int64_t>(threadIdx.x) * ntiles + blockIdx.x];
+  __syncthreads();
+  const int64_t tile = static_cast<int64_t>(blockIdx.x) * kTile;
+  const int64_t first = tile + static_cast<int64_t>(warp) * kWarpSlice + lane;
+  uint64_t key[kPer];
+  uint32_t dr[kPer];  // digit << 16 | rank among the warp's keys of that digit (kDigits: no key)
+#pragma unroll
+  for (int r = 0; r < kPer; r++) {
+    const int64_t i = first + r * 32;
+    const bool valid = i < n;
+    key[r] = valid ? src[i] : 0ull;
+    const uint32_t d = valid ? static_cast<uint32_t>(key[r] >> shift) & (kDigits - 1) : kDigits;
+    const unsigned peers = __match_any_sync(kFull, d);
+    const uint32_t below = __popc(peers & ((1u << lane) - 1u));
+    const uint32_t prior = valid ? wcnt[warp][d] : 0u;
+    __syncwarp();
+    if (valid && below == 0) wcnt[warp][d] = prior + __popc(peers);
+    __syncwarp();
+    dr[r] = d << 16 | (prior + below);
+  }
+  __syncthreads();
+  // thread d: digit d's warp prefixes and its count in the tile, then the
+  // exclusive scan of the counts over digits
+  uint32_t cnt = 0;
+#pragma unroll
+  for (int w = 0; w < kWarps; w++) {
+    const uint32_t c = wcnt[w][threadIdx.x];
+    wcnt[w][threadIdx.x] = cnt;
+    cnt += c;
+  }
+  uint32_t inc = cnt;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(kFull, inc, o);
+    if (static_cast<int>(lane) >= o) inc += y;
+  }
+  if (lane == 31) wsum[warp] = inc;
+  __syncthreads();
+  uint32_t before = 0;
+  for (unsigned w = 0; w < warp; w++) before += wsum[w];
+  const uint32_t start = before + inc - cnt;  // digit d = threadIdx.x starts here in the sorted tile
+  // one table per use: each warp's place for digit d in the sorted tile, and
+  // the shift from a sorted position to its place in dst
+#pragma unroll
+  for (int w = 0; w < kWarps; w++) wcnt[w][threadIdx.x] += start;
+  gbase[threadIdx.x] -= start;
+  __syncthreads();
+#pragma unroll
+  for (int r = 0; r < kPer; r++) {
+    const uint32_t d = dr[r] >> 16;
+    if (d < kDigits) sorted[wcnt[warp][d] + (dr[r] & 0xffffu)] = key[r];
+  }
+  __syncthreads();
+  const int tile_n = static_cast<int>(n - tile < kTile ? n - tile : kTile);
+  for (int j = threadIdx.x; j < tile_n; j += kThreads) {
+    const uint64_t k = sorted[j];
+    const uint32_t d = static_cast<uint32_t>(k >> shift) & (kDigits - 1);
+    dst[gbase[d] + j] = k;  // gbase[d] - start[d] + j, modulo 2^32
+  }
+}
+
+// CSR from row-major sorted keys: offset[r] = first entry of row >= r, by a
+// binary search per row (rows may be empty in long runs: the isolated
+// vertices all take the last labels); nonzero[e] = the column.
+__global__ void __launch_bounds__(256)
+    csr_offsets_kernel(const uint64_t *__restrict__ lk, int64_t nu, int64_t n, int S,
+                       int64_t *__restrict__ offset) {
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  for (int64_t r = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; r <= n; r += stride) {
+    int64_t lo = 0, hi = nu;
+    while (lo < hi) {
+      const int64_t mid = (lo + hi) >> 1;
+      if (static_cast<int64_t>(lk[mid] >> S) < r) lo = mid + 1; else hi = mid;
+    }
+    offset[r] = lo;
+  }
+}
+
+__global__ void __launch_bounds__(256)
+    csr_cols_kernel(const uint64_t *__restrict__ lk, int64_t nu, int S, int64_t *__restrict__ nonzero) {
+  const uint64_t mask = (uint64_t(1) << S) - 1;
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  for (int64_t e = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; e < nu; e += stride)
+    nonzero[e] = static_cast<int64_t>(lk[e] & mask);
+}
+
+}  // namespace
+
+unsigned grid_for(int64_t n) {
+  const int64_t want = (n + 255) / 256, cap = static_cast<int64_t>(num_sms()) * 16;
+  return static_cast<unsigned>(std::max<int64_t>(1, std::min(want, cap)));
+}
+
+size_t up256(size_t x) { return (x + 255) & ~size_t(255); }
+
+size_t ws_bytes(int64_t m, int64_t n, Ws *w, char *base) {
+  const int64_t mm = std::max<int64_t>(m, 1), nn = std::max<int64_t>(n, 1);
+  const int64_t tiles = (std::max(mm, nn) + kTile - 1) / kTile;
+  const int64_t hist_n = tiles * kDigits;
+  const int64_t scan_n = std::max(mm + 1, hist_n);
+  const int64_t nb = (scan_n + kScanBlock - 1) / kScanBlock + 1;
+  size_t o = 0;
+  auto take = [&](size_t bytes) {
+    const size_t at = o;
+    o += up256(bytes);
+    return base ? base + at : nullptr;
+  };
+  char *p;
+  p = take(8 * mm); if (w) w->ka = reinterpret_cast<uint64_t *>(p);
+  p = take(8 * mm); if (w) w->kb = reinterpret_cast<uint64_t *>(p);
+  p = take(8 * nn); if (w) w->va = reinterpret_cast<uint64_t *>(p);
+  p = take(8 * nn); if (w) w->vb = reinterpret_cast<uint64_t *>(p);
+  p = take(4 * (mm + 1)); if (w) w->flag = reinterpret_cast<uint32_t *>(p);
+  p = take(4 * (mm + 1)); if (w) w->pos = reinterpret_cast<uint32_t *>(p);
+  p = take(4 * hist_n); if (w) w->hist = reinterpret_cast<uint32_t *>(p);
+  p = take(4 * hist_n); if (w) w->hoff = reinterpret_cast<uint32_t *>(p);
+  p = take(4 * nb); if (w) w->bsum = reinterpret_cast<uint32_t *>(p);
+  p = take(4 * nn); if (w) w->deg = reinterpret_cast<uint32_t *>(p);
+  p = take(4 * nn); if (w) w->newid = reinterpret_cast<uint32_t *>(p);
+  p = take(64); if (w) w->words = reinterpret_cast<unsigned int *>(p);
+  return o;
+}
+
+int excl_scan(const uint32_t *in, uint32_t *out, int64_t n, uint32_t *bsum, unsigned int *total, cudaStream_t st) {
+  const int64_t nb = std::max<int64_t>(1, (n + kScanBlock - 1) / kScanBlock);
+  scan_blocksum_kernel<<<static_cast<unsigned>(nb), kScanThreads, 0, st>>>(in, n, bsum);
+  scan_top_kernel<<<1, kScanThreads, 0, st>>>(bsum, nb, total);
+  scan_apply_kernel<<<static_cast<unsigned>(nb), kScanThreads, 0, st>>>(in, n, bsum, out);
+  BALE_CUDA_OK(cudaGetLastError());
+  return BALE_OK;
+}
+
+int radix_pass(const uint64_t *a, uint64_t *b, int64_t n, int shift, Ws &w, cudaStream_t st) {
+  if (n < 1) return BALE_OK;
+  const int64_t tiles = (n + kTile - 1) / kTile;
+  radix_hist_kernel<<<static_cast<unsigned>(tiles), kThreads, 0, st>>>(a, n, shift, w.hist, tiles);
+  const int rc = excl_scan(w.hist, w.hoff, tiles * kDigits, w.bsum, w.words, st);
+  if (rc != BALE_OK) return rc;
+  radix_scatter_kernel<<<static_cast<unsigned>(tiles), kThreads, 0, st>>>(a, b, n, shift, w.hoff, tiles);
+  BALE_CUDA_OK(cudaGetLastError());
+  return BALE_OK;
+}
+
+int label_bits(int64_t n) {
+  int S = 1;
+  while ((int64_t(1) << S) < n) S++;
+  return S;
+}
+
+int csr_from_keys(const uint64_t *sk, int64_t nk, int64_t nrows, int S, int64_t *offset, int64_t *nonzero,
+                  cudaStream_t st) {
+  csr_offsets_kernel<<<grid_for(nrows + 1), 256, 0, st>>>(sk, nk, nrows, S, offset);
+  if (nonzero && nk > 0) csr_cols_kernel<<<grid_for(nk), 256, 0, st>>>(sk, nk, S, nonzero);
+  BALE_CUDA_OK(cudaGetLastError());
+  return BALE_OK;
+}
+
+uint64_t *radix_sort(uint64_t *a, uint64_t *b, int64_t n, int bits, Ws &w, cudaStream_t st, int *rc) {
+  *rc = BALE_OK;
+  if (n <= 1) return a;
+  for (int shift = 0; shift < bits; shift += kDigitBits) {
+    *rc = radix_pass(a, b, n, shift, w, st);
+    if (*rc != BALE_OK) return a;
+    std::swap(a, b);
+  }
+  return a;
+}
+
+}  // namespace bale

@@ -1,0 +1,46 @@
+// sort.cuh -- the stable LSD radix sort of 64-bit keys and the u32
+// exclusive scan, shared by the graph build (graph.cu) and spmat's
+// operations (spmat.cu).
+#pragma once
+
+#include "common.cuh"
+
+namespace bale {
+
+constexpr int kSortThreads = 256;                   // threads per sort block: one digit each
+constexpr int kSortPer = 16;                        // keys per thread per tile
+constexpr int64_t kTile = kSortThreads * kSortPer;  // 4096 keys per sort block
+constexpr int kDigitBits = 8;
+constexpr int kDigits = 1 << kDigitBits;
+constexpr int kScanThreads = 1024;
+constexpr int64_t kScanBlock = kScanThreads * 4;    // elements per scan block
+
+// Workspace of one graph build: two key buffers (m), flags and positions
+// (m + 1), the sort histogram and its scan, degrees, labels, vertex keys (n
+// each).  The sort and the scan use hist, hoff, bsum and words only.
+struct Ws {
+  uint64_t *ka, *kb, *va, *vb;
+  uint32_t *flag, *pos, *hist, *hoff, *bsum, *deg, *newid;
+  unsigned int *words;  // [0] scan total, [1] max degree
+};
+
+size_t up256(size_t x);
+// Blocks for a grid-stride loop over n items (at most 16 per SM).
+unsigned grid_for(int64_t n);
+// Bytes of a Ws for m edge keys and n vertices; with base, also lays it out in w.
+size_t ws_bytes(int64_t m, int64_t n, Ws *w, char *base);
+// out[0,n) = exclusive prefix of in[0,n); *total = the sum.
+int excl_scan(const uint32_t *in, uint32_t *out, int64_t n, uint32_t *bsum, unsigned int *total, cudaStream_t st);
+// One stable pass over the 8 bits from `shift`: a into b.
+int radix_pass(const uint64_t *a, uint64_t *b, int64_t n, int shift, Ws &w, cudaStream_t st);
+// Bits for labels [0, n): the least S with 2^S >= n (at least 1).
+int label_bits(int64_t n);
+// A CSR read off keys sorted by row: key = row << S | column (low S bits).
+// offset[r] = the first key of row >= r (r in [0, nrows]); nonzero[e] = the
+// column of key e (skipped when nonzero is null).
+int csr_from_keys(const uint64_t *sk, int64_t nk, int64_t nrows, int S, int64_t *offset, int64_t *nonzero,
+                  cudaStream_t st);
+// Stable sort of n keys on bits [0, bits); returns the buffer holding the result.
+uint64_t *radix_sort(uint64_t *a, uint64_t *b, int64_t n, int bits, Ws &w, cudaStream_t st, int *rc);
+
+}  // namespace bale

@@ -8,7 +8,7 @@
  * and read_matrix_mm_to_dist (:217-370) reads "coordinate" files whose field
  * is "pattern" or "integer" (the value is ignored), 1-based, keeping the file
  * order of the nonzeros within each row.  The body is parsed on the device
- * (spmat.cu); here are the writers and the header readers.
+ * (spmat_io.cu); here are the writers and the header readers.
  */
 #include <ctype.h>
 #include <inttypes.h>

@@ -219,6 +219,24 @@ __global__ void __launch_bounds__(256)
     nonzero[e] = static_cast<int64_t>(lk[e] & mask);
 }
 
+// CSR checks shared by transpose, permute and the dataset writer and reader: offsets ascending inside
+// [0, nnz] with offset[numrows] == nnz, columns inside [0, numcols).
+__global__ void __launch_bounds__(256)
+    csr_check_kernel(const int64_t *__restrict__ off, const int64_t *__restrict__ col, int64_t numrows,
+                     int64_t numcols, int64_t nnz, unsigned long long *__restrict__ bad) {
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  unsigned long long nb = 0;
+  for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i <= numrows; i += stride) {
+    const int64_t o = off[i];
+    if (o < 0 || o > nnz || (i < numrows && off[i + 1] < o) || (i == numrows && o != nnz) || (i == 0 && o != 0))
+      nb++;
+  }
+  for (int64_t k = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; k < nnz; k += stride)
+    if (col[k] < 0 || col[k] >= numcols) nb++;
+  nb = warp_sum_u64(nb);
+  if (lane_id() == 0 && nb) atomicAdd(bad, nb);
+}
+
 }  // namespace
 
 unsigned grid_for(int64_t n) {
@@ -288,6 +306,11 @@ int csr_from_keys(const uint64_t *sk, int64_t nk, int64_t nrows, int S, int64_t 
   if (nonzero && nk > 0) csr_cols_kernel<<<grid_for(nk), 256, 0, st>>>(sk, nk, S, nonzero);
   BALE_CUDA_OK(cudaGetLastError());
   return BALE_OK;
+}
+
+void launch_csr_check(const int64_t *off, const int64_t *col, int64_t numrows, int64_t numcols, int64_t nnz,
+                      unsigned long long *bad, cudaStream_t st) {
+  csr_check_kernel<<<grid_for(std::max(numrows + 1, nnz)), 256, 0, st>>>(off, col, numrows, numcols, nnz, bad);
 }
 
 uint64_t *radix_sort(uint64_t *a, uint64_t *b, int64_t n, int bits, Ws &w, cudaStream_t st, int *rc) {

@@ -1,6 +1,6 @@
-// sort.cuh -- the stable LSD radix sort of 64-bit keys and the u32
-// exclusive scan, shared by the graph build (graph.cu) and spmat's
-// operations (spmat.cu).
+// sort.cuh -- the stable LSD radix sort of 64-bit keys, the u32 exclusive
+// scan and the CSR helpers shared by the graph build (graph.cu) and spmat's
+// operations (spmat.cu, randperm.cu, spmat_io.cu).
 #pragma once
 
 #include "common.cuh"
@@ -40,6 +40,11 @@ int label_bits(int64_t n);
 // column of key e (skipped when nonzero is null).
 int csr_from_keys(const uint64_t *sk, int64_t nk, int64_t nrows, int S, int64_t *offset, int64_t *nonzero,
                   cudaStream_t st);
+// Adds to *bad the malformed entries of a CSR: offsets not ascending inside
+// [0, nnz] with offset[0] = 0 and offset[numrows] = nnz, columns outside
+// [0, numcols).  Asynchronous.
+void launch_csr_check(const int64_t *off, const int64_t *col, int64_t numrows, int64_t numcols, int64_t nnz,
+                      unsigned long long *bad, cudaStream_t st);
 // Stable sort of n keys on bits [0, bits); returns the buffer holding the result.
 uint64_t *radix_sort(uint64_t *a, uint64_t *b, int64_t n, int bits, Ws &w, cudaStream_t st, int *rc);
 

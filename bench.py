@@ -1,7 +1,8 @@
 """Benchmark of the GB300 irregular-access core.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
-                    [--workload ig|ig_zipf|histo|triangles] [--only]
+                    [--workload ig|ig_zipf|histo|triangles|graph|spmat|
+                                batch|batch_small|serve] [--only]
 
 Prints one JSON line (rank 0).  A "step" is one pass of a workload's kernels
 over its whole synthetic input (seeded SplitMix64 streams; R-MAT graph):
@@ -11,13 +12,22 @@ over its whole synthetic input (seeded SplitMix64 streams; R-MAT graph):
 * ig_zipf   : same table, requests Zipf(1.1) over a keyed permutation;
 * histo     : 10^7 uniform updates into 10^6 int64 counters -> GUP/s;
 * triangles : R-MAT scale 22, edge factor 16, (0.57,0.19,0.19,0.05),
-            symmetrised, degree-ordered strictly lower L -> edges/s (nnz(L)/s);
+            symmetrised, degree-ordered strictly lower L -> edges/s (nnz(L)/s),
+            with an Erdos-Renyi 2^20 sub-result (default and merge modes);
+* graph     : the same R-MAT graph generated and built into the
+            degree-ordered lower CSR on the device -> G input edges/s;
+* spmat     : transpose and permutation of that matrix, random
+            permutations of 2^26 (agi and exstack), MatrixMarket read and
+            binary dataset write/read -> G nonzeros/s (transpose headline);
 * batch     : the uneven 512-instance mix (256 histo, 192 ig, 64 R-MAT
             triangle instances) in one CUDA graph, against the same instances
-            launched one by one -> G items/s (updates + requests + edges).
+            launched one by one -> G items/s (updates + requests + edges);
+* batch_small: the same kinds with small instances (launch-bound mix);
+* serve     : Poisson arrivals against resident tables, counters and graphs,
+            rates swept to saturation -> G items/s with p50/p99 latency.
 
 The headline workload fills the top-level keys; unless --only is given the
-other three are measured in the same run and reported under "workloads".
+others are measured in the same run and reported under "workloads".
 
 ``value``: device time from CUDA events on the launching stream, inputs
 resident in HBM, W warm-up steps then K timed steps.  The ig index/output
@@ -494,9 +504,11 @@ def run_graph(ctx) -> dict:
 
 
 def run_spmat(ctx) -> dict:
-    """spmat's transpose, permutation and random permutation on the device
-    (the R-MAT scale-22 lower matrix, a 2^26-entry permutation), against the
-    oracle's one-thread restatements of the reference at one PE."""
+    """spmat's transpose, permutation and random permutations on the device
+    (the R-MAT scale-22 lower matrix, 2^26-entry permutations), the
+    MatrixMarket reader (scale-20 file) and the binary dataset writer and
+    reader (scale 22), against the oracle's one-thread restatements of the
+    reference at one PE."""
     import torch
 
     bale, dev, args = ctx["bale"], ctx["dev"], ctx["args"]

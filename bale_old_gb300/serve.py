@@ -130,4 +130,4 @@ def poisson_arrivals(n: int, rate_per_s: float, seed: int) -> np.ndarray:
     if rate_per_s <= 0:
         return np.zeros(n)
     rng = np.random.default_rng(seed)
-    return np.cumsum(rng.exponential(1.0 / rate_per_s, size=n)) - 0.0
+    return np.cumsum(rng.exponential(1.0 / rate_per_s, size=n))

@@ -5,11 +5,11 @@
 // leave most of the GPU idle and every launch pays its fixed cost.  Here a
 // host planner cuts every instance into tiles (tasks) sized per kind and size
 // class (the batch.* tuning knobs, set by the autotuner), orders them
-// longest-first, and one persistent kernel -- one 512-thread block per SM,
-// 192 KiB of shared memory -- pulls tasks from a device queue until it is
-// empty:
+// longest-first, and one persistent kernel -- two 512-thread blocks per SM,
+// 96 KiB of shared memory and 64 registers a thread -- pulls tasks from a
+// device queue until it is empty:
 //
-//   histo, table <= 48 Ki counters : the task's updates are counted in a
+//   histo, table <= 24 Ki counters : the task's updates are counted in a
 //                                    shared-memory copy of the table, then
 //                                    flushed with one L2 reduction per counter;
 //   histo, larger table            : plain red.global.add.u64 per update;

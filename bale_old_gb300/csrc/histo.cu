@@ -9,11 +9,16 @@
 //    copy of the whole table in shared memory, counts its slice of updates
 //    with shared-memory atomics, then flushes the non-zero counters to HBM
 //    with one L2 reduction each;
-//  * larger tables: updates are warp-aggregated (__match_any_sync groups the
-//    lanes that hit the same counter, the leader adds the group size with a
-//    single fire-and-forget L2 reduction, red.global.add.u64).  For tables
-//    that live in L2 this is bound by L2 atomic throughput, otherwise by one
-//    DRAM sector read and write-back per update.
+//  * larger tables: one fire-and-forget L2 reduction per update
+//    (red.global.add.u64).  For tables that live in L2 this is bound by the
+//    L2 reduction rate, otherwise by one DRAM sector read and write-back per
+//    update;
+//  * tables well beyond L2: the updates are first partitioned by 16 MiB
+//    region (ig_part.cu's partition), so the reductions of one region at a
+//    time stay in L2;
+//  * skewed updates (mode 1, chosen by the tuner or the caller): the lanes
+//    that hit the same counter are grouped with __match_any_sync and the
+//    leader adds the group size with one reduction.
 //
 // The drop-ins ADD into the caller's counts (apps/histo_src/histo.upc:210-213
 // relies on accumulation across models).

@@ -1,5 +1,7 @@
-// tri_wedge.cu -- triangle counting by wedge probes at the far vertex (the
-// default mode for matrices below 2^32 rows and nonzeros).
+// tri_wedge.cu -- triangle counting by wedge probes at the far vertex, for
+// matrices below 2^32 rows and nonzeros.  The default mode runs it for every
+// such matrix below 2^23 nonzeros, and above that when the device-side
+// choice in triangle.cu finds the graph has hubs (pulls well above pushes).
 //
 // The count is the reference's alg 0 (apps/triangle_src/triangle_agi.upc:69-99):
 // the sum over nonzeros L[i][j] of |row_i and row_j|.  Rows ascend and row j

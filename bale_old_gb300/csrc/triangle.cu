@@ -19,6 +19,11 @@
 // smaller partner in row i).  Inputs are validated on the fly: a malformed
 // row offset, a column outside [0,i) or a non-ascending row is counted in
 // *bad and skipped, so no access ever leaves the arrays.
+//
+// This file also holds launch_triangle, which dispatches tri.mode 0 (this
+// merge kernel), 1 (tri_hybrid.cu), 2 (tri_wedge.cu) and the default, whose
+// per-graph choice between wedges and the hybrid is made on the device
+// (tri_choose_kernel below).
 #include "common.cuh"
 
 namespace bale {

@@ -10,6 +10,12 @@
 // whole number of resident waves over the SMs.  The table loads can carry an
 // L2 evict-last policy so that the part of the table that fits in L2 stays
 // there while the streams pass through.
+//
+// launch_ig dispatches: this direct gather for tables that fit L2 and for
+// short request streams; for large tables with many requests (the
+// ig.part_min_* knobs) the region-partitioned gather of ig_part.cu, preceded
+// by its device-side skew test, which hands strongly skewed streams back to
+// the direct gather here.
 #include "common.cuh"
 
 namespace bale {

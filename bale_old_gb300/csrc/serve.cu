@@ -16,9 +16,10 @@
 //    instead of waiting for it to finish;
 //  * a request large enough to fill the GPU by itself (the batched form's
 //    standalone rule) skips the queue: it runs as its own specialised kernels
-//    (region-partitioned ig / histo, the heavy/light triangle kernels over the
-//    graph's resident 32-bit column copy) on one of a few express streams,
-//    concurrently with the ticks;
+//    (region-partitioned ig / histo; for a graph, the wedge count kernel over
+//    the prepared form built at registration, or beyond the wedge kernels'
+//    32-bit limits the hybrid's heavy/light kernels over its resident column
+//    copy) on one of a few express streams, concurrently with the ticks;
 //  * when a request's last task has run, its result is copied back on a copy
 //    stream (ig values, the triangle count) and its arena space is freed.
 //

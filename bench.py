@@ -31,8 +31,9 @@ others are measured in the same run and reported under "workloads".
 
 ``value``: device time from CUDA events on the launching stream, inputs
 resident in HBM, W warm-up steps then K timed steps.  The ig index/output
-streams (2 GiB each) exceed L2; for histo and triangles, whose inputs fit
-in L2, a 256 MiB buffer is rewritten between timed steps (outside the events).
+streams (2 GiB each) and the triangle CSR (513 MiB) exceed L2; for histo,
+whose inputs fit in L2, and for triangles too, a 256 MiB buffer is
+rewritten between timed steps (outside the events).
 ``e2e``: the same metric through the reference-facing C ABI (ig_agi,
 histo_agi, triangle_agi) with pinned host buffers, copies inside the timed
 region.  ``cpu_baseline``: the oracle restatement of the reference's AGI loop

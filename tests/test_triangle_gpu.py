@@ -15,7 +15,8 @@ DROPINS = ("triangle_agi", "triangle_exstack_push", "triangle_exstack2_push",
 @pytest.fixture(params=[0, 1, 2], ids=["merge", "hybrid", "wedge"])
 def mode(request, bale):
     """tri.mode 0: warp-per-row merge for every row; 1: bitmap/search hybrid
-    over rows i; 2 (the default): wedge probes grouped at the far vertex j."""
+    over rows i; 2: wedge probes grouped at the far vertex j (what the
+    default runs below 2^23 nonzeros, and above for graphs with hubs)."""
     bale.tune_set("tri.mode", request.param)
     yield request.param
     bale.tune_set("tri.mode", -1)

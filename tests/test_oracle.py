@@ -201,6 +201,39 @@ def test_spmat_restatements_match_reference_on_fresh_inputs(oracle, bale):
                                           ref.rand_perm_exstack(5000 + seed, seed, b), err_msg=str(b))
 
 
+def _small_matrices(r: int, c: int, descending: bool):
+    """Every r x c 0/1 matrix as a CSR, each row's columns ascending or descending."""
+    for mask in range(1 << (r * c)):
+        rows = [[j for j in range(c) if mask >> (i * c + j) & 1] for i in range(r)]
+        if descending:
+            rows = [row[::-1] for row in rows]
+        off = np.zeros(r + 1, np.int64)
+        off[1:] = np.cumsum([len(x) for x in rows])
+        yield off, np.array([j for x in rows for j in x], np.int64)
+
+
+@pytest.mark.skipif(not REF_LIB.exists(), reason="oracle/_ref is built only where the reference tree exists")
+def test_spmat_restatements_match_reference_on_every_small_matrix(oracle):
+    import itertools
+
+    ref = Reference()
+    for r, c in [(3, 3), (2, 4), (4, 2), (1, 5), (5, 1)]:
+        for desc in (False, True):
+            for off, col in _small_matrices(r, c, desc):
+                to, tc = oracle.transpose(off, col, c)
+                ro, rc = ref.transpose(off, col, c)
+                assert np.array_equal(to, ro) and np.array_equal(tc, rc), (r, c, desc, off, col)
+    for r, c in [(3, 3), (2, 4), (4, 2)]:
+        mats = list(_small_matrices(r, c, False))[::37] + list(_small_matrices(r, c, True))[-1:]
+        for rp in itertools.permutations(range(r)):
+            for cp in itertools.permutations(range(c)):
+                rinv, cinv = np.array(rp, np.int64), np.array(cp, np.int64)
+                for off, col in mats:
+                    po, pc = oracle.permute(off, col, rinv, cinv)
+                    qo, qc = ref.permute(off, col, c, rinv, cinv)
+                    assert np.array_equal(po, qo) and np.array_equal(pc, qc), (rp, cp, off, col)
+
+
 def test_matrix_market_reader_matches_reference_golden(oracle, golden):
     from pathlib import Path
 

@@ -464,6 +464,19 @@ int rand_perm_darts(int64_t n, uint64_t seed, int64_t per_round, int64_t *d_perm
   return BALE_EINVAL;
 }
 
+// The reference reseeds only when its int seed is nonzero (spmat_agi.upc:61,
+// spmat_exstack.upc:92); with 0 it continues the C library's drand48 stream
+// from wherever the caller left it.  The device path always starts from
+// srand48(seed), so it refuses such a seed rather than return a permutation
+// the reference would not.
+bool refuse_stream_seed(uint64_t seed, const char *who) {
+  if ((seed & 0xffffffffull) != 0) return false;
+  set_error("%s: seed 0 (low 32 bits) continues the C library's drand48 stream in the reference; "
+            "pass a nonzero seed",
+            who);
+  return true;
+}
+
 }  // namespace
 }  // namespace bale
 
@@ -476,7 +489,8 @@ int bale_rand_perm_dev(int64_t n, uint64_t seed, int64_t *d_perm, void *stream) 
     set_error("bale_rand_perm_dev: bad arguments (n=%lld)", static_cast<long long>(n));
     return BALE_EINVAL;
   }
-  if (n == 0) return BALE_OK;
+  if (n == 0) return BALE_OK;  // the reference draws nothing either
+  if (refuse_stream_seed(seed, "bale_rand_perm_dev")) return BALE_EINVAL;
   return rand_perm_darts(n, seed, 0, d_perm, static_cast<cudaStream_t>(stream), "bale_rand_perm_dev");
 }
 
@@ -486,7 +500,8 @@ int bale_rand_perm_exstack_dev(int64_t n, uint64_t seed, int64_t buf_cnt, int64_
               static_cast<long long>(buf_cnt));
     return BALE_EINVAL;
   }
-  if (n == 0) return BALE_OK;
+  if (n == 0) return BALE_OK;  // the reference draws nothing either
+  if (refuse_stream_seed(seed, "bale_rand_perm_exstack_dev")) return BALE_EINVAL;
   // a buffer that holds every dart never fills: the same as one of n
   return rand_perm_darts(n, seed, std::min(buf_cnt, n), d_perm, static_cast<cudaStream_t>(stream),
                          "bale_rand_perm_exstack_dev");

@@ -207,12 +207,18 @@ BALE_API int bale_gen_rmat_dev(int64_t scale, int64_t edgefactor, double a, doub
 /*    keep their order; d_poffset[numrows+1], d_pnonzero[nnz];               */
 /*  * bale_rand_perm_dev: rand_permp_agi(n, seed) (spmat/spmat_agi.upc:      */
 /*    56-107): the permutation the reference's dart throwing yields from     */
-/*    lrand48 after srand48(seed) (seed 0 is taken as srand48(0));           */
+/*    lrand48 after srand48(seed);                                          */
 /*  * bale_rand_perm_exstack_dev: rand_permp_exstack(n, seed, buf_cnt)        */
 /*    (spmat/spmat_exstack.upc:62-190), whose darts fly in rounds of buf_cnt; */
 /*    rand_permp(n, seed) (spmat/spmat_utils.upc:63-74) is buf_cnt = 1024.    */
 /*    A different permutation from rand_permp_agi's for the same seed.       */
-/* Both random permutations take 0 <= n < 2^30.                             */
+/* Both random permutations take 0 <= n < 2^30.  Only the low 32 bits of   */
+/* seed count (the reference's seed is an int).  A seed whose low 32 bits   */
+/* are 0 is refused with BALE_EINVAL for n > 0: the reference does not      */
+/* reseed then but continues the C library's drand48 stream from wherever   */
+/* the caller left it (spmat_agi.upc:61, spmat_exstack.upc:92), and these   */
+/* always start from srand48(seed).  Neither advances the C library's       */
+/* stream, which the reference leaves just past its last draw.              */
 /* BALE_EINPUT for malformed offsets or columns, or a rperminv/cperminv     */
 /* that is not a permutation.                                               */
 BALE_API int bale_transpose_dev(const int64_t *d_offset, const int64_t *d_nonzero, int64_t numrows,

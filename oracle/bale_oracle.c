@@ -269,22 +269,53 @@ void orc_permute(const int64_t *offset, const int64_t *nonzero, int64_t numrows,
   free(rperm);
 }
 
-/* rand_permp_agi (spmat/spmat_agi.upc:56-107) at THREADS = 1 with seed != 0.
+/* The random permutations draw from the C library's drand48 stream and
+ * reseed it only when seed != 0 (spmat_agi.upc:61, spmat_exstack.upc:92:
+ * `if (seed != 0) srand48(seed)`).  With seed 0 they continue from the state
+ * the caller left, and with any seed they leave the stream just past their
+ * last draw, where a later lrand48() or seed-0 call picks it up.  These two
+ * read and write that state: seed48 installs a state and returns the
+ * previous one, so a second call puts it back untouched. */
+static uint64_t libc_drand48_state(void) {
+  unsigned short probe[3] = {0, 0, 0};
+  const unsigned short *prev = seed48(probe);
+  unsigned short keep[3] = {prev[0], prev[1], prev[2]};
+  seed48(keep);
+  return (uint64_t)keep[0] | (uint64_t)keep[1] << 16 | (uint64_t)keep[2] << 32;
+}
+
+static void set_libc_drand48_state(uint64_t x) {
+  unsigned short s[3] = {(unsigned short)(x & 0xffff), (unsigned short)(x >> 16 & 0xffff),
+                         (unsigned short)(x >> 32 & 0xffff)};
+  seed48(s);
+}
+
+/* The reference's seed is an int: only the low 32 bits count, for the test
+ * against 0 as for srand48. */
+static int continues_stream(int64_t seed) { return ((uint64_t)seed & 0xffffffffull) == 0; }
+
+static uint64_t drand48_start(int64_t seed) {
+  return continues_stream(seed) ? libc_drand48_state() : ((((uint64_t)seed & 0xffffffffull) << 16) | 0x330eull);
+}
+
+/* rand_permp_agi (spmat/spmat_agi.upc:56-107) at THREADS = 1.
  * The drand48 family is the 48-bit linear congruential generator POSIX
  * specifies: srand48(s) sets X = (s & 0xffffffff) << 16 | 0x330e, and each
- * lrand48() steps X = (0x5deece66d X + 0xb) mod 2^48 and returns X >> 17. */
+ * lrand48() steps X = (0x5deece66d X + 0xb) mod 2^48 and returns X >> 17.
+ * Seed 0 continues the C library's stream (drand48_start above). */
 int orc_rand_perm(int64_t n, int64_t seed, int64_t *perm) {
   const int64_t m = 2 * n;
   int64_t *target = (int64_t *)malloc((size_t)(m > 0 ? m : 1) * sizeof(int64_t));
   if (!target) return -1;
   for (int64_t i = 0; i < m; i++) target[i] = -1;
-  uint64_t x = (((uint64_t)seed & 0xffffffffull) << 16) | 0x330eull;
+  uint64_t x = drand48_start(seed);
   int64_t i = 0;
   while (i < n) {
     x = (0x5deece66dull * x + 0xbull) & ((1ull << 48) - 1);
     const int64_t r = (int64_t)(x >> 17) % m;
     if (target[r] == -1) target[r] = i++;
   }
+  set_libc_drand48_state(x); /* where the reference leaves the C library's stream */
   int64_t pos = 0;
   for (int64_t s = 0; s < m; s++)
     if (target[s] != -1) perm[pos++] = target[s];
@@ -292,8 +323,8 @@ int orc_rand_perm(int64_t n, int64_t seed, int64_t *perm) {
   return 0;
 }
 
-/* rand_permp_exstack (spmat/spmat_exstack.upc:62-190) at THREADS = 1 with
- * seed != 0; rand_permp (spmat/spmat_utils.upc:63-74) is this with
+/* rand_permp_exstack (spmat/spmat_exstack.upc:62-190) at THREADS = 1 (seed 0
+ * continues the C library's drand48 stream); rand_permp (spmat/spmat_utils.upc:63-74) is this with
  * buf_cnt = 1024.  Darts wait in a list, initially 0..n-1.  Each round
  * throws the pending darts in list order into a buffer of buf_cnt packages
  * {slot = lrand48() % 2n, dart}; the draw that finds the buffer full is lost
@@ -313,7 +344,7 @@ int orc_rand_perm_exstack(int64_t n, int64_t seed, int64_t buf_cnt, int64_t *per
   if (!target || !list || !slot || !dart) goto done;
   for (int64_t i = 0; i < m; i++) target[i] = -1;
   for (int64_t i = 0; i < n; i++) list[i] = i;
-  uint64_t x = (((uint64_t)seed & 0xffffffffull) << 16) | 0x330eull;
+  uint64_t x = drand48_start(seed);
   int64_t iend = 0;
   while (iend != n) {
     int64_t i = iend, cnt = 0;
@@ -332,6 +363,7 @@ int orc_rand_perm_exstack(int64_t n, int64_t seed, int64_t buf_cnt, int64_t *per
     }
     for (int64_t k = 0; k < back; k++) list[--iend] = dart[k];
   }
+  set_libc_drand48_state(x); /* where the reference leaves the C library's stream */
   int64_t pos = 0;
   for (int64_t s = 0; s < m; s++)
     if (target[s] != -1) perm[pos++] = target[s];

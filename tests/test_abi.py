@@ -52,3 +52,19 @@ def test_sparsemat_layout_matches_reference():
 def test_version_and_error_calls_need_no_gpu(bale):
     assert "sm_103a" in bale.version()
     assert isinstance(bale._last_error(), str)
+
+
+def test_random_permutations_refuse_a_stream_continuing_seed(bale):
+    """A seed whose low 32 bits are 0 makes the reference continue the C
+    library's drand48 stream instead of reseeding; the device entry points
+    refuse it before any device work (n = 0 draws nothing and is accepted)."""
+    from bale_old_gb300._lib import _lib
+
+    fake = C.c_void_p(256)  # never dereferenced: the seed is refused first
+    for seed in (0, 1 << 32, 7 << 32):
+        assert _lib.bale_rand_perm_dev(10, seed, fake, None) == 1
+        assert "seed 0" in bale._last_error()
+        assert _lib.bale_rand_perm_exstack_dev(10, seed, 1024, fake, None) == 1
+        assert "seed 0" in bale._last_error()
+    assert _lib.bale_rand_perm_dev(0, 0, None, None) == 0
+    assert _lib.bale_rand_perm_exstack_dev(0, 0, 1024, None, None) == 0

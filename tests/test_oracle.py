@@ -234,6 +234,84 @@ def test_spmat_restatements_match_reference_on_every_small_matrix(oracle):
                     assert np.array_equal(po, qo) and np.array_equal(pc, qc), (rp, cp, off, col)
 
 
+def _tiny_graphs(nmax: int = 5):
+    """Every strictly lower, ascending CSR on 1..nmax vertices."""
+    for n in range(1, nmax + 1):
+        pairs = [(i, j) for i in range(n) for j in range(i)]
+        for mask in range(1 << len(pairs)):
+            rows = [[] for _ in range(n)]
+            for b, (i, j) in enumerate(pairs):
+                if mask >> b & 1:
+                    rows[i].append(j)
+            off = np.zeros(n + 1, np.int64)
+            off[1:] = np.cumsum([len(r) for r in rows])
+            yield off, np.array([j for r in rows for j in r], np.int64)
+
+
+@pytest.mark.skipif(not REF_LIB.exists(), reason="oracle/_ref is built only where the reference tree exists")
+def test_triangle_restatements_match_every_reference_variant_on_every_tiny_graph(oracle):
+    ref = Reference()
+    for off, col in _tiny_graphs():
+        r = ref.triangles(off, col)
+        cnt, pulls = oracle.triangle_agi(off, col)
+        pcnt, pushes = oracle.triangle_exstack_push(off, col)
+        assert {v[0] for v in r.values()} == {cnt} == {pcnt}, (off, col, r)
+        assert r["triangle_agi"][1] == pulls, (off, col)
+        assert r["triangle_exstack_push"][1] == pushes, (off, col)
+
+
+def _libc():
+    import ctypes
+
+    libc = ctypes.CDLL(None)
+    libc.srand48.argtypes = [ctypes.c_long]
+    libc.srand48.restype = None
+    libc.lrand48.restype = ctypes.c_long
+    return libc
+
+
+@pytest.mark.skipif(not REF_LIB.exists(), reason="oracle/_ref is built only where the reference tree exists")
+def test_rand_perm_seed_zero_continues_the_c_library_stream(oracle):
+    """Seed 0 does not reseed (spmat_agi.upc:61, spmat_exstack.upc:92): the
+    permutation depends on the drand48 state the caller left, and every call
+    leaves the stream just past its last draw.  Sequences of calls from the
+    same starting state, read out with a final lrand48(), must agree."""
+    libc, ref = _libc(), Reference()
+
+    def run(impl, call):
+        if call[0] == "agi":
+            return impl.rand_perm(call[1], call[2])
+        return impl.rand_perm_exstack(call[1], call[2], call[3])
+
+    sequences = [
+        [("agi", 10, 0), ("agi", 1, 0), ("x", 7, 0, 3), ("x", 100, 0, 1024), ("x", 33, 0, 1)],
+        [("agi", 5, 9), ("agi", 12, 0), ("x", 40, 4, 2), ("x", 40, 0, 2), ("agi", 3, 0)],
+        [("x", 1000, 0, 7), ("agi", 1000, 0), ("x", 64, 0, 64), ("x", 65, 0, 64)],
+    ]
+    for start in (0, 5, 123456):
+        for calls in sequences:
+            libc.srand48(start)
+            ours = [run(oracle, c) for c in calls]
+            ours_next = libc.lrand48()
+            libc.srand48(start)
+            theirs = [run(ref, c) for c in calls]
+            theirs_next = libc.lrand48()
+            for c, a, b in zip(calls, ours, theirs):
+                np.testing.assert_array_equal(a, b, err_msg=f"start {start} {c}")
+            assert ours_next == theirs_next, (start, calls)
+
+
+@pytest.mark.skipif(not REF_LIB.exists(), reason="oracle/_ref is built only where the reference tree exists")
+def test_rand_perm_restatements_match_reference_for_small_n(oracle):
+    ref = Reference()
+    for n in range(1, 130):
+        for seed in (1, 77, 2 ** 32 + 5):
+            np.testing.assert_array_equal(oracle.rand_perm(n, seed), ref.rand_perm(n, seed), err_msg=f"{n} {seed}")
+            for b in sorted({1, 2, 3, 7, n, 1024}):
+                np.testing.assert_array_equal(oracle.rand_perm_exstack(n, seed, b), ref.rand_perm_exstack(n, seed, b),
+                                              err_msg=f"{n} {seed} {b}")
+
+
 def test_matrix_market_reader_matches_reference_golden(oracle, golden):
     from pathlib import Path
 

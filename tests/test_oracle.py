@@ -312,6 +312,34 @@ def test_rand_perm_restatements_match_reference_for_small_n(oracle):
                                               err_msg=f"{n} {seed} {b}")
 
 
+@pytest.mark.skipif(not REF_LIB.exists(), reason="oracle/_ref is built only where the reference tree exists")
+def test_file_restatements_match_reference_on_small_matrices(oracle, tmp_path, monkeypatch):
+    """MatrixMarket files the reference writes, and the same entries shuffled,
+    read by both readers; binary datasets written by both writers."""
+    import shutil
+    from pathlib import Path
+
+    ref = Reference()
+    rng = np.random.default_rng(5)
+    monkeypatch.chdir(tmp_path)  # short relative names: the reference's file names are 64-byte buffers
+    for r, c in [(3, 3), (2, 4), (4, 2)]:
+        for k, (off, col) in enumerate(_small_matrices(r, c, False)):
+            ref.write_mm(off, col, c, "a.mm")
+            lines = Path("a.mm").read_text().splitlines()
+            body = lines[2:]
+            Path("s.mm").write_text("\n".join(lines[:2] + [body[i] for i in rng.permutation(len(body))]) + "\n")
+            for path in ("a.mm", "s.mm"):
+                oo, oc, onc = oracle.read_mm(path)
+                ro, rc, rnc = ref.read_mm(path)
+                assert onc == rnc == c and np.array_equal(oo, ro) and np.array_equal(oc, rc), (r, c, k, path)
+            oracle.write_dataset(off, col, c, "o")
+            ref.write_dataset(off, col, c, "r")
+            for name in ("metadata", "rowcnt_0", "nonzero_0"):
+                assert Path("o", name).read_bytes() == Path("r", name).read_bytes(), (r, c, k, name)
+            shutil.rmtree("o")
+            shutil.rmtree("r")
+
+
 def test_matrix_market_reader_matches_reference_golden(oracle, golden):
     from pathlib import Path
 

@@ -313,6 +313,43 @@ def test_rand_perm_restatements_match_reference_for_small_n(oracle):
 
 
 @pytest.mark.skipif(not REF_LIB.exists(), reason="oracle/_ref is built only where the reference tree exists")
+def test_histo_and_ig_restatements_match_every_reference_variant_on_tiny_inputs(oracle):
+    """Every index array of length 1..4 over tables of 1..3 entries, through
+    the reference's agi, exstack and exstack2 variants (buffers of 1 and
+    1024) and the oracle."""
+    import ctypes as C
+    import itertools
+
+    ref = Reference()
+    P = lambda a: a.ctypes.data_as(C.POINTER(C.c_int64))  # noqa: E731
+    for t in (1, 2, 3):
+        table = -(np.arange(t, dtype=np.int64) + 1) * 1000003
+        for length in (1, 2, 3, 4):
+            for idx in itertools.product(range(t), repeat=length):
+                index = np.array(idx, np.int64)
+                pck = index << 16
+                want = np.zeros(t, np.int64)
+                oracle.histo_agi(index, want)
+                got = np.zeros(t, np.int64)
+                assert ref.lib.histo_agi(P(index), length, P(got)) >= 0
+                np.testing.assert_array_equal(got, want)
+                for fn in ("histo_exstack", "histo_exstack2"):
+                    for b in (1, 1024):
+                        got = np.zeros(t, np.int64)
+                        assert getattr(ref.lib, fn)(P(pck), length, P(got), b) >= 0
+                        np.testing.assert_array_equal(got, want, err_msg=f"{fn} {b} {idx}")
+                gather = oracle.ig_agi(index, table)
+                tgt = np.zeros(length, np.int64)
+                assert ref.lib.ig_agi(P(tgt), P(index), length, P(table)) >= 0
+                np.testing.assert_array_equal(tgt, gather)
+                for fn in ("ig_exstack", "ig_exstack2"):
+                    for b in (1, 1024):
+                        tgt = np.zeros(length, np.int64)
+                        assert getattr(ref.lib, fn)(P(tgt), P(pck), length, P(table), b) >= 0
+                        np.testing.assert_array_equal(tgt, gather, err_msg=f"{fn} {b} {idx}")
+
+
+@pytest.mark.skipif(not REF_LIB.exists(), reason="oracle/_ref is built only where the reference tree exists")
 def test_file_restatements_match_reference_on_small_matrices(oracle, tmp_path, monkeypatch):
     """MatrixMarket files the reference writes, and the same entries shuffled,
     read by both readers; binary datasets written by both writers."""

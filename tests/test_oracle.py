@@ -271,6 +271,30 @@ def _libc():
 
 
 @pytest.mark.skipif(not REF_LIB.exists(), reason="oracle/_ref is built only where the reference tree exists")
+def test_reference_alg_1_counts_equal_alg_0(oracle, bale):
+    """The drop-ins compute alg 0 from L for either alg; the reference's alg 1
+    (L and U*L with U = L^T, triangle_agi.upc:100-136) must count the same,
+    in every variant, on every tiny graph and on R-MAT graphs."""
+    import ctypes as C
+
+    ref = Reference()
+    graphs = list(_tiny_graphs())
+    for scale, seed in ((9, 3), (10, 4)):
+        L = bale.gen_rmat(scale, 16, 0.57, 0.19, 0.19, seed)
+        graphs.append((L.offset, L.nonzero))
+    for off, col in graphs:
+        n = off.size - 1
+        uo, uc = oracle.transpose(off, col, n)
+        want = oracle.triangle_agi(off, col)[0]
+        Lm, Um = ref._mat(off, col), ref._mat(uo, uc)  # square: U = L^T has n rows too
+        for name, extra in (("triangle_agi", ()), ("triangle_exstack_push", (1024,)),
+                            ("triangle_exstack2_push", (1024,)), ("triangle_agi_iter", ())):
+            cnt, sr = C.c_int64(0), C.c_int64(0)
+            assert getattr(ref.lib, name)(C.byref(cnt), C.byref(sr), C.byref(Lm), C.byref(Um), 1, *extra) >= 0
+            assert cnt.value == want, (name, off, col)
+
+
+@pytest.mark.skipif(not REF_LIB.exists(), reason="oracle/_ref is built only where the reference tree exists")
 def test_rand_perm_seed_zero_continues_the_c_library_stream(oracle):
     """Seed 0 does not reseed (spmat_agi.upc:61, spmat_exstack.upc:92): the
     permutation depends on the drand48 state the caller left, and every call

@@ -197,6 +197,8 @@ class Reference:
             "triangle_exstack2_push": (C.c_double, [P64, P64, PS, PS, i64, i64]),
             "triangle_agi_iter": (C.c_double, [P64, P64, PS, PS, i64]),
             "gen_erdos_renyi_graph_dist": (PS, [C.c_int, C.c_double, i64, i64, i64]),
+            "gen_local_mat_from_stars": (PS, [i64, P64, C.c_int]),
+            "kron_prod_dist": (PS, [PS, PS, i64]),
             "clear_matrix": (None, [PS]),
             "transpose_matrix_agi": (PS, [PS]),
             "permute_matrix_agi": (PS, [PS, P64, P64]),
@@ -308,6 +310,25 @@ class Reference:
         """spmat's rand_permp (spmat/spmat_utils.upc:63-74) at one PE."""
         p = self.lib.rand_permp(n, seed)
         return np.ctypeslib.as_array(p, shape=(n,)).copy()
+
+    def kronecker_lower(self, mode: int, specs) -> tuple[np.ndarray, np.ndarray]:
+        """The triangle app's -K graph (apps/triangle_src/triangle.upc:147-168,
+        :297-299): the specs split in half, each half a local product of stars
+        (gen_local_mat_from_stars), combined by kron_prod_dist(B, C, lower=1)
+        (spmat/spmat_utils.upc:813-1049), at one PE."""
+        sp = np.ascontiguousarray(np.asarray(specs, dtype=np.int64))
+        half = sp.size // 2
+        b_spec, c_spec = np.ascontiguousarray(sp[:half]), np.ascontiguousarray(sp[half:])
+        B = self.lib.gen_local_mat_from_stars(b_spec.size, _p(b_spec), mode)
+        Cm = self.lib.gen_local_mat_from_stars(c_spec.size, _p(c_spec), mode)
+        if not B or not Cm:
+            raise RuntimeError("gen_local_mat_from_stars failed")
+        A = self.lib.kron_prod_dist(B, Cm, 1)
+        self.lib.clear_matrix(B)
+        self.lib.clear_matrix(Cm)
+        if not A:
+            raise RuntimeError("kron_prod_dist failed")
+        return self._unpack(A)
 
     def erdos_renyi_lower(self, n: int, p: float, seed: int) -> tuple[np.ndarray, np.ndarray]:
         """spmat's gen_erdos_renyi_graph_dist(n, p, 0, mode 1 = lower, seed)

@@ -271,6 +271,19 @@ def _libc():
 
 
 @pytest.mark.skipif(not REF_LIB.exists(), reason="oracle/_ref is built only where the reference tree exists")
+@pytest.mark.parametrize("mode", [0, 1, 2])
+def test_kronecker_generator_builds_the_reference_graph(bale, mode):
+    """bale_gen_kronecker against the triangle app's own -K construction,
+    nonzero for nonzero: the closed-form counts hold for exactly that graph."""
+    ref = Reference()
+    for specs in ([3, 4], [1, 2, 3], [3, 4, 5, 9], [2, 3, 4, 5, 2], [1, 4, 9, 16], [5, 1, 7]):
+        L = bale.gen_kronecker(mode, specs)
+        ro, rc = ref.kronecker_lower(mode, specs)
+        np.testing.assert_array_equal(L.offset, ro, err_msg=f"{mode} {specs}")
+        np.testing.assert_array_equal(L.nonzero, rc, err_msg=f"{mode} {specs}")
+
+
+@pytest.mark.skipif(not REF_LIB.exists(), reason="oracle/_ref is built only where the reference tree exists")
 def test_reference_alg_1_counts_equal_alg_0(oracle, bale):
     """The drop-ins compute alg 0 from L for either alg; the reference's alg 1
     (L and U*L with U = L^T, triangle_agi.upc:100-136) must count the same,

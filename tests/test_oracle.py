@@ -402,7 +402,11 @@ def test_file_restatements_match_reference_on_small_matrices(oracle, tmp_path, m
             lines = Path("a.mm").read_text().splitlines()
             body = lines[2:]
             Path("s.mm").write_text("\n".join(lines[:2] + [body[i] for i in rng.permutation(len(body))]) + "\n")
-            for path in ("a.mm", "s.mm"):
+            # the integer field: a value after each entry, read and dropped
+            Path("i.mm").write_text("\n".join(["%%MatrixMarket matrix coordinate integer", lines[1]] +
+                                              [f"{e} {int(v)}" for e, v in zip(body, rng.integers(-9, 99, len(body)))])
+                                    + "\n")
+            for path in ("a.mm", "s.mm", "i.mm"):
                 oo, oc, onc = oracle.read_mm(path)
                 ro, rc, rnc = ref.read_mm(path)
                 assert onc == rnc == c and np.array_equal(oo, ro) and np.array_equal(oc, rc), (r, c, k, path)

@@ -70,3 +70,42 @@ def test_dataset_header_reader(bale, tmp_path):
             bale.sparse_matrix_header(tmp_path)
     with pytest.raises(bale.BaleError):
         bale.sparse_matrix_header(tmp_path / "missing")
+
+
+def _small_matrices(r: int, c: int, descending: bool):
+    for mask in range(1 << (r * c)):
+        rows = [[j for j in range(c) if mask >> (i * c + j) & 1] for i in range(r)]
+        if descending:
+            rows = [row[::-1] for row in rows]
+        off = np.zeros(r + 1, np.int64)
+        off[1:] = np.cumsum([len(x) for x in rows])
+        yield off, np.array([j for x in rows for j in x], np.int64)
+
+
+def test_writers_match_reference_bytes_on_every_small_matrix(bale, tmp_path, monkeypatch):
+    """The library's host writers against the reference's own, byte for byte,
+    on every 0/1 matrix of five small shapes with rows in either order; the
+    header readers give back the sizes."""
+    from oracle.pyoracle import REF_LIB, Reference
+
+    if not REF_LIB.exists():
+        pytest.skip("oracle/_ref is built only where the reference tree exists")
+    ref = Reference()
+    monkeypatch.chdir(tmp_path)  # short relative names: the reference's file names are 64-byte buffers
+    import shutil
+
+    for r, c in [(3, 3), (2, 4), (4, 2), (1, 5), (5, 1)]:
+        for desc in (False, True):
+            for off, col in _small_matrices(r, c, desc):
+                L = bale.SparseMatrix(off, col, numcols=c)
+                bale.write_matrix_mm(L, "ours.mm")
+                ref.write_mm(off, col, c, "ref.mm")
+                assert Path("ours.mm").read_bytes() == Path("ref.mm").read_bytes(), (r, c, off, col)
+                assert bale.mm_header("ours.mm") == (r, c, col.size, 2)
+                bale.write_sparse_matrix(L, "o")
+                ref.write_dataset(off, col, c, "r")
+                for name in ("metadata", "rowcnt_0", "nonzero_0"):
+                    assert Path("o", name).read_bytes() == Path("r", name).read_bytes(), (r, c, name)
+                assert bale.sparse_matrix_header("o") == (r, c, col.size, 1)
+                shutil.rmtree("o")
+                shutil.rmtree("r")

@@ -406,7 +406,12 @@ def test_file_restatements_match_reference_on_small_matrices(oracle, tmp_path, m
             Path("i.mm").write_text("\n".join(["%%MatrixMarket matrix coordinate integer", lines[1]] +
                                               [f"{e} {int(v)}" for e, v in zip(body, rng.integers(-9, 99, len(body)))])
                                     + "\n")
-            for path in ("a.mm", "s.mm", "i.mm"):
+            # repeated entries are kept, in file order within each row
+            dup = body + [body[i] for i in rng.integers(0, len(body), len(body) // 2)] if body else []
+            dup = [dup[i] for i in rng.permutation(len(dup))]
+            Path("d.mm").write_text("\n".join(["%%MatrixMarket matrix coordinate pattern", f"{r} {c} {len(dup)}"]
+                                              + dup) + "\n")
+            for path in ("a.mm", "s.mm", "i.mm", "d.mm"):
                 oo, oc, onc = oracle.read_mm(path)
                 ro, rc, rnc = ref.read_mm(path)
                 assert onc == rnc == c and np.array_equal(oo, ro) and np.array_equal(oc, rc), (r, c, k, path)

@@ -68,3 +68,48 @@ def test_random_permutations_refuse_a_stream_continuing_seed(bale):
         assert "seed 0" in bale._last_error()
     assert _lib.bale_rand_perm_dev(0, 0, None, None) == 0
     assert _lib.bale_rand_perm_exstack_dev(0, 0, 1024, None, None) == 0
+
+
+def test_a_c_program_compiles_links_and_runs_against_the_library(tmp_path):
+    """What an app does: include the headers as strict C, link
+    libbale_gb300.so in place of the reference kernels, and resolve every
+    drop-in.  The program only calls bale_version(), which needs no GPU."""
+    import shutil
+    import subprocess
+
+    from bale_old_gb300._lib import LIB_PATH
+
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        import pytest
+
+        pytest.skip("no C compiler")
+    src = tmp_path / "app.c"
+    src.write_text(r'''
+#include <stdio.h>
+#include <string.h>
+#include "bale_gb300.h"
+#include "bale_inputs.h"
+typedef void (*any_fn)(void);
+int main(void) {
+  any_fn dropins[] = {
+    (any_fn)histo_agi, (any_fn)histo_exstack, (any_fn)histo_exstack2, (any_fn)histo_conveyor,
+    (any_fn)ig_agi, (any_fn)ig_exstack, (any_fn)ig_exstack2, (any_fn)ig_conveyor,
+    (any_fn)triangle_agi, (any_fn)triangle_exstack_push, (any_fn)triangle_exstack2_push,
+    (any_fn)triangle_convey_push, (any_fn)triangle_agi_iter};
+  for (size_t i = 0; i < sizeof dropins / sizeof dropins[0]; i++)
+    if (!dropins[i]) return 2;
+  if (sizeof(sparsemat_t) != 80) return 3;
+  printf("%s\n", bale_version());
+  return strstr(bale_version(), "sm_103a") ? 0 : 4;
+}
+''')
+    exe = tmp_path / "app"
+    lib_dir = LIB_PATH.parent
+    build = subprocess.run([cc, "-std=c99", "-Wall", "-Wextra", "-Werror", f"-I{ROOT / 'include'}", str(src),
+                            "-o", str(exe), f"-L{lib_dir}", "-lbale_gb300", f"-Wl,-rpath,{lib_dir}"],
+                           capture_output=True, text=True)
+    assert build.returncode == 0, build.stderr
+    run = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120)
+    assert run.returncode == 0, (run.returncode, run.stdout, run.stderr)
+    assert "sm_103a" in run.stdout

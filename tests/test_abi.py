@@ -113,3 +113,34 @@ int main(void) {
     run = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120)
     assert run.returncode == 0, (run.returncode, run.stdout, run.stderr)
     assert "sm_103a" in run.stdout
+
+
+def test_binding_signatures_match_the_header_prototypes():
+    """Each ctypes signature has as many parameters as the C prototype it
+    binds, and pointer-ness agrees parameter by parameter."""
+    from bale_old_gb300._lib import SIGNATURES
+
+    protos = {}
+    for h in sorted((ROOT / "include").glob("*.h")):
+        text = re.sub(r"/\*.*?\*/", "", h.read_text(), flags=re.S)
+        text = re.sub(r"//[^\n]*", "", text)
+        for m in re.finditer(r"\b([A-Za-z_][A-Za-z0-9_]*)\s*\(([^;{}()]*)\)\s*;", text):
+            params = [p.strip() for p in m.group(2).replace("\n", " ").split(",") if p.strip()]
+            if params == ["void"]:
+                params = []
+            protos[m.group(1)] = params
+    bad = []
+    for name, params in protos.items():
+        if name not in SIGNATURES:
+            continue
+        argtypes = SIGNATURES[name][1]
+        if len(argtypes) != len(params):
+            bad.append((name, len(params), len(argtypes)))
+            continue
+        for p, a in zip(params, argtypes):
+            c_ptr = "*" in p
+            py_ptr = a is C.c_void_p or a is C.c_char_p or hasattr(a, "contents") or \
+                (isinstance(a, type) and issubclass(a, C._Pointer))
+            if c_ptr != py_ptr:
+                bad.append((name, p, a))
+    assert not bad, bad

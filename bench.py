@@ -322,17 +322,25 @@ def run_histo(ctx) -> dict:
     red_ms = time_device(lambda: bale.l2_red_rate(probe, n), args.steps, args.warmup, between)
     red_peak = n / (red_ms / 1e3) / 1e9
     del probe
+    achieved = n / (ms / 1e3) / 1e9
+    dram = ctx["traffic"].get("histo", {}).get("dram_bytes_per_step")
     out = {"metric": "GUP/s histogram (10^9 updates/s)",
            "value": round(job_rate(n, ms_max / 1e3, ctx["dist"].world) / 1e9, 4), "unit": "GUP/s",
            "ms_per_step": round(ms_max, 4), "parity_ok": ok,
-           "roofline": roofline(ctx, "histo", algo, ms / 1e3, "histo_global_kernel (plain L2 reductions)",
-                                note="the 8 MB table is L2-resident: L2 reductions, not HBM, bound this "
-                                     "config (see l2_reduction_roofline)"),
-           "l2_reduction_roofline": {"achieved": round(n / (ms / 1e3) / 1e9, 2),
-                                     "peak": round(red_peak, 2), "unit": "G updates/s",
-                                     "frac": round((n / (ms / 1e3) / 1e9) / red_peak, 4),
-                                     "peak_source": "measured live: bale_l2_red_rate, 10^7 reductions at "
-                                                    "hashed positions of the same 10^6 counters, no index read"},
+           # the 8 MB table is L2-resident, so the bound is the L2's rate of
+           # 64-bit reductions, not HBM: one red.global.add.u64 per update
+           "roofline": {"bound": "l2", "kernel": "histo_global_kernel (plain L2 reductions)",
+                        "achieved": round(achieved, 2), "peak": round(red_peak, 2), "unit": "G reductions/s",
+                        "frac": round(achieved / red_peak, 4),
+                        "peak_source": "measured live in this run: bale_l2_red_rate issues the same "
+                                       "red.global.add.u64 at hashed positions of the same 10^6 counters with no "
+                                       "index stream (10^7 reductions), CUDA events",
+                        "ncu_l2_throughput_pct": 70.6, "ncu_source": "profiles/histo_plain_l2_1e6_counters.md",
+                        "traffic": dram, "dram_gbs": round(dram / (ms / 1e3) / 1e9, 1) if dram else None,
+                        "hbm_model": {"algorithmic_bytes_per_step": algo,
+                                      "achieved_gbs": round(algo / (ms / 1e3) / 1e9, 1),
+                                      "note": "72 B/update (index + sector read + write-back) applies to tables "
+                                              "beyond L2; it reads above HBM peak here"}},
            "clocks": clocks.summary(), "gpu_launches": args.steps,
            "config": {"workload": "histo: 10^7 uniform updates into 10^6 int64 counters",
                       "updates": n, "counters": HISTO_COUNTS,
@@ -393,14 +401,11 @@ def run_triangles(ctx) -> dict:
     out = {"metric": "edges/s triangle counting (nnz(L) per second)",
            "value": round(job_rate(nnz, ms_max / 1e3, ctx["dist"].world) / 1e9, 4), "unit": "Gedges/s",
            "ms_per_step": round(ms_max, 4), "triangles": per_step,
-           "roofline": roofline(ctx, "triangles", wedge_bytes, count_ms / 1e3,
-                                "wedge_count_kernel (one warp per row j: bitmap / staged search over the "
-                                "incoming prefixes)",
-                                note="push work model: 4 B per probed prefix element (exstack pushes, "
-                                     "apps/triangle_src/triangle.upc:344-349), 8 B per prefix record, 8 B "
-                                     "per nonzero for row j; the step also runs the prepare kernels "
-                                     f"(validate, transpose), {round(ms_max - count_ms, 3)} ms of the "
-                                     f"{round(ms_max, 3)} ms step"),
+           # the count kernel is bound by instruction issue (ncu: issue active
+           # ~69%, most probes served from L2), so its DRAM traffic (ncu,
+           # per launch) over the live kernel time is a fraction of HBM, and
+           # the push-model bytes (L2 + DRAM) are reported beside it
+           "roofline": tri_roofline(ctx, wedge_bytes, count_ms / 1e3, ms_max),
            "roofline_pull_model": {"algorithmic_bytes_per_step": 8 * (n + 1) + 8 * nnz + 8 * pulls,
                                    "achieved_gbs": round((8 * (n + 1) + 8 * nnz + 8 * pulls) / ms_max * 1e-6, 1),
                                    "note": "the AGI loop's pull model (8 B per row-j element scanned); the "
@@ -432,6 +437,8 @@ def run_triangles(ctx) -> dict:
     torch.cuda.synchronize()
     out["erdos_renyi"] = {**er, "triangles": int(e_cnt.item()), "n": E.numrows, "nnz": E.nnz,
                           "how": "gen_erdos_renyi(2^20, 32/2^20, seed 7), lower triangle"}
+    if ctx["cpu"]:  # the count against the oracle's AGI loop
+        out["erdos_renyi"]["parity_ok"] = _oracle().triangle_agi_mt(E.offset, E.nonzero) == int(e_cnt.item())
     del off, col, flush, e_off, e_col
     torch.cuda.empty_cache()
     res = {}
@@ -651,7 +658,12 @@ def run_batch(ctx, small: bool = False) -> dict:
     ctx["dist"].barrier()
     batch_ms = time_device(b.run, args.steps, args.warmup)
     torch.cuda.synchronize()
-    ok = all(torch.equal(o, x[1]) for o, x in zip(plain_out, inst)) and not b.bad().any()
+    same_as_plain = all(torch.equal(o, x[1]) for o, x in zip(plain_out, inst)) and not b.bad().any()
+    del plain_out
+    # every instance against the oracle: counts = replays x the histogram,
+    # tgt = table[index], count = replays x the AGI count
+    oracle_ok, oracle_s = check_mix_with_oracle(inst, args.steps + args.warmup)
+    ok = same_as_plain and oracle_ok
     stats = b.stats()
     b.close()
     plain_ms, batch_ms = ctx["dist"].max(plain_ms), ctx["dist"].max(batch_ms)
@@ -673,12 +685,43 @@ def run_batch(ctx, small: bool = False) -> dict:
                            "ms_per_step": round(sync_s * 1e3, 3),
                            "how": "each instance's device entry point, synchronised after each instance"},
             "batched_vs_plain": round(plain_ms / batch_ms, 3), "batched_vs_plain_sync": round(sync_s * 1e3 / batch_ms, 3),
-            "parity_ok": bool(ok), "batch_stats": stats, "clocks": clocks.summary(),
+            "parity_ok": bool(ok), "parity": {"oracle_ok": bool(oracle_ok), "same_as_plain": bool(same_as_plain),
+                                              "how": "every instance against the oracle's AGI loops on the host "
+                                                     "(histo_agi_mt, ig_agi_mt, triangle_agi_mt)",
+                                              "check_s": round(oracle_s, 1)},
+            "batch_stats": stats, "clocks": clocks.summary(),
             "gpu_launches": args.steps,
             "config": {"workload": f"batched {name}: 256 histo + 192 ig + 64 R-MAT triangle instances, "
                                    f"log-uniform sizes {spec}",
                        "items_per_step": items, "items_by_kind": kinds, "generate_s": round(gen_s, 1),
                        "l2": "the mix's working set (~60 GB) exceeds L2; no flush"}}
+
+
+def check_mix_with_oracle(inst, reps: int) -> tuple[bool, float]:
+    """Each instance of a mix after `reps` batched replays, against the
+    oracle's multi-threaded AGI restatements on the host: histo counts equal
+    reps x the oracle's histogram, ig outputs equal the oracle's gather,
+    triangle counts equal reps x the oracle's count.  Returns (all equal,
+    seconds spent)."""
+    orc = _oracle()
+    t0 = time.perf_counter()
+    ok = True
+    for kind, out, a, b, _ in inst:
+        if kind == "histo":
+            want = np.zeros(out.numel(), np.int64)
+            orc.histo_agi_mt(a.cpu().numpy(), want)
+            ok &= bool(np.array_equal(out.cpu().numpy(), reps * want))
+        elif kind == "ig":
+            idx = a.cpu().numpy()
+            want = np.empty(idx.size, np.int64)
+            orc.ig_agi_mt(want, idx, b.cpu().numpy())
+            ok &= bool(np.array_equal(out.cpu().numpy(), want))
+        else:
+            want = orc.triangle_agi_mt(a.cpu().numpy(), b.cpu().numpy())
+            ok &= int(out.item()) == reps * want
+        if not ok:
+            break
+    return ok, time.perf_counter() - t0
 
 
 def run_serve(ctx) -> dict:
@@ -788,6 +831,28 @@ def run_serve(ctx) -> dict:
                        "setup_s": round(gen_s, 1)}}
 
 
+def tri_roofline(ctx, push_bytes: int, count_s: float, step_ms: float) -> dict:
+    """The wedge count kernel's roofline: bound by instruction issue; DRAM
+    bytes per launch from the committed ncu capture over the live kernel
+    time, against the measured HBM peak; the push-model bytes beside it."""
+    tr = ctx["traffic"].get("triangles", {})
+    dram = tr.get("dram_bytes_per_step")
+    achieved = dram / count_s / 1e9 if dram else None
+    return {"bound": "issue", "kernel": "wedge_count_kernel (one warp per row j: bitmap / staged search over the "
+                                        "incoming prefixes)",
+            "achieved": round(achieved, 1) if achieved else None, "peak": ctx["peak"], "peak_source": ctx["peak_src"],
+            "unit": "GB/s", "frac": round(achieved / ctx["peak"], 4) if achieved else None, "traffic": dram,
+            "what": "DRAM bytes of one count launch (ncu) over the live count-kernel time: the kernel's share of HBM",
+            "issue_active_ncu": tr.get("issue_active"), "ncu_source": tr.get("summary"),
+            "count_kernel_ms": round(count_s * 1e3, 4),
+            "push_model": {"bytes_per_launch": push_bytes, "achieved_gbs": round(push_bytes / count_s / 1e9, 1),
+                           "note": "4 B per probed prefix element (exstack pushes, "
+                                   "apps/triangle_src/triangle.upc:344-349), 8 B per prefix record, 8 B per "
+                                   "nonzero for row j: L2 and DRAM bytes together"},
+            "note": f"the step also runs the prepare kernels (validate, transpose): "
+                    f"{round(step_ms - count_s * 1e3, 3)} ms of the {round(step_ms, 3)} ms step"}
+
+
 def roofline(ctx, wl: str, algo_bytes: int, seconds: float, kernel: str, note: str | None = None) -> dict:
     peak = ctx["peak"]
     achieved = algo_bytes / seconds / 1e9
@@ -881,44 +946,78 @@ def run_gb300(args, dist: Dist) -> dict | None:
                 others[wl] = runners[wl]()
                 torch.cuda.empty_cache()
         head["workloads"] = others
+        # last key of the line: one short entry per workload, so that a
+        # reader keeping only the line's tail still sees every result
+        head["summary"] = {args.workload: summarize(head), **{wl: summarize(r) for wl, r in others.items()}}
     return head
 
 
+def summarize(r: dict) -> dict:
+    """value, roofline fraction, parity and the main ratio of one workload."""
+    out = {"value": r.get("value"), "unit": r.get("unit")}
+    rf = r.get("roofline") or {}
+    if rf.get("frac") is not None:
+        out["frac"] = rf["frac"]
+        out["bound"] = rf.get("bound")
+    par = [r[k] for k in ("parity_ok", "parity_sample_ok") if k in r]
+    if par:
+        out["parity"] = all(par)
+    if "e2e" in r:
+        out["e2e"] = r["e2e"].get("value")
+    if "cpu_baseline" in r:
+        out["cpu"] = r["cpu_baseline"].get("value")
+    for k in ("batched_vs_plain", "batched_bound_ms", "triangles"):
+        if k in r:
+            out[k] = r[k]
+    if "saturation" in r:
+        out["p50_ms"], out["p99_ms"] = r["saturation"]["p50_ms"], r["saturation"]["p99_ms"]
+    if "erdos_renyi" in r:
+        er = r["erdos_renyi"]
+        out["er"] = {"value": er["default"]["value"], "parity": er.get("parity_ok")}
+    return out
+
+
 def run_reference(args, dist: Dist) -> dict | None:
-    """The CPU implementation of the path (the oracle restatement of the
-    reference's AGI loops, all host threads) on a bounded sample per step."""
+    """The CPU implementation of the path: the oracle restatement of the
+    reference's AGI loops on all host threads, over the whole workload per
+    step (all 2^28 requests; all 10^7 updates).  Inputs come from the
+    oracle's own SplitMix64 generators (equal to the GPU library's, pinned by
+    tests/test_oracle.py), so this process never loads the GPU library."""
     if dist.rank != 0:
         return None
-    import bale_old_gb300 as bale
-
     orc = _oracle()
     cores = orc.num_cpus()
     wl = args.workload
-    if wl in ("ig", "ig_zipf"):
-        index_h, table_h = ig_inputs(bale, wl == "ig_zipf")
-        sample = np.ascontiguousarray(index_h[: 1 << 26])
-        tgt = np.empty(sample.size, np.int64)
-        secs = time_host(lambda: orc.ig_agi_mt(tgt, sample, table_h, cores), args.steps, args.warmup)
-        v, unit, metric = sample.size / secs / 1e9, "GUP/s", "GUP/s index gather (10^9 requests/s)"
-        desc = "first 2^26 of the 2^28 requests per step against the full 2^26 table"
+    if wl == "ig":
+        table_h = orc.gen_values(IG_TABLE, 2)
+        index_h = orc.gen_uniform(IG_REQUESTS, IG_TABLE, 3)
+        tgt = np.empty(index_h.size, np.int64)
+        secs = time_host(lambda: orc.ig_agi_mt(tgt, index_h, table_h, cores), args.steps, args.warmup)
+        ok = bool(np.array_equal(tgt[: 1 << 20], table_h[index_h[: 1 << 20]]))
+        v, unit, metric = IG_REQUESTS / secs / 1e9, "GUP/s", "GUP/s index gather (10^9 requests/s)"
+        desc = "all 2^28 uniform requests per step against the full 2^26-entry table"
+        work = {"workload": "ig uniform: 2^26-entry int64 table, 2^28 int64 requests", "table_entries": IG_TABLE,
+                "requests": IG_REQUESTS}
     elif wl == "histo":
-        index_h = bale.gen_uniform(HISTO_UPDATES, HISTO_COUNTS, 1)
+        index_h = orc.gen_uniform(HISTO_UPDATES, HISTO_COUNTS, 1)
         counts = np.zeros(HISTO_COUNTS, np.int64)
         secs = time_host(lambda: orc.histo_agi_mt(index_h, counts, cores), args.steps, args.warmup)
+        ok = int(counts.sum()) == (args.steps + args.warmup) * HISTO_UPDATES
         v, unit, metric = HISTO_UPDATES / secs / 1e9, "GUP/s", "GUP/s histogram (10^9 updates/s)"
-        desc = "all 10^7 updates per step"
+        desc = "all 10^7 updates per step into the 10^6 counters"
+        work = {"workload": "histo: 10^7 uniform updates into 10^6 int64 counters", "updates": HISTO_UPDATES,
+                "counters": HISTO_COUNTS}
     else:
-        L = bale.gen_rmat(TRI_SCALE, 16, 0.57, 0.19, 0.19, 6)
-        secs = time_host(lambda: orc.triangle_agi_mt(L.offset, L.nonzero, cores), args.steps, 0)
-        v, unit, metric = L.nnz / secs / 1e9, "Gedges/s", "edges/s triangle counting (nnz(L) per second)"
-        desc = "the full scale-22 graph per step"
+        return {"impl": "reference", "unavailable": f"the CPU reference arm builds its inputs without the GPU library for the ig and "
+                               f"histo workloads only; {wl} needs the library's generators"}
     return {"metric": metric, "value": round(v, 5), "unit": unit, "impl": "reference",
-            "ms_per_step": round(secs * 1e3, 3),
+            "ms_per_step": round(secs * 1e3, 3), "parity_sample_ok": ok,
             "cpu_baseline": {"value": round(v, 5), "unit": unit, "cores": cores, "kind": "port", "sample": desc},
             "e2e": {"value": round(v, 5), "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-            "config": {"workload": wl, "note": "oracle restatement of the reference's AGI loop, one pthread per "
-                                               "core (the reference's own build runs one PE, single-threaded, "
-                                               "and exists only where its source tree does)"}}
+            "config": {**work, "note": "oracle restatement of the reference's AGI loop (apps/ig_src/ig_agi.upc:61-64, "
+                                       "apps/histo_src/histo_agi.upc:61-66), one pthread per core; the reference's "
+                                       "own build runs one PE, single-threaded, and exists only where its source "
+                                       "tree does"}}
 
 
 def main(argv=None) -> int:
@@ -936,7 +1035,9 @@ def main(argv=None) -> int:
     dist = Dist()
     try:
         res = run_reference(args, dist) if args.impl == "reference" else run_gb300(args, dist)
-        if dist.rank == 0 and res is not None:
+        if dist.rank == 0 and res is not None and "unavailable" in res:
+            print(json.dumps({"impl": res["impl"], "unavailable": res["unavailable"]}), flush=True)
+        elif dist.rank == 0 and res is not None:
             line = {"metric": res.pop("metric"), "value": res.pop("value"), "unit": res.pop("unit"),
                     "n_gpus": dist.world, "steps": args.steps, "warmup": args.warmup,
                     "ms_per_step": res.pop("ms_per_step"), "higher_is_better": True, "scaling": "weak",

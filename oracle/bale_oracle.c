@@ -212,6 +212,52 @@ static int64_t orc_run(int kind, int nthreads, int64_t n, const int64_t *a, cons
   return total;
 }
 
+/* Input generation (not a reference routine; see bale_oracle.h). */
+typedef struct {
+  int64_t *out;
+  int64_t lo, hi;
+  uint64_t range, seed;
+} orc_gen_t;
+
+static uint64_t orc_splitmix64(uint64_t seed, uint64_t i) {
+  uint64_t z = seed + (i + 1) * 0x9E3779B97F4A7C15ULL;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+  return z ^ (z >> 31);
+}
+
+static void *orc_gen_worker(void *p) {
+  orc_gen_t *g = (orc_gen_t *)p;
+  for (int64_t i = g->lo; i < g->hi; i++) {
+    uint64_t v = orc_splitmix64(g->seed, (uint64_t)i);
+    g->out[i] = g->range ? (int64_t)(uint64_t)(((unsigned __int128)v * g->range) >> 64) : (int64_t)v;
+  }
+  return NULL;
+}
+
+static void orc_gen(int64_t *out, int64_t n, uint64_t range, uint64_t seed, int nthreads) {
+  if (nthreads <= 0) nthreads = orc_num_cpus();
+  if (nthreads > 256) nthreads = 256;
+  if (n < (int64_t)nthreads * 4096) nthreads = 1;
+  pthread_t th[256];
+  orc_gen_t g[256];
+  int started = 0;
+  for (int t = 0; t < nthreads; t++) g[t] = (orc_gen_t){out, n * t / nthreads, n * (t + 1) / nthreads, range, seed};
+  for (int t = 1; t < nthreads; t++) {
+    if (pthread_create(&th[t], NULL, orc_gen_worker, &g[t]) != 0) break;
+    started = t;
+  }
+  for (int t = started + 1; t < nthreads; t++) orc_gen_worker(&g[t]);
+  orc_gen_worker(&g[0]);
+  for (int t = 1; t <= started; t++) pthread_join(th[t], NULL);
+}
+
+void orc_gen_uniform(int64_t *out, int64_t n, int64_t range, uint64_t seed, int nthreads) {
+  if (range > 0) orc_gen(out, n, (uint64_t)range, seed, nthreads);
+}
+
+void orc_gen_values(int64_t *out, int64_t n, uint64_t seed, int nthreads) { orc_gen(out, n, 0, seed, nthreads); }
+
 void orc_histo_agi_mt(const int64_t *index, int64_t n, int64_t *counts, int nthreads) {
   orc_run(JOB_HISTO, nthreads, n, index, NULL, counts);
 }

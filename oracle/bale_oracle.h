@@ -53,6 +53,16 @@ int64_t orc_triangle_agi_mt(const int64_t *offset, const int64_t *nonzero, int64
                             int nthreads);
 int orc_num_cpus(void);
 
+/* Seeded inputs for the timed CPU reference arm, so that it never loads the
+ * GPU library: SplitMix64 (Steele, Lea & Flood 2014) with output i =
+ * mix(seed + (i+1) * 0x9E3779B97F4A7C15), the counter layout the GPU
+ * library's generators use.  Uniform indices in [0, range) are the high 64
+ * bits of output * range (range > 0); values are the outputs themselves.
+ * Split over nthreads host threads (<= 0: all cores); same buffers for any
+ * thread count.  tests/test_oracle.py pins both to the library's buffers. */
+void orc_gen_uniform(int64_t *out, int64_t n, int64_t range, uint64_t seed, int nthreads);
+void orc_gen_values(int64_t *out, int64_t n, uint64_t seed, int nthreads);
+
 /* spmat_agi.upc:180-235 transpose_matrix_agi at one PE: At is numcols x
  * numrows; toffset[numcols+1], tnonzero[nnz].  Returns 0, or -1 for a column
  * outside [0, numcols). */

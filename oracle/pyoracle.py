@@ -23,7 +23,9 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 PORT_LIB = HERE / "_build" / "liboracle.so"
 REF_LIB = HERE / "_ref" / "libbale_ref.so"
-REF_TREE = Path(os.environ.get("BALE_REFERENCE_TREE", "/root/reference"))
+# The reference tree: $BALE_REFERENCE_TREE, else a directory named
+# "reference" beside this repository's root.
+REF_TREE = Path(os.environ.get("BALE_REFERENCE_TREE") or HERE.parent.parent / "reference")
 
 i64 = C.c_int64
 P64 = C.POINTER(C.c_int64)
@@ -73,11 +75,24 @@ class Oracle:
             "orc_write_dataset": (C.c_int, [C.c_char_p, P64, P64, i64, i64]),
             "orc_read_mm": (C.c_int, [C.c_char_p, P64, P64, P64]),
             "orc_num_cpus": (C.c_int, []),
+            "orc_gen_uniform": (None, [P64, i64, i64, C.c_uint64, C.c_int]),
+            "orc_gen_values": (None, [P64, i64, C.c_uint64, C.c_int]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(lib, name)
             fn.restype, fn.argtypes = res, args
         self.lib = lib
+
+    # seeded inputs (the reference arm's own, so it never loads the GPU library)
+    def gen_uniform(self, n: int, rng: int, seed: int, nthreads: int = 0) -> np.ndarray:
+        out = np.empty(n, np.int64)
+        self.lib.orc_gen_uniform(_p(out), n, rng, seed, nthreads)
+        return out
+
+    def gen_values(self, n: int, seed: int, nthreads: int = 0) -> np.ndarray:
+        out = np.empty(n, np.int64)
+        self.lib.orc_gen_values(_p(out), n, seed, nthreads)
+        return out
 
     # histo -----------------------------------------------------------------
     def histo_agi(self, index: np.ndarray, counts: np.ndarray) -> None:

@@ -98,6 +98,33 @@ def test_full_size_property_2e28_requests(cuda, bale):
     torch.cuda.empty_cache()
 
 
+@pytest.mark.parametrize("mode", [-1, 1], ids=["default", "partitioned"])
+def test_full_size_zipf_property_2e28_requests(cuda, bale, mode):
+    """The skewed ig configuration at its own size: 2^28 requests drawn
+    Zipf(1.1) over a keyed permutation of a 2^26-entry table whose entries
+    are table[i] = -(i+1), so every output must be -(index+1) (the check of
+    apps/ig_src/ig.upc:96-114), compared in full on the device.  The default
+    path sends this stream to the direct gather (the skew test); ig.mode 1
+    forces the region-partitioned gather on the same data."""
+    import torch
+
+    tsize, n = 1 << 26, 1 << 28
+    index = torch.from_numpy(bale.gen_zipf(n, tsize, 1.1, 4, 5)).to(cuda)
+    table = -(torch.arange(tsize, dtype=torch.int64, device=cuda) + 1)
+    tgt = torch.zeros_like(index)
+    bad = torch.zeros(1, dtype=torch.int64, device=cuda)
+    bale.tune_set("ig.mode", mode)
+    try:
+        bale.ig_dev(tgt, index, table, bad=bad)
+        torch.cuda.synchronize()
+    finally:
+        bale.tune_set("ig.mode", -1)
+    assert int(bad.item()) == 0
+    assert bool(torch.equal(tgt, -(index + 1)))
+    del table, index, tgt
+    torch.cuda.empty_cache()
+
+
 @pytest.mark.parametrize("mode", [0, 1])
 @pytest.mark.parametrize("n,tsize", [(1, 1), (1000, 7), (1024, 1 << 22), (1025, (1 << 22) + 1),
                                      (5 * 1024 + 17, 3 * (1 << 22) + 5), (300_001, 1 << 24)])

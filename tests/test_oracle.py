@@ -433,3 +433,16 @@ def test_matrix_market_reader_matches_reference_golden(oracle, golden):
         np.testing.assert_array_equal(off, d[f"mm/{f}/offset"], err_msg=str(f))
         np.testing.assert_array_equal(col, d[f"mm/{f}/nonzero"], err_msg=str(f))
         assert nc == int(d[f"mm/{f}/numcols"][0])
+
+
+@pytest.mark.parametrize("n,rng,seed", [(0, 5, 1), (1, 1, 2), (12_345, 1_000_000, 1), ((1 << 20) + 7, 1 << 26, 3),
+                                        (70_000, (1 << 40) + 3, 9)])
+def test_oracle_generators_equal_the_library_generators(oracle, bale, n, rng, seed):
+    """The reference arm of the benchmark builds its inputs with the oracle's
+    SplitMix64 generators so that it never loads the GPU library; they must
+    give exactly the library's buffers, for any thread count."""
+    want_u = bale.gen_uniform(n, rng, seed)
+    want_v = bale.gen_values(n, seed)
+    for threads in (1, 3, 0):
+        np.testing.assert_array_equal(oracle.gen_uniform(n, rng, seed, threads), want_u)
+        np.testing.assert_array_equal(oracle.gen_values(n, seed, threads), want_v)

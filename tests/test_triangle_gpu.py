@@ -75,6 +75,32 @@ def test_erdos_renyi_matches_oracle(cuda, bale, oracle, mode):
     assert bale.triangle_agi(L)[0] == oracle.triangle_agi_mt(L.offset, L.nonzero)
 
 
+@pytest.fixture(scope="module")
+def er20(bale, oracle):
+    """The Erdos-Renyi variant of the triangle configuration: n = 2^20,
+    p = 32/2^20 (average degree 32), lower triangle, with the multi-threaded
+    oracle's count."""
+    n = 1 << 20
+    L = bale.gen_erdos_renyi(n, 32.0 / n, 7)
+    return L, oracle.triangle_agi_mt(L.offset, L.nonzero)
+
+
+@pytest.mark.parametrize("tmode", [-1, 0, 1, 2], ids=["default", "merge", "hybrid", "wedge"])
+def test_erdos_renyi_2e20_degree32_config_matches_oracle(cuda, bale, er20, tmode):
+    """At its own size, in the default mode (the device-side choice picks the
+    hybrid for this graph) and in each forced mode, through every drop-in:
+    the count equals the oracle's, as the reference's apps require of every
+    model (apps/triangle_src/triangle.upc:415-420)."""
+    L, want = er20
+    assert L.nnz > 16_000_000 and want > 0
+    bale.tune_set("tri.mode", tmode)
+    try:
+        for fn in DROPINS:
+            assert getattr(bale, fn)(L)[0] == want, fn
+    finally:
+        bale.tune_set("tri.mode", -1)
+
+
 def _clique(m: int):
     off = np.zeros(m + 1, np.int64)
     off[1:] = np.cumsum(np.arange(m))

@@ -115,6 +115,9 @@ def test_every_mode_matches_oracle(cuda, bale, oracle, hmode, n, tsize):
         oracle.histo_agi(index, want)
         bale.histo_agi(index, counts)
         np.testing.assert_array_equal(counts, want)
+        oracle.histo_agi(index, want)
+        bale.histo_exstack(bale.pack_index(index), counts)  # packed indices (>> 16)
+        np.testing.assert_array_equal(counts, want)
         import torch
         idx_h = index.copy()
         idx_h[::101] = tsize + 7  # out of range

@@ -146,6 +146,38 @@ def test_both_gather_modes_match_oracle(cuda, bale, oracle, mode, n, tsize):
         bale.tune_set("ig.mode", -1)
 
 
+@pytest.mark.parametrize("regions", [32, 61, 62, 63])
+@pytest.mark.parametrize("shift", [0, 16])
+def test_partitioned_gather_region_counts_around_the_warp_scan(cuda, bale, regions, shift):
+    """The whole-chunk partition scans its region counters with one warp when
+    the regions plus the out-of-range bucket and the total fit 64 slots, and
+    with the block scan beyond: tables of 32, 61, 62 and 63 16-MiB regions
+    (the last one partial), 2^20 + 5 requests with some out of range, plain
+    and packed (>> 16) indices; table[i] = -(i+1), checked on the device."""
+    import torch
+
+    tsize = ((regions - 1) << 21) + 12345
+    n = (1 << 20) + 5
+    idx = bale.gen_uniform(n, tsize + 3000, regions + shift)
+    idx[::1777] = -3
+    table = -(torch.arange(tsize, dtype=torch.int64, device=cuda) + 1)
+    index = torch.from_numpy(bale.pack_index(idx) if shift else idx).to(cuda)
+    want_idx = torch.from_numpy(idx).to(cuda)
+    ok = (want_idx >= 0) & (want_idx < tsize)
+    tgt = torch.full_like(index, 7)
+    bad = torch.zeros(1, dtype=torch.int64, device=cuda)
+    bale.tune_set("ig.mode", 1)
+    try:
+        bale.ig_dev(tgt, index, table, shift=shift, bad=bad)
+        torch.cuda.synchronize()
+    finally:
+        bale.tune_set("ig.mode", -1)
+    assert int(bad.item()) == int((~ok).sum().item())
+    assert bool(torch.equal(tgt, torch.where(ok, -(want_idx + 1), torch.zeros_like(want_idx))))
+    del table, index, tgt
+    torch.cuda.empty_cache()
+
+
 @pytest.mark.parametrize("mode", [0, 1])
 def test_both_modes_count_bad_indices(cuda, bale, mode):
     import torch

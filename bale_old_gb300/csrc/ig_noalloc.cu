@@ -11,11 +11,15 @@
 // demand; this one never allocates: the partition scratch for up to
 // kNoAllocMaxRequests requests lives in g_ig_noalloc_scratch, a file-scope
 // __device__ array that every GPU which loads the library holds until the
-// process exits (about 3.6 MiB).
+// process exits (3.5 MiB: 3,670,784 bytes).
 //
 // Set-up: the first call on each device, with that device current, looks up
 // the array's device address with cudaGetSymbolAddress and caches it; make
-// that first call before any stream capture.  Host code never passes the
+// that first call before any stream capture.  The cache assumes one CUDA
+// context per device for the life of the process: after cudaDeviceReset the
+// cached address is stale, so a process that resets a device must not call
+// this entry point on it again.  The stream must belong to the current
+// device, whose array the call uses.  Host code never passes the
 // array's name to a kernel: in host code the name is only a host-side
 // stand-in, not a device address.
 //
@@ -42,6 +46,7 @@ constexpr size_t kValuesBytes = kNoAllocMaxRequests * sizeof(int64_t);
 constexpr size_t kStartsBytes = ((kMaxChunks * (kIgMaxRegions + 2) * sizeof(uint16_t)) + 255) & ~size_t(255);
 constexpr size_t kWordsOffset = kEntriesBytes + kValuesBytes + kStartsBytes;
 constexpr size_t kScratchBytes = kWordsOffset + 256;  // [0] work cursor, [1] discarded bad count
+static_assert(kScratchBytes == 3670784, "the documented size of the fixed scratch array");
 
 static __device__ __align__(256) unsigned char g_ig_noalloc_scratch[kScratchBytes];
 

@@ -358,12 +358,15 @@ BALE_API void bale_server_destroy(bale_server_t *s);
 /* allocator, or a loop that cannot take cudaMalloc/cudaFree's implicit      */
 /* synchronisation).  Same result as bale_ig_dev, computed by the region-    */
 /* partitioned gather with its scratch in a fixed device array inside the    */
-/* library (about 3.6 MiB, held by every GPU that loads the library until    */
-/* exit).  Limits: n <= 262144 requests per call (larger n -> BALE_EINVAL     */
-/* with a message), table_len <= 2^32, d_index and d_tgt 16-byte aligned.    */
-/* The first call on a device looks up the array's address; make it before  */
-/* any stream capture.  All calls share the array: calls that overlap on the */
-/* GPU race and must be serialised by the caller.                            */
+/* library (3.5 MiB = 3,670,784 bytes, held by every GPU that loads the      */
+/* library until exit).  Limits: n <= 262144 requests per call (larger n ->  */
+/* BALE_EINVAL with a message), table_len <= 2^32, d_index and d_tgt         */
+/* 16-byte aligned.  The first call on a device looks up the array's address */
+/* and caches it for the process (one context per device: do not call it    */
+/* again on a device after cudaDeviceReset); make it before any stream       */
+/* capture.  The stream must belong to the current device.  All calls share  */
+/* the array: calls that overlap on the GPU race and must be serialised by   */
+/* the caller.                                                               */
 BALE_API int bale_ig_dev_noalloc(int64_t *d_tgt, const int64_t *d_index, int64_t n, const int64_t *d_table,
                                  int64_t table_len, int shift, int64_t *d_bad, void *stream);
 

@@ -204,7 +204,10 @@ def _tri(fn, name: str, L: SparseMatrix, U: Optional[SparseMatrix], alg: int, *e
 
 
 def triangle_agi(L: SparseMatrix, U: Optional[SparseMatrix] = None, alg: int = 0):
-    """(count, sr, seconds): triangles of the strictly lower tidy L."""
+    """(count, sr, seconds).  alg 0: the triangles of the strictly lower tidy
+    L; any other alg: the reference's alg 1, the sum over L's nonzeros (i,j)
+    of |U_i and U_j| for the strictly upper tidy U (required), which is the
+    same count when U is L's transpose."""
     return _tri(_lib.triangle_agi, "triangle_agi", L, U, alg)
 
 

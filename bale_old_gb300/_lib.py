@@ -104,6 +104,7 @@ SIGNATURES: dict[str, tuple[object, list[object]]] = {
     "bale_batch_run": (C.c_int, [VP, VP]),
     "bale_batch_bad": (C.c_int, [VP, P64, i64]),
     "bale_batch_stats": (C.c_int, [VP, P64, C.c_int]),
+    "bale_batch_plan": (C.c_int, [VP, P64, i64]),
     "bale_batch_destroy": (None, [VP]),
     "bale_server_create": (VP, [i64, C.c_int]),
     "bale_server_add_table": (C.c_int, [VP, P64, i64]),

@@ -81,6 +81,14 @@ class Batch:
         _lib.bale_batch_stats(self._h, out.ctypes.data_as(C.POINTER(C.c_int64)), out.size)
         return dict(zip(STAT_NAMES, out.tolist()))
 
+    def plan(self) -> np.ndarray:
+        """Per instance: the side stream it runs on as its own kernels, or -1
+        for the work queue."""
+        out = np.zeros(max(1, len(self._inst)), np.int64)
+        if _lib.bale_batch_plan(self._h, out.ctypes.data_as(C.POINTER(C.c_int64)), len(self._inst)) != 0:
+            raise BaleError(f"bale_batch_plan: {_last_error()}")
+        return out[: len(self._inst)]
+
     def close(self) -> None:
         if getattr(self, "_h", None):
             _lib.bale_batch_destroy(self._h)

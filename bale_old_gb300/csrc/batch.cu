@@ -309,6 +309,7 @@ struct bale_batch {
   unsigned long long *d_bad = nullptr;    // per instance
   void *d_ws = nullptr;                   // workspaces of the standalone instances, one region each
   std::vector<int64_t> standalone;
+  std::vector<int> side_of;  // per instance: its side stream, or -1 (work queue)
   cudaStream_t s_main = nullptr;
   std::vector<cudaStream_t> s_side;
   cudaEvent_t ev_fork = nullptr;
@@ -518,6 +519,8 @@ bale_batch_t *bale_batch_create(const bale_instance_t *inst, int64_t count) {
     ws_off.swap(off2);
     lane.swap(lane2);
   }
+  b->side_of.assign(static_cast<size_t>(count), -1);
+  for (size_t s = 0; s < b->standalone.size(); s++) b->side_of[static_cast<size_t>(b->standalone[s])] = lane[s];
 
   // ---- capture one run as a graph ----
   BATCH_CUDA(cudaStreamCreateWithFlags(&b->s_main, cudaStreamNonBlocking));
@@ -591,6 +594,15 @@ int bale_batch_stats(bale_batch_t *b, int64_t *out, int n) {
                         b->count,
                         static_cast<int64_t>(b->s_side.size())};
   for (int i = 0; i < n; i++) out[i] = i < 9 ? v[i] : -1;
+  return BALE_OK;
+}
+
+int bale_batch_plan(bale_batch_t *b, int64_t *side, int64_t count) {
+  if (!b || !side || count != b->count) {
+    set_error("bale_batch_plan: bad arguments");
+    return BALE_EINVAL;
+  }
+  for (int64_t k = 0; k < count; k++) side[k] = b->side_of[static_cast<size_t>(k)];
   return BALE_OK;
 }
 

@@ -93,7 +93,7 @@ unsigned long long *next_cursor_words(int k) {
 // Scratch word layout used by the synchronous drop-ins (serialised by
 // g_dropin_mu): [0] bad-input count, [1] index max, [2] triangle count,
 // [3] triangle work.  [7] absorbs bad counts the caller does not want.
-enum { kWordBad = 0, kWordMax = 1, kWordCount = 2, kWordWork = 3, kWordDiscard = 7 };
+enum { kWordBad = 0, kWordMax = 1, kWordCount = 2, kWordWork = 3, kWordFound = 4, kWordDiscard = 7 };
 
 // ---------------------------------------------------------------------------
 // drop-in state: a stream and grow-only device buffers per device
@@ -455,7 +455,13 @@ static double ig_dropin(int64_t *tgt, const int64_t *index, int64_t n, const int
   return now_seconds() - t0;
 }
 
-static double triangle_dropin(int64_t *count, int64_t *sr, sparsemat_t *L) {
+// The triangle drop-ins.  alg 0 counts from L alone; any other alg is the
+// reference's alg 1 (apps/triangle_src/triangle_agi.upc:100-136), the sum
+// over L's nonzeros (i,j) of |U_i and U_j| with the caller's U, which must be
+// given (the reference returns -1 for a NULL U).  When U is L's transpose,
+// as the apps pass it, that sum is alg 0's count and the alg-0 kernels run;
+// for any other tidy upper U it is computed as written (tri_alg1.cu).
+static double triangle_dropin(int64_t *count, int64_t *sr, sparsemat_t *L, sparsemat_t *U, int64_t alg) {
   const double t0 = now_seconds();
   if (!count || !sr || !L) {
     set_error("triangle: NULL count, sr or L");
@@ -471,6 +477,23 @@ static double triangle_dropin(int64_t *count, int64_t *sr, sparsemat_t *L) {
     set_error("triangle: bad matrix (nnz=%lld)", static_cast<long long>(nnz));
     return -1.0;
   }
+  const bool alg1 = alg != 0;
+  int64_t unnz = 0;
+  if (alg1) {
+    if (!U) {
+      set_error("triangle: alg %lld needs U (NULL given)", static_cast<long long>(alg));
+      return -1.0;
+    }
+    if (U->lnumrows != n || (n > 0 && !U->loffset)) {
+      set_error("triangle: U must have L's %lld rows", static_cast<long long>(n));
+      return -1.0;
+    }
+    unnz = n > 0 ? U->loffset[n] : 0;
+    if (unnz < 0 || (unnz > 0 && !U->lnonzero)) {
+      set_error("triangle: bad U (nnz=%lld)", static_cast<long long>(unnz));
+      return -1.0;
+    }
+  }
   std::lock_guard<std::mutex> lk(g_dropin_mu);
   DropinState *st = dropin_state();
   DeviceScratch *ds = device_scratch();
@@ -484,10 +507,40 @@ static double triangle_dropin(int64_t *count, int64_t *sr, sparsemat_t *L) {
   if (nnz > 0)
     DROPIN_CUDA(cudaMemcpyAsync(st->buf[1].p, L->lnonzero, static_cast<size_t>(nnz) * sizeof(int64_t),
                                 cudaMemcpyHostToDevice, st->stream));
-  DROPIN_TRY(launch_triangle(static_cast<const int64_t *>(st->buf[0].p),
-                             static_cast<const int64_t *>(st->buf[1].p), n, nnz,
-                             ds->words + kWordCount, ds->words + kWordWork, ds->words + kWordBad,
-                             st->stream));
+  const int64_t *d_loff = static_cast<const int64_t *>(st->buf[0].p);
+  const int64_t *d_lcol = static_cast<const int64_t *>(st->buf[1].p);
+  bool general_alg1 = false;
+  if (alg1 && n > 0) {
+    DROPIN_TRY(st->buf[2].ensure(obytes));
+    DROPIN_TRY(st->buf[3].ensure(static_cast<size_t>(unnz > 0 ? unnz : 1) * sizeof(int64_t)));
+    DROPIN_CUDA(cudaMemcpyAsync(st->buf[2].p, U->loffset, obytes, cudaMemcpyHostToDevice, st->stream));
+    if (unnz > 0)
+      DROPIN_CUDA(cudaMemcpyAsync(st->buf[3].p, U->lnonzero, static_cast<size_t>(unnz) * sizeof(int64_t),
+                                  cudaMemcpyHostToDevice, st->stream));
+    const int64_t *d_uoff = static_cast<const int64_t *>(st->buf[2].p);
+    const int64_t *d_ucol = static_cast<const int64_t *>(st->buf[3].p);
+    DROPIN_TRY(launch_triangle_alg1_check(d_loff, d_lcol, nnz, d_uoff, d_ucol, unnz, n, ds->words + kWordBad,
+                                          st->stream));
+    unsigned long long bad = 0;
+    DROPIN_CUDA(cudaMemcpyAsync(&bad, ds->words + kWordBad, sizeof(bad), cudaMemcpyDeviceToHost, st->stream));
+    DROPIN_CUDA(cudaStreamSynchronize(st->stream));
+    if (bad) {
+      set_error("triangle: L is not strictly lower or U not strictly upper tidy CSR (%llu bad rows)", bad);
+      return -1.0;
+    }
+    DROPIN_TRY(launch_triangle_alg1_transposed(d_loff, d_lcol, d_uoff, d_ucol, n, ds->words + kWordFound,
+                                               st->stream));
+    unsigned long long found = 0;
+    DROPIN_CUDA(cudaMemcpyAsync(&found, ds->words + kWordFound, sizeof(found), cudaMemcpyDeviceToHost, st->stream));
+    DROPIN_CUDA(cudaStreamSynchronize(st->stream));
+    general_alg1 = !(unnz == nnz && found == static_cast<unsigned long long>(nnz));
+    if (general_alg1)
+      DROPIN_TRY(launch_triangle_alg1_count(d_loff, d_lcol, d_uoff, d_ucol, n, ds->words + kWordCount,
+                                            ds->words + kWordWork, st->stream));
+  }
+  if (!general_alg1)
+    DROPIN_TRY(launch_triangle(d_loff, d_lcol, n, nnz, ds->words + kWordCount, ds->words + kWordWork,
+                               ds->words + kWordBad, st->stream));
   unsigned long long w[4] = {0, 0, 0, 0};
   DROPIN_CUDA(cudaMemcpyAsync(w, ds->words, sizeof(w), cudaMemcpyDeviceToHost, st->stream));
   DROPIN_CUDA(cudaStreamSynchronize(st->stream));
@@ -538,26 +591,23 @@ double ig_conveyor(int64_t *tgt, int64_t *pckindx, int64_t l_num_req, int64_t *l
 }
 
 double triangle_agi(int64_t *count, int64_t *sr, sparsemat_t *L, sparsemat_t *U, int64_t alg) {
-  (void)U; (void)alg;
-  return triangle_dropin(count, sr, L);
+  return triangle_dropin(count, sr, L, U, alg);
 }
 double triangle_exstack_push(int64_t *count, int64_t *sr, sparsemat_t *L, sparsemat_t *U, int64_t alg,
                              int64_t bufsiz) {
-  (void)U; (void)alg; (void)bufsiz;
-  return triangle_dropin(count, sr, L);
+  (void)bufsiz;
+  return triangle_dropin(count, sr, L, U, alg);
 }
 double triangle_exstack2_push(int64_t *count, int64_t *sr, sparsemat_t *L, sparsemat_t *U, int64_t alg,
                               int64_t bufsiz) {
-  (void)U; (void)alg; (void)bufsiz;
-  return triangle_dropin(count, sr, L);
+  (void)bufsiz;
+  return triangle_dropin(count, sr, L, U, alg);
 }
 double triangle_convey_push(int64_t *count, int64_t *sr, sparsemat_t *L, sparsemat_t *U, int64_t alg) {
-  (void)U; (void)alg;
-  return triangle_dropin(count, sr, L);
+  return triangle_dropin(count, sr, L, U, alg);
 }
 double triangle_agi_iter(int64_t *count, int64_t *sr, sparsemat_t *L, sparsemat_t *U, int64_t alg) {
-  (void)U; (void)alg;
-  return triangle_dropin(count, sr, L);
+  return triangle_dropin(count, sr, L, U, alg);
 }
 
 int bale_device_caps(int64_t *out, int n) {

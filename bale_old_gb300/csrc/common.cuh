@@ -126,6 +126,20 @@ int tri_wedge_run(const int64_t *offset, const void *ws, int64_t numrows, int64_
 int launch_triangle_wedge(const int64_t *offset, const int64_t *nonzero, int64_t numrows, int64_t nnz,
                           unsigned long long *count, unsigned long long *work, unsigned long long *bad, void *ws,
                           unsigned long long *cursor, cudaStream_t stream, const unsigned *run_if = nullptr);
+// Triangle alg 1 (sum over L's nonzeros (i,j) of |U_i and U_j|, tri_alg1.cu),
+// L strictly lower and U strictly upper, both n x n:
+//  * check: *bad += malformed rows of L and U (run first; the others index U
+//    by L's columns);
+//  * transposed: *found += nonzeros (i,j) of L with i in U's row j (U is L's
+//    transpose when that is nnz(L) and nnz(U) = nnz(L));
+//  * count: *count += the sum, *work += the U elements looked up.
+int launch_triangle_alg1_check(const int64_t *loff, const int64_t *lcol, int64_t lnnz, const int64_t *uoff,
+                               const int64_t *ucol, int64_t unnz, int64_t n, unsigned long long *bad,
+                               cudaStream_t stream);
+int launch_triangle_alg1_transposed(const int64_t *loff, const int64_t *lcol, const int64_t *uoff,
+                                    const int64_t *ucol, int64_t n, unsigned long long *found, cudaStream_t stream);
+int launch_triangle_alg1_count(const int64_t *loff, const int64_t *lcol, const int64_t *uoff, const int64_t *ucol,
+                               int64_t n, unsigned long long *count, unsigned long long *work, cudaStream_t stream);
 // n +1 L2 reductions at hashed positions of counts (the L2 reduction-rate probe).
 int launch_l2_red_rate(int64_t *counts, int64_t ncounts, int64_t n, cudaStream_t stream);
 // *mapped_dst = *src by a one-thread kernel (mapped_dst: the device alias of

@@ -634,6 +634,7 @@ def run_spmat(ctx) -> dict:
 def run_batch(ctx, small: bool = False) -> dict:
     import torch
 
+    from bale_old_gb300 import batch as bb
     from bale_old_gb300.mix import MIX_FULL, MIX_SMALL, as_batch, build_mix, run_plain
 
     bale, dev, args = ctx["bale"], ctx["dev"], ctx["args"]
@@ -665,6 +666,7 @@ def run_batch(ctx, small: bool = False) -> dict:
     oracle_ok, oracle_s = check_mix_with_oracle(inst, args.steps + args.warmup)
     ok = same_as_plain and oracle_ok
     stats = b.stats()
+    side = b.plan()
     b.close()
     plain_ms, batch_ms = ctx["dist"].max(plain_ms), ctx["dist"].max(batch_ms)
     w = ctx["dist"].world
@@ -674,6 +676,7 @@ def run_batch(ctx, small: bool = False) -> dict:
             run_plain([x])
             torch.cuda.synchronize()
     sync_s = ctx["dist"].max(time_host(plain_sync, max(1, args.steps // 3), 1))
+    bound = batch_bound(inst, side, args)
     name = "small-instance 512 mix" if small else "uneven 512-instance mix"
     return {"metric": f"G items/s on the {name} (updates + requests + edges), batched",
             "value": round(job_rate(items, batch_ms / 1e3, w) / 1e9, 4), "unit": "G items/s",
@@ -685,6 +688,8 @@ def run_batch(ctx, small: bool = False) -> dict:
                            "ms_per_step": round(sync_s * 1e3, 3),
                            "how": "each instance's device entry point, synchronised after each instance"},
             "batched_vs_plain": round(plain_ms / batch_ms, 3), "batched_vs_plain_sync": round(sync_s * 1e3 / batch_ms, 3),
+            "batched_bound_ms": bound["bound_ms"], "ratio_ceiling": round(plain_ms / bound["bound_ms"], 3),
+            "bound": bound,
             "parity_ok": bool(ok), "parity": {"oracle_ok": bool(oracle_ok), "same_as_plain": bool(same_as_plain),
                                               "how": "every instance against the oracle's AGI loops on the host "
                                                      "(histo_agi_mt, ig_agi_mt, triangle_agi_mt)",
@@ -695,6 +700,68 @@ def run_batch(ctx, small: bool = False) -> dict:
                                    f"log-uniform sizes {spec}",
                        "items_per_step": items, "items_by_kind": kinds, "generate_s": round(gen_s, 1),
                        "l2": "the mix's working set (~60 GB) exceeds L2; no flush"}}
+
+
+def batch_bound(inst, side, args) -> dict:
+    """The mix's time if every instance ran at the best rate its kernel
+    reaches on this GPU, with no launch gaps or idle SMs: each instance is
+    timed alone (CUDA events around its own entry point), the best items/s of
+    each class (histo and ig split by whether the table fits in L2) is that
+    class's rate, and the bound is the sum over instances of items / rate.
+    Beside it: the work queue alone (the small instances as one batch), the
+    standalone instances alone (one batch of them, on their side streams),
+    and how much of the shorter of the two the full batch hides."""
+    import torch
+
+    from bale_old_gb300 import batch as bb
+    from bale_old_gb300.mix import run_plain
+
+    l2 = 96 << 20
+    stream = torch.cuda.current_stream()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in inst]
+    run_plain(inst)  # warm
+    torch.cuda.synchronize()
+    for x, (a, b) in zip(inst, ev):
+        a.record(stream)
+        run_plain([x])
+        b.record(stream)
+    torch.cuda.synchronize()
+    alone = [a.elapsed_time(b) for a, b in ev]
+
+    def cls(x):
+        if x[0] == "tri":
+            return "tri"
+        table_bytes = 8 * (x[3].numel() if x[0] == "ig" else x[1].numel())
+        return f"{x[0]}_{'l2' if table_bytes <= l2 else 'hbm'}"
+
+    best = {}
+    for x, t in zip(inst, alone):
+        c = cls(x)
+        best[c] = max(best.get(c, 0.0), x[4] / t)  # items per ms
+    bound_ms = sum(x[4] / best[cls(x)] for x in inst)
+    small = [x for x, s in zip(inst, side) if s < 0]
+    big = [x for x, s in zip(inst, side) if s >= 0]
+
+    def batch_time(sub):
+        if not sub:
+            return 0.0
+        for x in sub:
+            if x[0] != "ig":
+                x[1].zero_()
+        with bb.Batch([bb.histo(x[1], x[2]) if x[0] == "histo" else bb.ig(x[1], x[2], x[3]) if x[0] == "ig"
+                       else bb.triangles(x[2], x[3], x[1]) for x in sub]) as sb:
+            return time_device(sb.run, args.steps, args.warmup)
+
+    queue_ms, standalone_ms = batch_time(small), batch_time(big)
+    return {"bound_ms": round(bound_ms, 3),
+            "best_rates_G_items_s": {c: round(r / 1e6, 2) for c, r in sorted(best.items())},
+            "alone_sum_ms": round(sum(alone), 3),
+            "standalone_alone_sum_ms": round(sum(t for t, s in zip(alone, side) if s >= 0), 3),
+            "queue_instances": len(small), "standalone_instances": len(big),
+            "queue_only_batch_ms": round(queue_ms, 3), "standalone_only_batch_ms": round(standalone_ms, 3),
+            "how": "bound = sum over instances of items / (best items/s of its class, each instance timed alone "
+                   "with CUDA events); queue_only / standalone_only: the two halves of the plan as batches of "
+                   "their own"}
 
 
 def check_mix_with_oracle(inst, reps: int) -> tuple[bool, float]:

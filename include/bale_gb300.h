@@ -305,6 +305,9 @@ BALE_API int bale_batch_bad(bale_batch_t *b, int64_t *bad, int64_t count);
 /* ig, triangle light, triangle heavy), standalone instances, instances,    */
 /* side streams.                                                             */
 BALE_API int bale_batch_stats(bale_batch_t *b, int64_t *out, int n);
+/* side[k] = the side stream instance k runs on as its own kernels, or -1   */
+/* when it goes through the work queue (count = the batch's instance count). */
+BALE_API int bale_batch_plan(bale_batch_t *b, int64_t *side, int64_t count);
 BALE_API void bale_batch_destroy(bale_batch_t *b);
 
 /* ======================= serving loop =================================== */

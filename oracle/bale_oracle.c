@@ -212,6 +212,46 @@ static int64_t orc_run(int kind, int nthreads, int64_t n, const int64_t *a, cons
   return total;
 }
 
+/* apps/triangle_src/triangle_agi.upc:100-136 (alg 1): for every nonzero
+ * L[i][j] (the first of each row included), walk U's row j from its end
+ * downwards while its columns are at least the smallest column of U's row
+ * i, and advance a cursor down U's row i (both rows ascending), counting
+ * equal columns: the sum over L's nonzeros of |U_i and U_j|.  pulled counts
+ * 2 per (i,j) and one per row-j element read, as the reference does; like
+ * the reference, an empty U row i reads the next stored column as its
+ * "smallest" (only the tally can change).  Returns -1 for a NULL U. */
+int64_t orc_triangle_agi_alg1(const int64_t *loff, const int64_t *lcol, int64_t n, const int64_t *uoff,
+                              const int64_t *ucol, int64_t unnz, int64_t *pulled) {
+  if (!uoff) return -1;
+  int64_t cnt = 0, np = 0;
+  for (int64_t i = 0; i < n; i++) {
+    for (int64_t k = loff[i]; k < loff[i + 1]; k++) {
+      const int64_t j = lcol[k];
+      int64_t start = uoff[i + 1] - 1;
+      const int64_t smallest = uoff[i] < unnz ? ucol[uoff[i]] : 0;
+      np += 2;
+      for (int64_t kk = uoff[j + 1] - 1; kk >= uoff[j]; kk--) {
+        const int64_t w = ucol[kk];
+        np++;
+        if (w < smallest) break;
+        for (int64_t ii = start; ii >= uoff[i]; ii--) {
+          if (w == ucol[ii]) {
+            cnt++;
+            start = ii - 1;
+            break;
+          }
+          if (w > ucol[ii]) {
+            start = ii;
+            break;
+          }
+        }
+      }
+    }
+  }
+  if (pulled) *pulled = np;
+  return cnt;
+}
+
 /* Input generation (not a reference routine; see bale_oracle.h). */
 typedef struct {
   int64_t *out;

@@ -38,6 +38,11 @@ int64_t orc_triangle_agi(const int64_t *offset, const int64_t *nonzero, int64_t 
  * *pushed gets the number of wedge packages pushed.                          */
 int64_t orc_triangle_exstack_push(const int64_t *offset, const int64_t *nonzero,
                                   int64_t numrows, int64_t *pushed);
+/* triangles alg 1, AGI scan of U (apps/triangle_src/triangle_agi.upc:100-136):
+ * sum over L's nonzeros (i,j) of |U_i and U_j|; *pulled gets the reference's
+ * shared-reference tally; -1 for a NULL U. */
+int64_t orc_triangle_agi_alg1(const int64_t *loff, const int64_t *lcol, int64_t n, const int64_t *uoff,
+                              const int64_t *ucol, int64_t unnz, int64_t *pulled);
 /* Work model printed by the reference app (apps/triangle_src/triangle.upc:325-361):
  * pulls = sum_i deg(i) * colcount(i), pushes = sum_i C(deg(i), 2).            */
 void orc_triangle_work(const int64_t *offset, const int64_t *nonzero, int64_t numrows,

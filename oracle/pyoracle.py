@@ -75,6 +75,7 @@ class Oracle:
             "orc_write_dataset": (C.c_int, [C.c_char_p, P64, P64, i64, i64]),
             "orc_read_mm": (C.c_int, [C.c_char_p, P64, P64, P64]),
             "orc_num_cpus": (C.c_int, []),
+            "orc_triangle_agi_alg1": (i64, [P64, P64, i64, P64, P64, i64, P64]),
             "orc_gen_uniform": (None, [P64, i64, i64, C.c_uint64, C.c_int]),
             "orc_gen_values": (None, [P64, i64, C.c_uint64, C.c_int]),
         }
@@ -122,6 +123,14 @@ class Oracle:
     def triangle_agi(self, offset: np.ndarray, nonzero: np.ndarray) -> tuple[int, int]:
         pulled = C.c_int64(0)
         c = self.lib.orc_triangle_agi(_p(offset), _p(nonzero), offset.size - 1, C.byref(pulled))
+        return int(c), int(pulled.value)
+
+    def triangle_agi_alg1(self, loff: np.ndarray, lcol: np.ndarray, uoff: np.ndarray,
+                          ucol: np.ndarray) -> tuple[int, int]:
+        """alg 1: sum over L's nonzeros (i,j) of |U_i and U_j| and the tally."""
+        pulled = C.c_int64(0)
+        c = self.lib.orc_triangle_agi_alg1(_p(loff), _p(lcol), loff.size - 1, _p(uoff), _p(ucol), ucol.size,
+                                           C.byref(pulled))
         return int(c), int(pulled.value)
 
     def triangle_exstack_push(self, offset: np.ndarray, nonzero: np.ndarray) -> tuple[int, int]:

@@ -446,3 +446,41 @@ def test_oracle_generators_equal_the_library_generators(oracle, bale, n, rng, se
     for threads in (1, 3, 0):
         np.testing.assert_array_equal(oracle.gen_uniform(n, rng, seed, threads), want_u)
         np.testing.assert_array_equal(oracle.gen_values(n, seed, threads), want_v)
+
+
+@pytest.mark.skipif(not REF_LIB.exists(), reason="oracle/_ref is built only where the reference tree exists")
+def test_alg1_restatement_matches_reference_with_any_upper_u(oracle, bale):
+    """The restatement of triangle_agi's alg 1 (triangle_agi.upc:100-136) gives
+    the reference's count and shared-reference tally for U = L^T and for
+    upper matrices U that are not L^T (another graph's transpose, L^T with
+    entries dropped): alg 1 sums |U_i and U_j| over L's nonzeros whatever U
+    is.  U's column array carries one zero past its end, as the reference
+    reads the first column of an empty last row."""
+    import ctypes as C
+
+    ref = Reference()
+    rng = np.random.default_rng(5)
+    cases = []
+    for off, col in list(_tiny_graphs())[::37]:
+        cases.append((off, col, off, col))
+    for scale, seed in ((8, 3), (9, 4)):
+        L = bale.gen_rmat(scale, 16, 0.57, 0.19, 0.19, seed)
+        cases.append((L.offset, L.nonzero, L.offset, L.nonzero))
+        L2 = bale.gen_rmat(scale, 8, 0.57, 0.19, 0.19, seed + 10)
+        cases.append((L.offset, L.nonzero, L2.offset, L2.nonzero))  # U from another graph
+        keep = rng.random(L.nnz) < 0.7
+        rows = np.repeat(np.arange(L.numrows), np.diff(L.offset))
+        off3 = np.zeros(L.numrows + 1, np.int64)
+        np.add.at(off3, rows[keep] + 1, 1)
+        cases.append((L.offset, L.nonzero, np.cumsum(off3), np.ascontiguousarray(L.nonzero[keep])))
+    for loff, lcol, moff, mcol in cases:
+        n = loff.size - 1
+        uo, uc = oracle.transpose(moff, mcol, n)
+        ucp = np.concatenate([uc, np.zeros(1, np.int64)])
+        Lm = ref._mat(loff, lcol)
+        Um = ref._mat(uo, ucp)
+        Um.nnz = Um.lnnz = uc.size
+        cnt, sr = C.c_int64(0), C.c_int64(0)
+        assert ref.lib.triangle_agi(C.byref(cnt), C.byref(sr), C.byref(Lm), C.byref(Um), 1) >= 0
+        got = oracle.triangle_agi_alg1(loff, lcol, uo, uc)
+        assert got == (cnt.value, sr.value)

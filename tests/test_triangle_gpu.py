@@ -255,3 +255,74 @@ def test_default_mode_choice(cuda, bale, graph, want):
     assert cnt == fcnt and sr == fsr
     if graph == "kron":
         assert cnt == bale.kronecker_triangles(1, [3, 4, 5, 9, 16, 25])
+
+
+def _transpose(oracle, off, col):
+    uo, uc = oracle.transpose(off, col, off.size - 1)
+    return uo, uc
+
+
+@pytest.mark.parametrize("fn", DROPINS)
+def test_alg1_with_u_transpose_counts_like_alg0(cuda, bale, oracle, golden, fn):
+    """alg 1 (apps/triangle_src/triangle_agi.upc:100-136) with U = L^T, as the
+    apps pass it (triangle.upc:306-307): every drop-in gives alg 0's count,
+    on the reference's golden graphs and on R-MAT graphs."""
+    d = golden("triangles")
+    graphs = [(d[f"{g}/offset"], d[f"{g}/nonzero"], int(d[f"{g}/triangle_agi"][0])) for g in d["graphs"]]
+    for scale in (10, 14):
+        L = bale.gen_rmat(scale, 16, 0.57, 0.19, 0.19, 200 + scale)
+        graphs.append((L.offset, L.nonzero, oracle.triangle_agi(L.offset, L.nonzero)[0]))
+    for off, col, want in graphs:
+        uo, uc = _transpose(oracle, off, col)
+        L = bale.SparseMatrix(off, col)
+        U = bale.SparseMatrix(uo, uc, off.size - 1)
+        assert getattr(bale, fn)(L, U, 1)[0] == want
+
+
+def test_alg1_with_other_upper_matrices_matches_oracle(cuda, bale, oracle):
+    """alg 1 sums |U_i and U_j| over L's nonzeros for any tidy upper U: U from
+    another graph, and L^T with a third of its entries dropped, against the
+    oracle's restatement of the reference loop (pinned to the reference)."""
+    rng = np.random.default_rng(11)
+    for scale in (9, 12):
+        L = bale.gen_rmat(scale, 16, 0.57, 0.19, 0.19, 300 + scale)
+        L2 = bale.gen_rmat(scale, 8, 0.57, 0.19, 0.19, 400 + scale)
+        keep = rng.random(L.nnz) < 0.67
+        rows = np.repeat(np.arange(L.numrows), np.diff(L.offset))
+        o3 = np.zeros(L.numrows + 1, np.int64)
+        np.add.at(o3, rows[keep] + 1, 1)
+        for moff, mcol in ((L2.offset, L2.nonzero), (np.cumsum(o3), np.ascontiguousarray(L.nonzero[keep]))):
+            uo, uc = _transpose(oracle, moff, mcol)
+            want = oracle.triangle_agi_alg1(L.offset, L.nonzero, uo, uc)[0]
+            U = bale.SparseMatrix(uo, uc, L.numrows)
+            for fn in ("triangle_agi", "triangle_exstack_push"):
+                assert getattr(bale, fn)(L, U, 1)[0] == want
+
+
+def test_alg1_needs_a_well_formed_u(cuda, bale, oracle):
+    """alg 1 without U is an error (the reference returns -1 for a NULL U);
+    so is a U that is not strictly upper, or not ascending; the library
+    stays usable."""
+    off, col = _clique(7)
+    L = bale.SparseMatrix(off, col)
+    with pytest.raises(bale.BaleError):
+        bale.triangle_agi(L, None, 1)
+    uo, uc = _transpose(oracle, off, col)
+    bad = uc.copy()
+    bad[0] = 0  # row 0 of U holding column 0: not strictly upper
+    with pytest.raises(bale.BaleError):
+        bale.triangle_agi(L, bale.SparseMatrix(uo, bad, 7), 1)
+    bad = uc.copy()
+    bad[0], bad[1] = bad[1], bad[0]  # not ascending
+    with pytest.raises(bale.BaleError):
+        bale.triangle_agi(L, bale.SparseMatrix(uo, bad, 7), 1)
+    assert bale.triangle_agi(L, bale.SparseMatrix(uo, uc, 7), 1)[0] == 35
+
+
+def test_alg1_full_size_rmat_scale22(cuda, bale, oracle):
+    """alg 1 on the R-MAT scale-22 configuration with U = L^T: the count of
+    alg 0, exact against the multi-threaded oracle."""
+    L = bale.gen_rmat(22, 16, 0.57, 0.19, 0.19, 6)
+    uo, uc = _transpose(oracle, L.offset, L.nonzero)
+    cnt = bale.triangle_agi(L, bale.SparseMatrix(uo, uc, L.numrows), 1)[0]
+    assert cnt == oracle.triangle_agi_mt(L.offset, L.nonzero)

@@ -27,7 +27,7 @@ __all__ = [
     "triangle_agi", "triangle_exstack_push", "triangle_exstack2_push",
     "triangle_convey_push", "triangle_agi_iter",
     "histo_dev", "ig_dev", "triangle_dev", "ig_dev_noalloc", "TrianglePrepared", "l2_red_rate",
-    "graph_build_dev", "gen_rmat_dev", "transpose_dev", "permute_dev", "rand_perm_dev", "rand_perm_exstack_dev",
+    "graph_build_dev", "gen_rmat_dev", "transpose_dev", "permute_dev", "rand_perm_dev", "rand_perm_exstack_dev", "rand_perm_exstack2_dev",
     "write_matrix_mm", "mm_header", "read_matrix_mm_dev",
     "write_sparse_matrix", "write_sparse_matrix_dev", "sparse_matrix_header", "read_sparse_matrix_dev",
     "splitmix64", "gen_uniform", "gen_values", "gen_uniform_dev", "gen_values_dev", "gen_negative_table", "gen_zipf",
@@ -360,7 +360,9 @@ def permute_dev(offset, nonzero, numcols: int, rperminv, cperminv, stream=None):
 
 
 def rand_perm_dev(n: int, seed: int, device=None, stream=None):
-    """spmat's rand_permp_agi(n, seed) on the device (a device int64 tensor)."""
+    """spmat's rand_permp_agi(n, seed) on the device (a device int64 tensor).
+    Seed 0 continues the C library's drand48 stream; every call leaves that
+    stream past the reference's last draw."""
     import torch
 
     dev = device if device is not None else torch.device("cuda", torch.cuda.current_device())
@@ -379,6 +381,18 @@ def rand_perm_exstack_dev(n: int, seed: int, buf_cnt: int = 1024, device=None, s
     out = torch.empty(max(n, 1), dtype=torch.int64, device=dev)
     _status(_lib.bale_rand_perm_exstack_dev(int(n), seed & (2**64 - 1), int(buf_cnt), _dptr(out, "perm"),
                                             _stream(stream)), "bale_rand_perm_exstack_dev")
+    return out[:n]
+
+
+def rand_perm_exstack2_dev(n: int, seed: int, buf_cnt: int = 1024, device=None, stream=None):
+    """spmat's rand_permp_exstack2(n, seed, buf_cnt) on the device, which in
+    the reference is rand_permp_exstack(n, seed, buf_cnt)."""
+    import torch
+
+    dev = device if device is not None else torch.device("cuda", torch.cuda.current_device())
+    out = torch.empty(max(n, 1), dtype=torch.int64, device=dev)
+    _status(_lib.bale_rand_perm_exstack2_dev(int(n), seed & (2**64 - 1), int(buf_cnt), _dptr(out, "perm"),
+                                             _stream(stream)), "bale_rand_perm_exstack2_dev")
     return out[:n]
 
 

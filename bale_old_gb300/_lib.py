@@ -90,6 +90,7 @@ SIGNATURES: dict[str, tuple[object, list[object]]] = {
     "bale_permute_dev": (C.c_int, [VP, VP, i64, i64, i64, VP, VP, VP, VP, VP]),
     "bale_rand_perm_dev": (C.c_int, [i64, C.c_uint64, VP, VP]),
     "bale_rand_perm_exstack_dev": (C.c_int, [i64, C.c_uint64, i64, VP, VP]),
+    "bale_rand_perm_exstack2_dev": (C.c_int, [i64, C.c_uint64, i64, VP, VP]),
     "bale_write_matrix_mm": (C.c_int, [C.POINTER(sparsemat_t), C.c_char_p]),
     "bale_mm_header": (C.c_int, [C.c_char_p, P64, P64, P64, P64, C.POINTER(C.c_int)]),
     "bale_read_matrix_mm_dev": (C.c_int, [C.c_char_p, VP, VP, VP]),

@@ -6,6 +6,7 @@
 // their claims stay in L2.
 #include <algorithm>
 #include <climits>
+#include <cstdlib>
 
 #include "sort.cuh"
 
@@ -196,6 +197,21 @@ __global__ void dart_kstar_kernel(const uint32_t *__restrict__ bits, const uint3
   words[1] = static_cast<unsigned int>(lo);
 }
 
+// rand_permp_agi stops drawing at the throw that places its n-th dart:
+// words[6] = the smallest t with S(t + 1) >= n (the caller has checked that
+// the throws so far hold n hits).
+__global__ void dart_nth_hit_kernel(const uint32_t *__restrict__ bits, const uint32_t *__restrict__ wpre,
+                                    int64_t nthrows, int64_t n, unsigned int *__restrict__ words) {
+  if (threadIdx.x | blockIdx.x) return;
+  int64_t lo = 0, hi = nthrows - 1;
+  while (lo < hi) {
+    const int64_t mid = lo + (hi - lo) / 2;
+    if (dart_S(bits, wpre, mid + 1) >= n) hi = mid;
+    else lo = mid + 1;
+  }
+  words[6] = static_cast<unsigned int>(lo);
+}
+
 // Throws from t0 on are drawn again for the rounds from k* on (no draw is
 // lost there): forget their claims and hits.
 __global__ void __launch_bounds__(256)
@@ -326,7 +342,8 @@ struct DartWs {
   uint32_t *owner, *target, *pos;           // per slot
   uint32_t *bits, *pc, *wpre;               // hit bits per throw, popcounts and their prefix per word
   uint32_t *hist, *hoff, *bsum, *rstart;    // radix pass, scans, rounds
-  unsigned int *words;  // [0] scan total, [1] k*, [2] last throw, [3] rounds, [4] rounds status, [5] lost chains
+  unsigned int *words;  // [0] scan total, [1] k*, [2] last throw, [3] rounds, [4] rounds status, [5] lost chains,
+                        // [6] the throw of rand_permp_agi's n-th hit
 };
 
 size_t dart_ws(int64_t m, int64_t nkeys, int64_t nbits, DartWs *w, char *base) {
@@ -398,10 +415,15 @@ int dart_claims(const uint64_t *keys, int64_t nk, int tb, int64_t nwords, DartWs
 // needed are not known in advance: about 1.39 n hit n distinct slots of 2n.
 // Take 1.5 n + 1024 (and for the exstack rounds from k* on, which throw at
 // most per_round pending darts, 2 per_round + 1024) and double while short.
-int rand_perm_darts(int64_t n, uint64_t seed, int64_t per_round, int64_t *d_perm, cudaStream_t st,
-                    const char *who) {
+//
+// x0 is the generator's state before the first draw; *draws receives the
+// number of lrand48 draws the reference makes (rand_permp_agi: up to the
+// throw of the n-th hit; rand_permp_exstack: up to the end of the last
+// round, plus the draw lost by each of the k* rounds that found the buffer
+// full).
+int rand_perm_darts(int64_t n, uint64_t x0, int64_t per_round, int64_t *d_perm, cudaStream_t st, const char *who,
+                    int64_t *draws) {
   const int64_t m = 2 * n;
-  const uint64_t x0 = ((seed & 0xffffffffull) << 16) | 0x330eull;
   for (int grow = 0; grow < 6; grow++) {
     int64_t nt = (n + n / 2 + 1024) << grow, tail = 0;
     if (per_round) {
@@ -424,17 +446,20 @@ int rand_perm_darts(int64_t n, uint64_t seed, int64_t per_round, int64_t *d_perm
     int rc = BALE_OK;
     const uint64_t *keys = dart_region_keys(x0, 0, nt, per_round, INT64_MAX, m, tb, w, st, &rc);
     if (rc != BALE_OK || (rc = dart_claims(keys, nt, tb, nwords, w, st)) != BALE_OK) return rc;
-    unsigned int h[6] = {0, 0, 0, 0, 0, 0};
+    unsigned int h[7] = {0, 0, 0, 0, 0, 0, 0};
+    int64_t kstar_used = 0;
     if (!per_round) {
       if ((rc = read_words(w.words, h, 1, st)) != BALE_OK) return rc;
       if (static_cast<int64_t>(h[0]) < n) continue;
       dart_place_agi_kernel<<<static_cast<unsigned>((nt + kDartKeysPerBlock - 1) / kDartKeysPerBlock), 256, 0, st>>>(
           keys, nt, tb, w.bits, w.wpre, n, w.target);
+      dart_nth_hit_kernel<<<1, 32, 0, st>>>(w.bits, w.wpre, nt, n, w.words);
     } else {
       dart_kstar_kernel<<<1, 32, 0, st>>>(w.bits, w.wpre, nt, per_round, n, w.words);
       if ((rc = read_words(w.words, h, 2, st)) != BALE_OK) return rc;
       if (h[1] == ~0u) continue;
       const int64_t kstar = h[1], t0 = kstar * per_round, t2 = t0 + tail;
+      kstar_used = kstar;
       dart_forget_kernel<<<grid_for(std::max(m, nwords)), 256, 0, st>>>(w.owner, m, static_cast<uint32_t>(t0), w.bits,
                                                                          nwords);
       const uint64_t *tk = dart_region_keys(x0, t0, t2, per_round, kstar, m, tb, w, st, &rc);
@@ -453,11 +478,12 @@ int rand_perm_darts(int64_t n, uint64_t seed, int64_t per_round, int64_t *d_perm
     if ((rc = excl_scan(w.owner, w.pos, m, w.bsum, w.words, st)) != BALE_OK) return rc;
     dart_perm_kernel<<<grid_for(m), 256, 0, st>>>(w.target, w.pos, m, n, d_perm);
     BALE_CUDA_OK(cudaGetLastError());
-    if ((rc = read_words(w.words, h, 6, st)) != BALE_OK) return rc;
+    if ((rc = read_words(w.words, h, 7, st)) != BALE_OK) return rc;
     if (static_cast<int64_t>(h[0]) != n || h[5] != 0) {
       set_error("%s: %u darts placed of %lld (%u lost)", who, h[0], static_cast<long long>(n), h[5]);
       return BALE_EINVAL;
     }
+    *draws = per_round ? static_cast<int64_t>(h[2]) + kstar_used : static_cast<int64_t>(h[6]) + 1;
     return BALE_OK;
   }
   set_error("%s: too many throws for n = %lld", who, static_cast<long long>(n));
@@ -465,16 +491,58 @@ int rand_perm_darts(int64_t n, uint64_t seed, int64_t per_round, int64_t *d_perm
 }
 
 // The reference reseeds only when its int seed is nonzero (spmat_agi.upc:61,
-// spmat_exstack.upc:92); with 0 it continues the C library's drand48 stream
-// from wherever the caller left it.  The device path always starts from
-// srand48(seed), so it refuses such a seed rather than return a permutation
-// the reference would not.
-bool refuse_stream_seed(uint64_t seed, const char *who) {
-  if ((seed & 0xffffffffull) != 0) return false;
-  set_error("%s: seed 0 (low 32 bits) continues the C library's drand48 stream in the reference; "
-            "pass a nonzero seed",
-            who);
-  return true;
+// spmat_exstack.upc:92: `if (seed != 0) srand48(seed)`); with 0 it continues
+// the C library's drand48 stream from wherever the caller left it, and with
+// any seed it leaves that stream just past its last draw, where a later
+// lrand48() or seed-0 call picks it up.  The entry points do the same with
+// the process's C library state: seed48 installs a state and returns the
+// previous one, so reading it is two calls.  (Like the reference, this is
+// not safe against other threads drawing from the same stream meanwhile.)
+uint64_t libc_drand48_state() {
+  unsigned short probe[3] = {0, 0, 0};
+  const unsigned short *prev = seed48(probe);
+  unsigned short keep[3] = {prev[0], prev[1], prev[2]};
+  seed48(keep);
+  return static_cast<uint64_t>(keep[0]) | static_cast<uint64_t>(keep[1]) << 16 | static_cast<uint64_t>(keep[2]) << 32;
+}
+
+void set_libc_drand48_state(uint64_t x) {
+  unsigned short s[3] = {static_cast<unsigned short>(x & 0xffff), static_cast<unsigned short>(x >> 16 & 0xffff),
+                         static_cast<unsigned short>(x >> 32 & 0xffff)};
+  seed48(s);
+}
+
+uint64_t host_lcg_jump(uint64_t x, uint64_t k) {
+  uint64_t a = kLcgA, c = kLcgC, ra = 1, rc = 0;
+  while (k) {
+    if (k & 1) {
+      ra = (ra * a) & kLcgMask;
+      rc = (rc * a + c) & kLcgMask;
+    }
+    c = (c * a + c) & kLcgMask;
+    a = (a * a) & kLcgMask;
+    k >>= 1;
+  }
+  return (ra * x + rc) & kLcgMask;
+}
+
+// The generator's state before the first draw: srand48(seed) for a seed
+// whose low 32 bits (the reference's int) are nonzero, else the C library's.
+uint64_t start_state(uint64_t seed) {
+  if ((seed & 0xffffffffull) == 0) return libc_drand48_state();
+  const uint64_t x0 = ((seed & 0xffffffffull) << 16) | 0x330eull;
+  set_libc_drand48_state(x0);  // srand48(seed), as the reference does before it draws
+  return x0;
+}
+
+// The darts, then the C library's stream left past the reference's last draw.
+int rand_perm_entry(int64_t n, uint64_t seed, int64_t per_round, int64_t *d_perm, cudaStream_t st, const char *who) {
+  const uint64_t x0 = start_state(seed);
+  if (n == 0) return BALE_OK;  // the reference draws nothing either
+  int64_t draws = 0;
+  const int rc = rand_perm_darts(n, x0, per_round, d_perm, st, who, &draws);
+  if (rc == BALE_OK) set_libc_drand48_state(host_lcg_jump(x0, static_cast<uint64_t>(draws)));
+  return rc;
 }
 
 }  // namespace
@@ -489,9 +557,7 @@ int bale_rand_perm_dev(int64_t n, uint64_t seed, int64_t *d_perm, void *stream) 
     set_error("bale_rand_perm_dev: bad arguments (n=%lld)", static_cast<long long>(n));
     return BALE_EINVAL;
   }
-  if (n == 0) return BALE_OK;  // the reference draws nothing either
-  if (refuse_stream_seed(seed, "bale_rand_perm_dev")) return BALE_EINVAL;
-  return rand_perm_darts(n, seed, 0, d_perm, static_cast<cudaStream_t>(stream), "bale_rand_perm_dev");
+  return rand_perm_entry(n, seed, 0, d_perm, static_cast<cudaStream_t>(stream), "bale_rand_perm_dev");
 }
 
 int bale_rand_perm_exstack_dev(int64_t n, uint64_t seed, int64_t buf_cnt, int64_t *d_perm, void *stream) {
@@ -500,11 +566,22 @@ int bale_rand_perm_exstack_dev(int64_t n, uint64_t seed, int64_t buf_cnt, int64_
               static_cast<long long>(buf_cnt));
     return BALE_EINVAL;
   }
-  if (n == 0) return BALE_OK;  // the reference draws nothing either
-  if (refuse_stream_seed(seed, "bale_rand_perm_exstack_dev")) return BALE_EINVAL;
   // a buffer that holds every dart never fills: the same as one of n
-  return rand_perm_darts(n, seed, std::min(buf_cnt, n), d_perm, static_cast<cudaStream_t>(stream),
-                         "bale_rand_perm_exstack_dev");
+  return rand_perm_entry(n, seed, std::min(buf_cnt, std::max<int64_t>(n, 1)), d_perm,
+                         static_cast<cudaStream_t>(stream), "bale_rand_perm_exstack_dev");
+}
+
+// The reference's rand_permp_exstack2 returns rand_permp_exstack(N, seed,
+// buf_cnt) (spmat/spmat_exstack2.upc:60-73; its own exstack2 form is
+// compiled out), so this is that permutation too.
+int bale_rand_perm_exstack2_dev(int64_t n, uint64_t seed, int64_t buf_cnt, int64_t *d_perm, void *stream) {
+  if (n < 0 || n >= (int64_t(1) << 30) || buf_cnt < 1 || (n > 0 && !d_perm)) {
+    set_error("bale_rand_perm_exstack2_dev: bad arguments (n=%lld, buf_cnt=%lld)", static_cast<long long>(n),
+              static_cast<long long>(buf_cnt));
+    return BALE_EINVAL;
+  }
+  return rand_perm_entry(n, seed, std::min(buf_cnt, std::max<int64_t>(n, 1)), d_perm,
+                         static_cast<cudaStream_t>(stream), "bale_rand_perm_exstack2_dev");
 }
 
 }  // extern "C"

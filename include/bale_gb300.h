@@ -212,13 +212,17 @@ BALE_API int bale_gen_rmat_dev(int64_t scale, int64_t edgefactor, double a, doub
 /*    (spmat/spmat_exstack.upc:62-190), whose darts fly in rounds of buf_cnt; */
 /*    rand_permp(n, seed) (spmat/spmat_utils.upc:63-74) is buf_cnt = 1024.    */
 /*    A different permutation from rand_permp_agi's for the same seed.       */
-/* Both random permutations take 0 <= n < 2^30.  Only the low 32 bits of   */
-/* seed count (the reference's seed is an int).  A seed whose low 32 bits   */
-/* are 0 is refused with BALE_EINVAL for n > 0: the reference does not      */
-/* reseed then but continues the C library's drand48 stream from wherever   */
-/* the caller left it (spmat_agi.upc:61, spmat_exstack.upc:92), and these   */
-/* always start from srand48(seed).  Neither advances the C library's       */
-/* stream, which the reference leaves just past its last draw.              */
+/*  * bale_rand_perm_exstack2_dev: rand_permp_exstack2(n, seed, buf_cnt)     */
+/*    (spmat/spmat_exstack2.upc:60-73), which in the reference returns       */
+/*    rand_permp_exstack(n, seed, buf_cnt): the same permutation.            */
+/* The random permutations take 0 <= n < 2^30.  Only the low 32 bits of     */
+/* seed count (the reference's seed is an int).  As in the reference        */
+/* (spmat_agi.upc:61, spmat_exstack.upc:92), a nonzero seed calls           */
+/* srand48(seed) first and a zero one continues the C library's drand48     */
+/* stream from wherever the caller left it; either way the call leaves that */
+/* stream just past the reference's last draw, where a later lrand48() or a */
+/* seed-0 call picks it up (the process's C library state, not thread-safe, */
+/* like the reference's).                                                   */
 /* BALE_EINPUT for malformed offsets or columns, or a rperminv/cperminv     */
 /* that is not a permutation.                                               */
 BALE_API int bale_transpose_dev(const int64_t *d_offset, const int64_t *d_nonzero, int64_t numrows,
@@ -231,6 +235,8 @@ BALE_API int bale_permute_dev(const int64_t *d_offset, const int64_t *d_nonzero,
 BALE_API int bale_rand_perm_dev(int64_t n, uint64_t seed, int64_t *d_perm, void *stream);
 BALE_API int bale_rand_perm_exstack_dev(int64_t n, uint64_t seed, int64_t buf_cnt, int64_t *d_perm,
                                         void *stream);
+BALE_API int bale_rand_perm_exstack2_dev(int64_t n, uint64_t seed, int64_t buf_cnt, int64_t *d_perm,
+                                         void *stream);
 
 /* MatrixMarket files of the reference's kind (spmat/spmat_utils.upc:128-149 */
 /* write_matrix_mm, :217-370 read_matrix_mm_to_dist): "%%MatrixMarket matrix */

@@ -229,6 +229,7 @@ class Reference:
             "rand_permp_agi": (P64, [i64, C.c_int]),
             "rand_permp_exstack": (P64, [i64, C.c_int, i64]),
             "rand_permp": (P64, [i64, C.c_int]),
+            "rand_permp_exstack2": (P64, [i64, C.c_int, i64]),
             "write_matrix_mm": (C.c_int, [PS, C.c_char_p]),
             "read_matrix_mm_to_dist": (PS, [C.c_char_p]),
             "write_sparse_matrix_agi": (i64, [C.c_char_p, PS]),
@@ -328,6 +329,11 @@ class Reference:
         """spmat's rand_permp_exstack (spmat/spmat_exstack.upc:62-190) at one
         PE; rand_permp (spmat/spmat_utils.upc:63-74) calls it with 1024."""
         p = self.lib.rand_permp_exstack(n, seed, buf_cnt)
+        return np.ctypeslib.as_array(p, shape=(n,)).copy()
+
+    def rand_perm_exstack2(self, n: int, seed: int, buf_cnt: int = 1024) -> np.ndarray:
+        """spmat's rand_permp_exstack2 (spmat/spmat_exstack2.upc:60-73) at one PE."""
+        p = self.lib.rand_permp_exstack2(n, seed, buf_cnt)
         return np.ctypeslib.as_array(p, shape=(n,)).copy()
 
     def rand_permp(self, n: int, seed: int) -> np.ndarray:

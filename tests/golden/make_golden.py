@@ -174,6 +174,12 @@ def make_spmat(ref: Reference) -> dict:
         cases[f"xperm_{n}_{seed}_{b}"] = ref.rand_perm_exstack(n, seed, b)
     cases["xperms"] = np.array(xperms)
     cases["permp_100000_31"] = ref.rand_permp(100_000, 31)
+    # rand_permp_exstack2(n, seed, buf_cnt), as the randperm app's model 4 calls it
+    x2perms = []
+    for n, seed, b in ((1, 1, 1024), (40, 9, 2), (1000, 99, 7), (5000, 8, 64), (100_000, 31, 1024)):
+        x2perms.append(f"x2perm_{n}_{seed}_{b}")
+        cases[f"x2perm_{n}_{seed}_{b}"] = ref.rand_perm_exstack2(n, seed, b)
+    cases["x2perms"] = np.array(x2perms)
     # MatrixMarket: files written by the reference's writer, and a hand-made
     # one with rows out of order, comment-free, integer field; read back by
     # the reference's reader

@@ -54,20 +54,34 @@ def test_version_and_error_calls_need_no_gpu(bale):
     assert isinstance(bale._last_error(), str)
 
 
-def test_random_permutations_refuse_a_stream_continuing_seed(bale):
-    """A seed whose low 32 bits are 0 makes the reference continue the C
-    library's drand48 stream instead of reseeding; the device entry points
-    refuse it before any device work (n = 0 draws nothing and is accepted)."""
+def test_random_permutations_follow_the_reference_seed_rule_on_empty_input(bale):
+    """The reference calls srand48(seed) for a seed whose low 32 bits (its
+    int) are nonzero and otherwise continues the C library's drand48 stream
+    (spmat_agi.upc:61, spmat_exstack.upc:92), even when it then draws
+    nothing.  With n = 0 the entry points do no device work, so this runs
+    without a GPU: the next lrand48() shows the stream they left."""
     from bale_old_gb300._lib import _lib
 
-    fake = C.c_void_p(256)  # never dereferenced: the seed is refused first
-    for seed in (0, 1 << 32, 7 << 32):
-        assert _lib.bale_rand_perm_dev(10, seed, fake, None) == 1
-        assert "seed 0" in bale._last_error()
-        assert _lib.bale_rand_perm_exstack_dev(10, seed, 1024, fake, None) == 1
-        assert "seed 0" in bale._last_error()
-    assert _lib.bale_rand_perm_dev(0, 0, None, None) == 0
-    assert _lib.bale_rand_perm_exstack_dev(0, 0, 1024, None, None) == 0
+    libc = C.CDLL(None)
+    libc.srand48.argtypes = [C.c_long]
+    libc.lrand48.restype = C.c_long
+
+    def next_after(call, start):
+        libc.srand48(start)
+        assert call() == 0
+        return libc.lrand48()
+
+    for call in (lambda s: (lambda: _lib.bale_rand_perm_dev(0, s, None, None)),
+                 lambda s: (lambda: _lib.bale_rand_perm_exstack_dev(0, s, 1024, None, None)),
+                 lambda s: (lambda: _lib.bale_rand_perm_exstack2_dev(0, s, 1024, None, None))):
+        for seed in (0, 1 << 32, 7 << 32):  # low 32 bits 0: the stream continues
+            libc.srand48(99)
+            want = libc.lrand48()
+            assert next_after(call(seed), 99) == want
+        libc.srand48(12345)
+        want = libc.lrand48()
+        assert next_after(call(12345), 99) == want  # reseeded with 12345
+        assert next_after(call((5 << 32) + 12345), 99) == want  # only the low 32 bits count
 
 
 def test_a_c_program_compiles_links_and_runs_against_the_library(tmp_path):

@@ -140,6 +140,63 @@ def test_rand_perm_exstack_matches_oracle_at_size(cuda, bale, oracle, n, seed, b
     np.testing.assert_array_equal(got, oracle.rand_perm_exstack(n, seed, b))
 
 
+def test_rand_perm_exstack2_matches_reference_golden(cuda, bale, golden):
+    """rand_permp_exstack2 (spmat/spmat_exstack2.upc:60-73) as the reference
+    computes it, against its own outputs, and equal to the exstack form."""
+    d = golden("spmat")
+    for p in d["x2perms"]:
+        _, n, seed, b = str(p).split("_")
+        got = bale.rand_perm_exstack2_dev(int(n), int(seed), int(b)).cpu().numpy()
+        np.testing.assert_array_equal(got, d[p], err_msg=str(p))
+    np.testing.assert_array_equal(bale.rand_perm_exstack2_dev(3000, 2, 4096).cpu().numpy(),
+                                  bale.rand_perm_exstack_dev(3000, 2, 4096).cpu().numpy())
+
+
+def _libc():
+    import ctypes
+
+    libc = ctypes.CDLL(None)
+    libc.srand48.argtypes = [ctypes.c_long]
+    libc.srand48.restype = None
+    libc.lrand48.restype = ctypes.c_long
+    return libc
+
+
+def test_rand_perm_seed_zero_continues_the_c_library_stream(cuda, bale, oracle):
+    """Seed 0 continues the C library's drand48 stream and every call leaves
+    it just past the reference's last draw: sequences of seeded and seed-0
+    calls on the device give the oracle's permutations (pinned to the
+    reference on the same sequences) and leave the same stream behind, read
+    out with a final lrand48()."""
+    libc = _libc()
+
+    def run(impl, c):
+        if c[0] == "agi":
+            out = impl.rand_perm_dev(c[1], c[2]) if impl is bale else impl.rand_perm(c[1], c[2])
+        else:
+            out = (impl.rand_perm_exstack_dev(c[1], c[2], c[3]) if impl is bale
+                   else impl.rand_perm_exstack(c[1], c[2], c[3]))
+        return out.cpu().numpy() if impl is bale else out
+
+    sequences = [
+        [("agi", 10, 0), ("agi", 1, 0), ("x", 7, 0, 3), ("x", 100, 0, 1024), ("x", 33, 0, 1)],
+        [("agi", 5, 9), ("agi", 12, 0), ("x", 40, 4, 2), ("x", 40, 0, 2), ("agi", 3, 0)],
+        [("x", 1000, 0, 7), ("agi", 1000, 0), ("x", 64, 0, 64), ("x", 65, 0, 64)],
+        [("agi", 100_000, 0), ("x", 70_001, 0, 1024), ("agi", 4097, 77), ("x", 5000, 0, 64)],
+    ]
+    for start in (0, 5, 123456):
+        for calls in sequences:
+            libc.srand48(start)
+            dev = [run(bale, c) for c in calls]
+            dev_next = libc.lrand48()
+            libc.srand48(start)
+            orc = [run(oracle, c) for c in calls]
+            orc_next = libc.lrand48()
+            for c, a, b in zip(calls, dev, orc):
+                np.testing.assert_array_equal(a, b, err_msg=f"start {start} {c}")
+            assert dev_next == orc_next, (start, calls)
+
+
 def test_rand_perm_exstack_rejects_bad_arguments(cuda, bale):
     with pytest.raises(bale.BaleError):
         bale.rand_perm_exstack_dev(100, 1, 0)

@@ -484,3 +484,17 @@ def test_alg1_restatement_matches_reference_with_any_upper_u(oracle, bale):
         assert ref.lib.triangle_agi(C.byref(cnt), C.byref(sr), C.byref(Lm), C.byref(Um), 1) >= 0
         got = oracle.triangle_agi_alg1(loff, lcol, uo, uc)
         assert got == (cnt.value, sr.value)
+
+
+@pytest.mark.skipif(not REF_LIB.exists(), reason="oracle/_ref is built only where the reference tree exists")
+def test_rand_permp_exstack2_is_the_exstack_form(oracle, golden):
+    """The reference's rand_permp_exstack2 returns rand_permp_exstack (spmat/
+    spmat_exstack2.upc:60-73): its golden outputs equal the exstack
+    restatement's, and the reference's two functions agree on fresh cases."""
+    d = golden("spmat")
+    for p in d["x2perms"]:
+        _, n, seed, b = str(p).split("_")
+        np.testing.assert_array_equal(oracle.rand_perm_exstack(int(n), int(seed), int(b)), d[p], err_msg=str(p))
+    ref = Reference()
+    for n, seed, b in ((77, 3, 5), (2048, 11, 1024)):
+        np.testing.assert_array_equal(ref.rand_perm_exstack2(n, seed, b), ref.rand_perm_exstack(n, seed, b))

@@ -10,6 +10,12 @@ events after warm-up:
            request counts -> ig.part_min_table_bytes, ig.part_min_requests;
 * histo -- plain L2 reductions vs the region partition across table sizes
            -> histo.part_min_table_bytes, histo.part_min_updates;
+* tri   -- the intersection strategy per graph: wedge probes (bitmap and
+           staged search at the far vertex) or the bitmap/search hybrid over
+           rows i, timed on R-MAT, Erdos-Renyi and Kronecker graphs, with the
+           rule keyed on the reference's work model (pulls and pushes,
+           apps/triangle_src/triangle.upc:325-369) fitted to the times ->
+           tri.wedge_pull_pct, tri.wedge_push_per_nnz;
 * batch -- tile sizes per size class, the standalone thresholds and the
            number of side streams of the batched graph, by coordinate
            descent on the small and full uneven mixes (bale_old_gb300.mix).
@@ -132,6 +138,76 @@ def tune_histo(quick: bool) -> tuple[dict, list]:
     return knobs, rows
 
 
+def work_model(offset, nonzero) -> tuple[int, int]:
+    """The reference's work model of alg 0 (apps/triangle_src/triangle.upc:
+    325-369): pulls = sum over nonzeros (i,j) of d_j; pushes = sum over rows
+    of C(d, 2)."""
+    import numpy as np
+
+    deg = np.diff(offset)
+    pushes = int((deg * (deg - 1) // 2).sum())
+    pulls = int(deg[nonzero].sum()) if nonzero.size else 0
+    return pulls, pushes
+
+
+def fit_tri_rule(rows: list[dict]) -> tuple[int, int]:
+    """Thresholds (pull_pct, push_per_nnz) of the rule "wedges when pulls >=
+    pull_pct % of the pushes or pushes >= push_per_nnz per nonzero" that
+    minimise the summed time of the chosen path over the measured graphs;
+    ties go to the larger thresholds.  rows: pulls, pushes, nnz, wedge_ms,
+    hybrid_ms."""
+    ratios = sorted({r["pulls"] * 100.0 / max(r["pushes"], 1) for r in rows})
+    per_nnz = sorted({r["pushes"] / max(r["nnz"], 1) for r in rows})
+    pct_cands = sorted({int(x) + 1 for x in ratios} | {int((a + b) / 2) for a, b in zip(ratios, ratios[1:])} | {150})
+    ppn_cands = sorted({int(x) + 1 for x in per_nnz} | {int((a + b) / 2) for a, b in zip(per_nnz, per_nnz[1:])}
+                       | {128, 1 << 30})
+
+    def cost(pct, ppn):
+        t = 0.0
+        for r in rows:
+            wedge = r["pushes"] == 0 or r["pulls"] * 100 >= pct * r["pushes"] or r["pushes"] >= ppn * r["nnz"]
+            t += r["wedge_ms"] if wedge else r["hybrid_ms"]
+        return t
+
+    best = min(((cost(p, q), -p, -q) for p in pct_cands for q in ppn_cands))
+    return -best[1], -best[2]
+
+
+def tune_tri(quick: bool) -> tuple[dict, list]:
+    import torch
+
+    import bale_old_gb300 as bale
+
+    dev = torch.device("cuda:0")
+    graphs = [("rmat", s) for s in ((18, 20) if quick else (16, 18, 20, 21))]
+    graphs += [("er", (lg, d)) for lg, d in (((19, 32), (20, 32), (18, 128)) if quick else
+                                              ((19, 32), (20, 32), (21, 32), (18, 64), (18, 128), (20, 64)))]
+    graphs += [("kron", (3, 4, 5, 9, 16, 25))]
+    rows = []
+    bale.tune_set("tri.choose_min_nnz", 1)  # the choice is what is being fitted
+    for kind, g in graphs:
+        if kind == "rmat":
+            L = bale.gen_rmat(g, 16, 0.57, 0.19, 0.19, 6)
+        elif kind == "er":
+            L = bale.gen_erdos_renyi(1 << g[0], g[1] / (1 << g[0]), 7)
+        else:
+            L = bale.gen_kronecker(1, list(g))
+        off, col = torch.from_numpy(L.offset).to(dev), torch.from_numpy(L.nonzero).to(dev)
+        cnt = torch.zeros(1, dtype=torch.int64, device=dev)
+        pulls, pushes = work_model(L.offset, L.nonzero)
+        r = {"graph": f"{kind} {g}", "nnz": L.nnz, "pulls": pulls, "pushes": pushes}
+        for mode, key in ((2, "wedge_ms"), (1, "hybrid_ms")):
+            bale.tune_set("tri.mode", mode)
+            r[key] = round(_time(lambda: bale.triangle_dev(off, col, cnt), reps=3), 4)
+        rows.append(r)
+        del off, col
+    bale.tune_set("tri.mode", -1)
+    bale.tune_set("tri.choose_min_nnz", -1)
+    torch.cuda.empty_cache()
+    pct, ppn = fit_tri_rule(rows)
+    return {"tri.wedge_pull_pct": pct, "tri.wedge_push_per_nnz": ppn}, rows
+
+
 def _batch_time(inst, reps: int) -> float:
     from .mix import as_batch
 
@@ -212,6 +288,7 @@ def main(argv=None) -> int:
     ap = argparse.ArgumentParser()
     ap.add_argument("--out", type=Path, default=DEFAULT_OUT)
     ap.add_argument("--quick", action="store_true", help="fewer sizes; skips the full-mix thresholds")
+    ap.add_argument("--only", choices=["ig", "histo", "tri", "batch"], help="tune one part, keep the file's others")
     a = ap.parse_args(argv)
     if not torch.cuda.is_available():
         print("autotune needs a CUDA device", file=sys.stderr)
@@ -221,7 +298,17 @@ def main(argv=None) -> int:
     t0 = time.time()
     report = {"gpu": torch.cuda.get_device_name(0)}
     knobs = {}
-    for part, fn in (("ig", tune_ig), ("histo", tune_histo), ("batch", tune_batch)):
+    if a.only and a.out.exists():  # keep the other parts' knobs and report
+        for line in a.out.read_text().splitlines():
+            f = line.split()
+            if len(f) == 2 and not line.startswith("#"):
+                knobs[f[0]] = int(f[1])
+        rep = a.out.with_name(a.out.stem + "_report.json")
+        if rep.exists():
+            report.update({k: v for k, v in json.loads(rep.read_text()).items() if k not in ("gpu", "seconds")})
+    for part, fn in (("ig", tune_ig), ("histo", tune_histo), ("tri", tune_tri), ("batch", tune_batch)):
+        if a.only and part != a.only:
+            continue
         k, rows = fn(a.quick)
         knobs.update(k)
         report[part] = {"chosen": k, "measurements": rows}

@@ -170,7 +170,15 @@ int g_tri_blocks_per_sm[2][64] = {{0}, {0}};
 // graphs without (Erdos-Renyi: pulls = pushes, 8-43 wedges per nonzero) by
 // the hybrid, 10-30% faster there.  The pushes are summed exactly over the
 // rows, the pulls estimated from kChooseSamples evenly spaced nonzeros; the
-// last block to finish writes choice[0] = 1 (wedge) or 0 (hybrid).
+// last block to finish writes choice[0] = 1 (wedge) or 0 (hybrid): wedges
+// when pulls >= pull_pct % of the pushes or the pushes reach push_per_nnz
+// per nonzero.  Both thresholds are tuning knobs that the autotuner fits to
+// measured wedge and hybrid times over R-MAT, Erdos-Renyi and Kronecker
+// graphs.  The built-in values are the fit on GB300: 192 % and no push
+// clause -- a product of stars with thousands of wedges per nonzero and
+// pulls a third of the pushes ({3,4,5,9,16,25}) took 372 ms by wedges and
+// 9.6 ms by the hybrid, R-MAT graphs (pulls 2.9-3.8x the pushes) are 2.3-3.2x
+// faster by wedges, Erdos-Renyi graphs (pulls = pushes) within 25% either way.
 // words: [0] pushes, [1] sampled pulls, [2] blocks done (zeroed by the caller).
 constexpr int kChooseSamples = 4096;
 constexpr int kChooseThreads = 256;
@@ -181,7 +189,8 @@ constexpr int64_t kChooseMinNnz = int64_t(1) << 23;
 
 __global__ void __launch_bounds__(kChooseThreads)
     tri_choose_kernel(const int64_t *__restrict__ off, const int64_t *__restrict__ col, int64_t n, int64_t nnz,
-                      unsigned long long *__restrict__ words, unsigned *__restrict__ choice) {
+                      double pull_ratio, double push_per_nnz, unsigned long long *__restrict__ words,
+                      unsigned *__restrict__ choice) {
   __shared__ unsigned last;
   unsigned long long pushes = 0, pulls = 0;
   const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
@@ -209,7 +218,7 @@ __global__ void __launch_bounds__(kChooseThreads)
   __threadfence();
   const double push = static_cast<double>(atomicAdd(&words[0], 0ull));
   const double pull = static_cast<double>(atomicAdd(&words[1], 0ull)) * static_cast<double>(nnz) / kChooseSamples;
-  const bool wedge = push == 0.0 || pull >= 1.5 * push || push >= 128.0 * static_cast<double>(nnz);
+  const bool wedge = push == 0.0 || pull >= pull_ratio * push || push >= push_per_nnz * static_cast<double>(nnz);
   *choice = wedge ? 1u : 0u;
 }
 
@@ -222,7 +231,7 @@ int launch_triangle(const int64_t *offset, const int64_t *nonzero, int64_t numro
   // by tri_choose_kernel; mode 2 the wedge path, mode 1 the hybrid, mode 0
   // this file's warp-per-row merge kernel for every row.
   const int64_t mode = knob("tri.mode");
-  if (mode < 0 && tri_wedge_supported(numrows, nnz) && nnz >= kChooseMinNnz) {
+  if (mode < 0 && tri_wedge_supported(numrows, nnz) && nnz >= knob_or("tri.choose_min_nnz", kChooseMinNnz)) {
     // both paths launched, the one not chosen returning at once; their
     // workspaces side by side
     const size_t wbytes = (tri_wedge_workspace_bytes(numrows, nnz) + 255) & ~size_t(255);
@@ -232,8 +241,11 @@ int launch_triangle(const int64_t *offset, const int64_t *nonzero, int64_t numro
     unsigned *choice = reinterpret_cast<unsigned *>(cw + 3);
     BALE_CUDA_OK(cudaMemsetAsync(cw, 0, 3 * sizeof(unsigned long long), stream));
     const int64_t want = (numrows + kChooseThreads - 1) / kChooseThreads, cap = static_cast<int64_t>(num_sms()) * 4;
+    const double pull_ratio = static_cast<double>(knob_or("tri.wedge_pull_pct", 192)) / 100.0;
+    const int64_t ppn = knob("tri.wedge_push_per_nnz");  // -1: no push clause
+    const double push_per_nnz = ppn < 0 ? 1e300 : static_cast<double>(ppn);
     tri_choose_kernel<<<static_cast<unsigned>(want < cap ? want : cap), kChooseThreads, 0, stream>>>(
-        offset, nonzero, numrows, nnz, cw, choice);
+        offset, nonzero, numrows, nnz, pull_ratio, push_per_nnz, cw, choice);
     BALE_CUDA_OK(cudaGetLastError());
     int rc = launch_triangle_wedge(offset, nonzero, numrows, nnz, count, work, bad, ws, cursor, stream, choice);
     if (rc != BALE_OK) return rc;

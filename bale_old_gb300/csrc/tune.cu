@@ -65,6 +65,9 @@ Knob g_knobs[] = {
     {"serve.express_streams", -1},  // express streams (2, at most 4)
     {"tri.mode", -1},           // 0 warp-per-row merge, 1 bitmap/search hybrid, 2 wedge probes; -1 per graph
     {"tri.wedge_stage_max", -1}, // wedge mode: rows above 2^16 with at most this many columns are binary-searched (64)
+    {"tri.wedge_pull_pct", -1},     // default mode: wedges when pulls >= this % of pushes (192)
+    {"tri.wedge_push_per_nnz", -1}, // ... or when pushes >= this many per nonzero (no such clause)
+    {"tri.choose_min_nnz", -1},     // the per-graph choice from this many nonzeros; wedges below (2^23)
 };
 std::mutex g_mu;
 }  // namespace

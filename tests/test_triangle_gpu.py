@@ -230,11 +230,13 @@ def test_prepared_graph_malformed_is_flagged(cuda, bale):
 
 
 # The default mode picks the path per graph on the device (from 2^23
-# nonzeros; below, the wedge path): wedges for graphs with hubs (R-MAT,
-# Kronecker products of stars), the hybrid for graphs without (Erdos-Renyi).
+# nonzeros; below, the wedge path): wedges for graphs with hubs (R-MAT: pulls
+# well above the pushes), the hybrid for graphs without (Erdos-Renyi) and for
+# products of stars, whose thousands of wedges per nonzero make the wedge
+# path far slower there.
 # The count is exact either way; the work tally shows which path ran (it
 # equals the forced mode's).
-@pytest.mark.parametrize("graph,want", [("rmat20", 2), ("er20", 1), ("er64", 1), ("kron", 2), ("er16", 2)])
+@pytest.mark.parametrize("graph,want", [("rmat20", 2), ("er20", 1), ("er64", 1), ("kron", 1), ("er16", 2)])
 def test_default_mode_choice(cuda, bale, graph, want):
     if graph.startswith("rmat"):
         L = bale.gen_rmat(int(graph[4:]), 16, 0.57, 0.19, 0.19, 6)
@@ -326,3 +328,26 @@ def test_alg1_full_size_rmat_scale22(cuda, bale, oracle):
     uo, uc = _transpose(oracle, L.offset, L.nonzero)
     cnt = bale.triangle_agi(L, bale.SparseMatrix(uo, uc, L.numrows), 1)[0]
     assert cnt == oracle.triangle_agi_mt(L.offset, L.nonzero)
+
+
+def test_strategy_thresholds_steer_the_choice(cuda, bale):
+    """The per-graph choice follows its tuned thresholds (the work-model rule
+    tri.wedge_pull_pct / tri.wedge_push_per_nnz from tri.choose_min_nnz on):
+    thresholds out of reach send an R-MAT graph to the hybrid, thresholds
+    at zero to the wedges; the work tally shows which path ran and the count
+    never changes."""
+    L = bale.gen_rmat(14, 16, 0.57, 0.19, 0.19, 21)
+    forced = {}
+    for m in (1, 2):
+        bale.tune_set("tri.mode", m)
+        forced[m] = bale.triangle_agi(L)[:2]
+    bale.tune_set("tri.mode", -1)
+    try:
+        bale.tune_set("tri.choose_min_nnz", 1)
+        for pct, ppn, want in ((1 << 30, 1 << 40, 1), (0, 1 << 40, 2), (1 << 30, 0, 2)):
+            bale.tune_set("tri.wedge_pull_pct", pct)
+            bale.tune_set("tri.wedge_push_per_nnz", ppn)
+            assert bale.triangle_agi(L)[:2] == forced[want], (pct, ppn)
+    finally:
+        for k in ("tri.choose_min_nnz", "tri.wedge_pull_pct", "tri.wedge_push_per_nnz"):
+            bale.tune_set(k, -1)

@@ -89,3 +89,31 @@ def test_load_of_a_missing_file(bale, knobs, tmp_path: Path):
     assert _lib.bale_tune_load(str(tmp_path / "absent.tune").encode()) == -1
     assert "cannot open" in bale._last_error()
     assert bale.tune_knobs() == knobs
+
+
+def test_tri_rule_fit_picks_the_faster_path():
+    """The intersection-strategy fit: graphs with hubs (pulls well above the
+    pushes) are faster by wedges, graphs without by the hybrid; the fitted
+    thresholds send each measured graph to its faster path."""
+    rows = [
+        {"graph": "rmat", "nnz": 100, "pulls": 400, "pushes": 100, "wedge_ms": 1.0, "hybrid_ms": 3.0},
+        {"graph": "rmat2", "nnz": 100, "pulls": 210, "pushes": 100, "wedge_ms": 1.0, "hybrid_ms": 2.0},
+        {"graph": "er", "nnz": 100, "pulls": 100, "pushes": 100, "wedge_ms": 1.2, "hybrid_ms": 1.0},
+        {"graph": "kron", "nnz": 10, "pulls": 30, "pushes": 3000, "wedge_ms": 0.5, "hybrid_ms": 0.7},
+    ]
+    pct, ppn = autotune.fit_tri_rule(rows)
+    for r in rows:
+        wedge = r["pulls"] * 100 >= pct * r["pushes"] or r["pushes"] >= ppn * r["nnz"]
+        assert wedge == (r["wedge_ms"] < r["hybrid_ms"]), (r, pct, ppn)
+
+
+def test_work_model_matches_the_oracle(oracle):
+    """pulls and pushes as the autotuner computes them equal the oracle's
+    restatement of the reference app's work model."""
+    import numpy as np
+
+    import bale_old_gb300 as bale
+
+    L = bale.gen_rmat(10, 16, 0.57, 0.19, 0.19, 3)
+    assert autotune.work_model(L.offset, L.nonzero) == oracle.triangle_work(L.offset, L.nonzero)
+    assert autotune.work_model(np.zeros(1, np.int64), np.zeros(0, np.int64)) == (0, 0)

@@ -22,6 +22,9 @@
 //    copy) on one of a few express streams, concurrently with the ticks;
 //  * when a request's last task has run, its result is copied back on a copy
 //    stream (ig values, the triangle count) and its arena space is freed.
+//    The express requests' uploads and downloads have copy streams of their
+//    own, so a small request's copies do not queue behind a large one's
+//    (they share the link, but a small copy finishes in microseconds).
 //
 // Latency is completion time minus arrival time.  Results are exactly the
 // per-instance entry points': ig overwrites the caller's out, triangles write
@@ -120,6 +123,9 @@ struct bale_server {
   int max_active = 64;
   int64_t reserve_bytes = int64_t(1) << 30;
   cudaStream_t s_compute = nullptr, s_up = nullptr, s_down = nullptr;
+  // the large (express) requests' index uploads and result downloads, so
+  // that a small request's copies never queue behind a gigabyte of them
+  cudaStream_t s_up_big = nullptr, s_down_big = nullptr;
   static constexpr int kExpress = 4;
   cudaStream_t s_express[kExpress] = {};
 };
@@ -161,6 +167,8 @@ void server_free(bale_server *s) {
   if (s->s_compute) cudaStreamDestroy(s->s_compute);
   if (s->s_up) cudaStreamDestroy(s->s_up);
   if (s->s_down) cudaStreamDestroy(s->s_down);
+  if (s->s_up_big) cudaStreamDestroy(s->s_up_big);
+  if (s->s_down_big) cudaStreamDestroy(s->s_down_big);
   for (auto st : s->s_express)
     if (st) cudaStreamDestroy(st);
   delete s;
@@ -219,6 +227,8 @@ bale_server_t *bale_server_create(int64_t arena_bytes, int max_active) {
   if (cudaStreamCreateWithFlags(&s->s_compute, cudaStreamNonBlocking) != cudaSuccess ||
       cudaStreamCreateWithFlags(&s->s_up, cudaStreamNonBlocking) != cudaSuccess ||
       cudaStreamCreateWithFlags(&s->s_down, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&s->s_up_big, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&s->s_down_big, cudaStreamNonBlocking) != cudaSuccess ||
       [&] {
         for (auto &st : s->s_express)
           if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) return true;
@@ -377,6 +387,11 @@ int bale_server_run(bale_server_t *s, const bale_request_t *req, int64_t nreq, d
   const int nlanes = static_cast<int>(
       std::min<int64_t>(bale_server::kExpress, std::max<int64_t>(1, knob_or("serve.express_streams", 2))));
   const int rows_per_fetch = static_cast<int>(knob_or("tri.rows_per_fetch", 8));
+  // serve.copy_lanes 1: every copy on one upload and one download stream;
+  // 2 (default): the express requests' copies on streams of their own
+  const bool split_copies = knob_or("serve.copy_lanes", 2) != 1;
+  cudaStream_t up_big = split_copies ? s->s_up_big : s->s_up;
+  cudaStream_t down_big = split_copies ? s->s_down_big : s->s_down;
   double lane_load[bale_server::kExpress] = {0, 0, 0, 0};
 #define SRV_CUDA(expr)                                                                 \
   do {                                                                                 \
@@ -490,9 +505,10 @@ int bale_server_run(bale_server_t *s, const bale_request_t *req, int64_t nreq, d
           inst.out = reinterpret_cast<int64_t *>(d_tri + id);
         }
         if (x.kind != BALE_KIND_TRIANGLES && x.n)
-          SRV_CUDA(cudaMemcpyAsync(buf, x.index, 8 * static_cast<size_t>(x.n), cudaMemcpyHostToDevice, s->s_up));
+          SRV_CUDA(cudaMemcpyAsync(buf, x.index, 8 * static_cast<size_t>(x.n), cudaMemcpyHostToDevice,
+                                   express ? up_big : s->s_up));
         if (express) {
-          SRV_CUDA(cudaEventRecord(a->uploaded, s->s_up));
+          SRV_CUDA(cudaEventRecord(a->uploaded, up_big));
           // the least loaded express stream runs it once its index is on the device
           int lane = 0;
           for (int l = 1; l < nlanes; l++)
@@ -565,12 +581,13 @@ int bale_server_run(bale_server_t *s, const bale_request_t *req, int64_t nreq, d
         Active *a = ap.get();
         if (a->downloading || (a->express ? !a->computed : a->finished < a->tasks.size())) continue;
         const bale_request_t &x = req[a->id];
+        cudaStream_t down = a->express && x.kind == BALE_KIND_IG ? down_big : s->s_down;
         if (x.kind == BALE_KIND_IG && x.n)
           SRV_CUDA(cudaMemcpyAsync(x.out, a->buf + 8 * x.n, 8 * static_cast<size_t>(x.n), cudaMemcpyDeviceToHost,
-                                   s->s_down));
+                                   down));
         else if (x.kind == BALE_KIND_TRIANGLES)
-          SRV_CUDA(cudaMemcpyAsync(x.out, d_tri + a->id, 8, cudaMemcpyDeviceToHost, s->s_down));
-        SRV_CUDA(cudaEventRecord(a->downloaded, s->s_down));
+          SRV_CUDA(cudaMemcpyAsync(x.out, d_tri + a->id, 8, cudaMemcpyDeviceToHost, down));
+        SRV_CUDA(cudaEventRecord(a->downloaded, down));
         a->downloading = true;
         progressed = true;
       }

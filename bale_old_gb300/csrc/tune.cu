@@ -63,6 +63,7 @@ Knob g_knobs[] = {
     {"serve.reserve_bytes", -1},  // free HBM a registration must leave (1 GiB)
     {"serve.express", -1},          // 0: every request goes through the queue kernel
     {"serve.express_streams", -1},  // express streams (2, at most 4)
+    {"serve.copy_lanes", -1},       // 1: all copies on one upload and one download stream; 2: express ones apart
     {"tri.mode", -1},           // 0 warp-per-row merge, 1 bitmap/search hybrid, 2 wedge probes; -1 per graph
     {"tri.wedge_stage_max", -1}, // wedge mode: rows above 2^16 with at most this many columns are binary-searched (64)
     {"tri.wedge_pull_pct", -1},     // default mode: wedges when pulls >= this % of pushes (192)

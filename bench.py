@@ -856,15 +856,22 @@ def run_serve(ctx) -> dict:
     s.run(trace(np.zeros(nreq)))  # warm-up
     _, cap = s.run(trace(np.zeros(nreq)))
     cap_rate = nreq / cap["makespan_s"]
+    # each offered rate on three Poisson traces (arrival seeds): the median
+    # and the spread (min, max) of p50 / p99 / throughput
     rates = []
     for frac in (0.25, 0.5, 0.75, 1.0, 1.5):
-        lat, st = s.run(trace(sv.poisson_arrivals(nreq, frac * cap_rate, 17)))
-        rates.append({"offered_requests_per_s": round(frac * cap_rate, 2), "load": frac,
-                      "p50_ms": round(st["p50_s"] * 1e3, 3), "p99_ms": round(st["p99_s"] * 1e3, 3),
-                      "mean_ms": round(st["mean_s"] * 1e3, 3), "items_per_s": round(st["items_per_s"], 1),
-                      "makespan_s": round(st["makespan_s"], 4), "ticks": st["ticks"],
-                      "max_active": st["max_active"], "admission_waits": st["admission_waits"],
-                      "express_requests": st["express"]})
+        runs = [s.run(trace(sv.poisson_arrivals(nreq, frac * cap_rate, seed)))[1] for seed in (17, 18, 19)]
+
+        def med(key, scale=1.0):
+            v = sorted(r[key] * scale for r in runs)
+            return {"median": round(v[1], 3), "min": round(v[0], 3), "max": round(v[2], 3)}
+
+        rates.append({"offered_requests_per_s": round(frac * cap_rate, 2), "load": frac, "traces": len(runs),
+                      "p50_ms": med("p50_s", 1e3), "p99_ms": med("p99_s", 1e3), "mean_ms": med("mean_s", 1e3),
+                      "G_items_per_s": med("items_per_s", 1e-9),
+                      "ticks": [r["ticks"] for r in runs], "max_active": [r["max_active"] for r in runs],
+                      "admission_waits": [r["admission_waits"] for r in runs],
+                      "express_requests": runs[0]["express"]})
     # exactness of the last run: triangle counts and a sample of ig values
     ok = True
     tri_want = {}
@@ -1038,6 +1045,8 @@ def summarize(r: dict) -> dict:
             out[k] = r[k]
     if "saturation" in r:
         out["p50_ms"], out["p99_ms"] = r["saturation"]["p50_ms"], r["saturation"]["p99_ms"]
+    if "rates" in r:
+        out["p50_ms_by_load"] = {str(x["load"]): x["p50_ms"]["median"] for x in r["rates"]}
     if "erdos_renyi" in r:
         er = r["erdos_renyi"]
         out["er"] = {"value": er["default"]["value"], "parity": er.get("parity_ok")}

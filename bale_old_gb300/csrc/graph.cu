@@ -205,7 +205,7 @@ int build_from_keys(Ws &w, int64_t m, int64_t n, int S, int64_t *d_offset, int64
   rc = csr_from_keys(ls, nu, n, S, d_offset, d_nonzero, st);
   if (rc != BALE_OK) return rc;
   BALE_CUDA_OK(cudaGetLastError());
-  BALE_CUDA_OK(cudaStreamSynchronize(st));
+  if ((rc = sort_status(w.words, st, "graph build")) != BALE_OK) return rc;
   *nnz = nu;
   return BALE_OK;
 }

@@ -342,8 +342,9 @@ struct DartWs {
   uint32_t *owner, *target, *pos;           // per slot
   uint32_t *bits, *pc, *wpre;               // hit bits per throw, popcounts and their prefix per word
   uint32_t *hist, *hoff, *bsum, *rstart;    // radix pass, scans, rounds
+  uint32_t *osw;                            // radix pass: digit starts and tile counter
   unsigned int *words;  // [0] scan total, [1] k*, [2] last throw, [3] rounds, [4] rounds status, [5] lost chains,
-                        // [6] the throw of rand_permp_agi's n-th hit
+                        // [6] the throw of rand_permp_agi's n-th hit, [kSortErrWord] a radix wait gave up
 };
 
 size_t dart_ws(int64_t m, int64_t nkeys, int64_t nbits, DartWs *w, char *base) {
@@ -370,6 +371,7 @@ size_t dart_ws(int64_t m, int64_t nkeys, int64_t nbits, DartWs *w, char *base) {
   p = take(4 * tiles * kDigits); if (w) w->hoff = reinterpret_cast<uint32_t *>(p);
   p = take(4 * nb); if (w) w->bsum = reinterpret_cast<uint32_t *>(p);
   p = take(4 * (kDartRoundsMax + 1)); if (w) w->rstart = reinterpret_cast<uint32_t *>(p);
+  p = take(4 * kOsWords); if (w) w->osw = reinterpret_cast<uint32_t *>(p);
   p = take(64); if (w) w->words = reinterpret_cast<unsigned int *>(p);
   return o;
 }
@@ -394,6 +396,7 @@ uint64_t *dart_region_keys(uint64_t x0, int64_t t_begin, int64_t t_end, int64_t 
   rw.hist = w.hist;
   rw.hoff = w.hoff;
   rw.bsum = w.bsum;
+  rw.osw = w.osw;
   rw.words = w.words;
   *rc = radix_pass(w.ka, w.kb, nk, tb + kDartRegionBits, rw, st);  // the region is the 8 bits from there
   return *rc == BALE_OK ? w.kb : w.ka;
@@ -478,7 +481,8 @@ int rand_perm_darts(int64_t n, uint64_t x0, int64_t per_round, int64_t *d_perm, 
     if ((rc = excl_scan(w.owner, w.pos, m, w.bsum, w.words, st)) != BALE_OK) return rc;
     dart_perm_kernel<<<grid_for(m), 256, 0, st>>>(w.target, w.pos, m, n, d_perm);
     BALE_CUDA_OK(cudaGetLastError());
-    if ((rc = read_words(w.words, h, 7, st)) != BALE_OK) return rc;
+    if ((rc = read_words(w.words, h, 7, st)) != BALE_OK || (rc = sort_status(w.words, st, who)) != BALE_OK)
+      return rc;
     if (static_cast<int64_t>(h[0]) != n || h[5] != 0) {
       set_error("%s: %u darts placed of %lld (%u lost)", who, h[0], static_cast<long long>(n), h[5]);
       return BALE_EINVAL;

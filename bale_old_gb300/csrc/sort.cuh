@@ -15,13 +15,20 @@ constexpr int kDigits = 1 << kDigitBits;
 constexpr int kScanThreads = 1024;
 constexpr int64_t kScanBlock = kScanThreads * 4;    // elements per scan block
 
+constexpr int kOsPasses = 8;                                // digit passes of a 64-bit key
+constexpr int kOsWords = kOsPasses * kDigits + kOsPasses;  // per pass: digit starts; then its tile counter
+// words[kSortErrWord] is set when a sort pass's bounded wait gave up.  Every
+// caller zeroes words before its first sort and reads it with sort_status.
+constexpr int kSortErrWord = 15;
+
 // Workspace of one graph build: two key buffers (m), flags and positions
-// (m + 1), the sort histogram and its scan, degrees, labels, vertex keys (n
-// each).  The sort and the scan use hist, hoff, bsum and words only.
+// (m + 1), the sort's per-tile words and their scan, degrees, labels, vertex
+// keys (n each).  The sort and the scan use hist, hoff, bsum, osw and words only.
 struct Ws {
   uint64_t *ka, *kb, *va, *vb;
   uint32_t *flag, *pos, *hist, *hoff, *bsum, *deg, *newid;
-  unsigned int *words;  // [0] scan total, [1] max degree
+  uint32_t *osw;        // kOsWords: the single-sweep sort's digit starts and tile counters
+  unsigned int *words;  // [0] scan total, [1] max degree, [kSortErrWord] a sort wait gave up
 };
 
 size_t up256(size_t x);
@@ -33,6 +40,9 @@ size_t ws_bytes(int64_t m, int64_t n, Ws *w, char *base);
 int excl_scan(const uint32_t *in, uint32_t *out, int64_t n, uint32_t *bsum, unsigned int *total, cudaStream_t st);
 // One stable pass over the 8 bits from `shift`: a into b.
 int radix_pass(const uint64_t *a, uint64_t *b, int64_t n, int shift, Ws &w, cudaStream_t st);
+// BALE_ETIMEDOUT (with the error text naming `who`) when a sort since words
+// was zeroed gave up a wait, else BALE_OK; synchronises st.
+int sort_status(const unsigned int *words, cudaStream_t st, const char *who);
 // Bits for labels [0, n): the least S with 2^S >= n (at least 1).
 int label_bits(int64_t n);
 // A CSR read off keys sorted by row: key = row << S | column (low S bits).

@@ -173,8 +173,7 @@ int bale_transpose_dev(const int64_t *d_offset, const int64_t *d_nonzero, int64_
   rc = csr_from_keys(sk, nnz, numcols, rb, d_toffset, d_tnonzero, st);
   if (rc != BALE_OK) return rc;
   BALE_CUDA_OK(cudaGetLastError());
-  BALE_CUDA_OK(cudaStreamSynchronize(st));
-  return BALE_OK;
+  return sort_status(w.words, st, "bale_transpose_dev");
 }
 
 int bale_permute_dev(const int64_t *d_offset, const int64_t *d_nonzero, int64_t numrows, int64_t numcols,

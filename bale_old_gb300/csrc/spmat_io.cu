@@ -296,7 +296,7 @@ int bale_read_matrix_mm_dev(const char *path, int64_t *d_offset, int64_t *d_nonz
   const int64_t tiles = (nn + kTile - 1) / kTile;
   const int64_t nb = (std::max(ll + 1, tiles * kDigits) + kScanBlock - 1) / kScanBlock + 1;
   const size_t need = up256(ll) + 2 * up256(4 * (ll + 1)) + 2 * up256(4 * nn) + 2 * up256(8 * nn) +
-                      2 * up256(4 * tiles * kDigits) + up256(4 * nb) + 256;
+                      2 * up256(4 * tiles * kDigits) + up256(4 * nb) + up256(4 * kOsWords) + 256;
   char *ws = static_cast<char *>(device_workspace(need, st));
   if (!ws) return BALE_ENOMEM;
   char *o = ws;
@@ -316,6 +316,7 @@ int bale_read_matrix_mm_dev(const char *path, int64_t *d_offset, int64_t *d_nonz
   w.hist = reinterpret_cast<uint32_t *>(take(4 * tiles * kDigits));
   w.hoff = reinterpret_cast<uint32_t *>(take(4 * tiles * kDigits));
   w.bsum = reinterpret_cast<uint32_t *>(take(4 * nb));
+  w.osw = reinterpret_cast<uint32_t *>(take(4 * kOsWords));
   w.words = reinterpret_cast<unsigned int *>(take(64));
   w.va = w.vb = nullptr;
   w.deg = w.newid = nullptr;
@@ -362,8 +363,7 @@ int bale_read_matrix_mm_dev(const char *path, int64_t *d_offset, int64_t *d_nonz
   if ((rc = csr_from_keys(sk, nnz, nr, lb, d_offset, nullptr, st)) != BALE_OK) return rc;
   if (nnz > 0) mm_cols_kernel<<<grid_for(nnz), 256, 0, st>>>(sk, nnz, lb, cols, d_nonzero);
   BALE_CUDA_OK(cudaGetLastError());
-  BALE_CUDA_OK(cudaStreamSynchronize(st));
-  return BALE_OK;
+  return sort_status(w.words, st, "bale_read_matrix_mm_dev");
 }
 
 int bale_write_sparse_matrix_dev(const char *dirname, const int64_t *d_offset, const int64_t *d_nonzero,

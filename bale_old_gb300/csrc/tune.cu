@@ -64,6 +64,9 @@ Knob g_knobs[] = {
     {"serve.express", -1},          // 0: every request goes through the queue kernel
     {"serve.express_streams", -1},  // express streams (2, at most 4)
     {"serve.copy_lanes", -1},       // 1: all copies on one upload and one download stream; 2: express ones apart
+    {"sort.onesweep", -1},        // 0: every radix pass as histogram + scan + scatter (1: single sweep below 2^30 keys)
+    {"sort.lookback_spins", -1},  // reads without progress before a sort pass's look-back gives up (2^22)
+    {"sort.test_withhold", -1},   // 1: tile 0 of each sort pass publishes nothing (tests the bounded wait)
     {"tri.mode", -1},           // 0 warp-per-row merge, 1 bitmap/search hybrid, 2 wedge probes; -1 per graph
     {"tri.wedge_stage_max", -1}, // wedge mode: rows above 2^16 with at most this many columns are binary-searched (64)
     {"tri.wedge_pull_pct", -1},     // default mode: wedges when pulls >= this % of pushes (192)

@@ -233,12 +233,13 @@ __global__ void __launch_bounds__(kThreads, 4)
     const bool valid = i < n;
     key[r] = valid ? src[i] : 0ull;
     const uint32_t d = valid ? static_cast<uint32_t>(key[r] >> shift) & (kDigits - 1) : kDigits;
+    // the lowest lane of each digit adds the digit's keys to the warp's count
+    // and hands the count before them to the others
     const unsigned peers = __match_any_sync(kFull, d);
     const uint32_t below = __popc(peers & ((1u << lane) - 1u));
-    const uint32_t prior = valid ? wcnt[warp][d] : 0u;
-    __syncwarp();
-    if (valid && below == 0) wcnt[warp][d] = prior + __popc(peers);
-    __syncwarp();
+    uint32_t prior = 0;
+    if (valid && below == 0) prior = atomicAdd(&wcnt[warp][d], __popc(peers));
+    prior = __shfl_sync(kFull, prior, __ffs(peers) - 1);
     dr[r] = d << 16 | (prior + below);
   }
   __syncthreads();

@@ -510,18 +510,22 @@ def run_graph(ctx) -> dict:
     offs_h, col_h = off.cpu().numpy(), col.cpu().numpy()
     maxdeg = int((np.diff(offs_h) + np.bincount(col_h, minlength=1 << S)).max())
     p_edges, p_vert, p_lower = (2 * S + 1 + 7) // 8, (S + maxdeg.bit_length() + 7) // 8, (2 * S + 7) // 8
-    # the dominant work: three LSD radix sorts, each 8-bit pass reading every
-    # 8-byte key twice (histogram, scatter) and writing it once
-    algo = 24 * (p_edges * m + p_vert * (1 << S) + p_lower * nnz)
-    launches = 1 + 5 * p_edges + 1 + 3 + 1 + 1 + 1 + 5 * p_vert + 1 + 1 + 5 * p_lower + 2
+    # the dominant work: three LSD radix sorts, each reading its 8-byte keys
+    # once for the digit counts of all passes, then every 8-bit pass reading
+    # and writing each key once
+    algo = 16 * (p_edges * m + p_vert * (1 << S) + p_lower * nnz) + 8 * (m + (1 << S) + nnz)
+    # edge keys, per sort the digit counts + starts + one kernel per pass,
+    # dedup (flag, 3 scan kernels, compact), max, vertex keys, labels, lower keys, CSR
+    launches = 1 + (2 + p_edges) + 1 + 3 + 1 + 1 + 1 + (2 + p_vert) + 1 + 1 + (2 + p_lower) + 2
     out = {"metric": "G input edges/s building the degree-ordered lower CSR (R-MAT scale 22) on the device",
            "value": round(job_rate(m, ms_max / 1e3, ctx["dist"].world) / 1e9, 4), "unit": "G edges/s",
            "ms_per_step": round(ms_max, 3), "nnz": nnz,
            "roofline": roofline(ctx, "graph", algo, ms / 1e3,
-                                "the build's radix sorts (hist + scatter per 8-bit pass) and graph steps",
-                                note="algorithmic bytes: 24 B per key per 8-bit pass over the m edge keys "
-                                     "(45 bits), the 2^22 vertex keys and the nnz lower keys (44 bits); the "
-                                     "generation, dedup and CSR steps are not counted"),
+                                "the build's radix sorts (one digit count per sort, one look-back scatter "
+                                "per 8-bit pass) and graph steps",
+                                note="algorithmic bytes: 16 B per key per 8-bit pass plus 8 B per key per sort "
+                                     "over the m edge keys (45 bits), the 2^22 vertex keys and the nnz lower keys "
+                                     "(44 bits); the generation, dedup and CSR steps are not counted"),
            "clocks": clocks.summary(), "gpu_launches": launches * args.steps,
            "config": {"workload": "R-MAT scale 22, edge factor 16, (0.57,0.19,0.19,0.05): 67,108,864 generated "
                                   "edges -> symmetrised, deduplicated, degree-ordered strictly lower CSR",
@@ -603,14 +607,14 @@ def run_spmat(ctx) -> dict:
                        "write_GB_s": round(ds_bytes / dw_s / 1e9, 3), "read_GB_s": round(ds_bytes / dr_s / 1e9, 3),
                        "how": "bale_write_sparse_matrix_dev / bale_read_sparse_matrix_dev of the scale-22 lower "
                               "matrix, one writer (files in the page cache)"},
-           # transpose: the sort's passes dominate -- 24 B per key per 8-bit pass
-           "roofline": roofline(ctx, "spmat", 24 * ((2 * S + 7) // 8) * nnz, t_ms / 1e3,
+           # transpose: the sort dominates -- 8 B per key for its digit counts, 16 B per key per 8-bit pass
+           "roofline": roofline(ctx, "spmat", (16 * ((2 * S + 7) // 8) + 8) * nnz, t_ms / 1e3,
                                 "transpose: radix sort of (column, row) keys",
-                                note="algorithmic bytes: 24 B per key per 8-bit pass (44-bit keys); the "
-                                     "check, key and CSR kernels are not counted"),
-           # a transpose step: the CSR check, the key pass, ceil(44/8) = 6 radix passes of histogram + 3 scan
-           # kernels + scatter, then the CSR offsets and columns
-           "clocks": clocks.summary(), "gpu_launches": (2 + 6 * 5 + 2) * args.steps,
+                                note="algorithmic bytes: 16 B per key per 8-bit pass (44-bit keys) plus 8 B per "
+                                     "key for the digit counts; the check, key and CSR kernels are not counted"),
+           # a transpose step: the CSR check, the key pass, the sort's digit counts and starts, ceil(44/8) = 6
+           # look-back scatter passes, then the CSR offsets and columns
+           "clocks": clocks.summary(), "gpu_launches": (2 + 2 + 6 + 2) * args.steps,
            "config": {"workload": "transpose_matrix / permute_matrix of the R-MAT scale-22 degree-ordered lower "
                                   "matrix (n = 2^22, 64,155,075 nonzeros); rand_permp_agi and rand_permp of 2^26 "
                                   "elements",

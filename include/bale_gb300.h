@@ -186,6 +186,10 @@ BALE_API void bale_triangle_release(bale_tri_prepared_t *g);
 /* :1055-1062 sort_nonzeros).  d_offset[n+1]; d_nonzero needs room for m    */
 /* entries; *nnz receives the count.  Synchronous; BALE_EINPUT if an        */
 /* endpoint is outside [0,n).  n <= 2^31, m < 2^32 - 1.  New entry points.   */
+/* These, the transpose, the random permutations and the MatrixMarket       */
+/* reader sort with a radix sort whose passes wait, bounded, on earlier     */
+/* tiles: BALE_ETIMEDOUT if a wait gave up (the output is still exact; the  */
+/* limit is the knob sort.lookback_spins).                                  */
 BALE_API int bale_graph_build_dev(const int64_t *d_u, const int64_t *d_v, int64_t m, int64_t n,
                                   int64_t *d_offset, int64_t *d_nonzero, int64_t *nnz, void *stream);
 /* Device scratch a build of m edges on n vertices takes (bytes). */

@@ -313,7 +313,12 @@ def run_ig(ctx, zipf: bool) -> dict:
                                     "4.83 GB per call needs >= 14.1 ms"}
         if ctx["cpu"]:
             sample = np.ascontiguousarray(index_h[: 1 << 25])
-            ctx["later"].append(lambda: out.__setitem__("cpu_baseline", cpu_ig(sample, table_h, ctx["budget"])))
+
+            def cpu_leg():
+                out["cpu_baseline"] = cpu_ig(sample, table_h, ctx["budget"])
+                out["cpu_baseline"]["one_pe"] = one_pe_legs("ig", 2.0, index=sample[: 1 << 23], table=table_h)
+
+            ctx["later"].append(cpu_leg)
     return out
 
 
@@ -380,7 +385,11 @@ def run_histo(ctx) -> dict:
                   "d2h_bytes_per_step": 8 * HISTO_COUNTS, "path": "histo_agi C ABI, pinned host buffers",
                   "parity_ok": bool(np.array_equal(pin_cnt.numpy(), calls * want)), "per_call": e2e_spread}
     if ctx["cpu"]:
-        ctx["later"].append(lambda: out.__setitem__("cpu_baseline", cpu_histo(index_h, ctx["budget"])))
+        def cpu_leg():
+            out["cpu_baseline"] = cpu_histo(index_h, ctx["budget"])
+            out["cpu_baseline"]["one_pe"] = one_pe_legs("histo", 2.0, index=index_h)
+
+        ctx["later"].append(cpu_leg)
     return out
 
 
@@ -482,6 +491,8 @@ def run_triangles(ctx) -> dict:
         def cpu_leg():
             out["cpu_baseline"] = cpu_triangles(L, ctx["budget"])
             out["parity_ok"] = out["cpu_baseline"].get("triangles") == per_step == res["r"][0]
+            out["cpu_baseline"]["one_pe"] = one_pe_legs("triangles", 0, offset=L.offset, nonzero=L.nonzero,
+                                                         row_step=256)
 
         ctx["later"].append(cpu_leg)
     return out
@@ -1012,6 +1023,52 @@ def cpu_histo(index_h, budget_s: float) -> dict:
     return {"value": round(reps * index_h.size / secs / 1e9, 5), "unit": "GUP/s", "cores": cores, "kind": "port",
             "sample": f"{reps} x all 10^7 updates (histo_agi loop, apps/histo_src/histo_agi.upc:61-66, "
                       "relaxed atomic adds, one pthread per core)"}
+
+
+def _reps(fn, budget_s: float) -> tuple[int, float]:
+    reps, t0 = 0, time.perf_counter()
+    while True:
+        fn()
+        reps += 1
+        if time.perf_counter() - t0 >= budget_s:
+            return reps, time.perf_counter() - t0
+
+
+def one_pe_legs(kind: str, budget_s: float, **a) -> dict:
+    """The AGI loop and the exstack variant (its buffers of 1024 packages,
+    exchange and pops modelled at one PE) on one host thread: the reference's
+    single-PE runs, restated, on a bounded sample."""
+    orc = _oracle()
+    if kind == "ig":
+        idx, table = a["index"], a["table"]
+        pck = (idx << 16).astype(np.int64)
+        ra, sa = _reps(lambda: orc.ig_agi(idx, table), budget_s)
+        rx, sx = _reps(lambda: orc.ig_exstack_buffered(pck, table, 1024), budget_s)
+        n, unit = idx.size, "GUP/s"
+        sample = f"the first {idx.size} requests against the full table (ig_agi, ig_exstack)"
+    elif kind == "histo":
+        idx = a["index"]
+        pck = (idx << 16).astype(np.int64)
+        counts = np.zeros(HISTO_COUNTS, np.int64)
+        ra, sa = _reps(lambda: orc.histo_agi(idx, counts), budget_s)
+        rx, sx = _reps(lambda: orc.histo_exstack_buffered(pck, counts, 1024), budget_s)
+        n, unit = idx.size, "GUP/s"
+        sample = "all 10^7 updates (histo_agi, histo_exstack)"
+    else:
+        off, col, step = a["offset"], a["nonzero"], a["row_step"]
+        rows = np.arange(0, off.size - 1, step)
+        n, unit = int((off[rows + 1] - off[rows]).sum()), "G edges/s"
+        t0 = time.perf_counter()
+        ca = orc.triangle_agi_sampled(off, col, 0, step)
+        ra, sa = 1, time.perf_counter() - t0
+        t0 = time.perf_counter()
+        cx, _ = orc.triangle_exstack_push_buffered(off, col, 1024, 0, step)
+        rx, sx = 1, time.perf_counter() - t0
+        sample = f"rows 0, {step}, {2 * step}, ... ({n} nonzeros; triangle_agi alg 0, triangle_exstack_push)"
+        if ca != cx:
+            return {"error": f"sampled counts differ: {ca} against {cx}"}
+    return {"cores": 1, "kind": "port", "unit": unit, "sample": sample,
+            "agi": round(ra * n / sa / 1e9, 6), "exstack": round(rx * n / sx / 1e9, 6)}
 
 
 def cpu_triangles(L, budget_s: float) -> dict:

@@ -31,6 +31,179 @@ void orc_histo_exstack(const int64_t *pckindx, int64_t n, int64_t *lcounts) {
   for (int64_t i = 0; i < n; i++) lcounts[pckindx[i] >> 16]++;
 }
 
+/* A one-PE exstack (exstack/exstack.upc:163-340 at THREADS == 1): a send
+ * buffer of cap packages headed by its 64-bit count, an exchange that copies
+ * the used part into the receive buffer (lgp_memput to itself) and clears the
+ * send count, and FIFO pops from the receive buffer.  It keeps the reference's
+ * data movement -- every package copied into a buffer, across and out again
+ * -- so the buffered variants below time the exstack machinery at one PE. */
+typedef struct {
+  int64_t cap, pkg;
+  char *snd, *rcv, *push, *fifo;
+} orc_ex1_t;
+
+static int ex1_init(orc_ex1_t *x, int64_t cap, int64_t pkg) {
+  x->cap = cap;
+  x->pkg = pkg;
+  x->snd = malloc((size_t)(8 + cap * pkg));
+  x->rcv = malloc((size_t)(8 + cap * pkg));
+  if (!x->snd || !x->rcv) {
+    free(x->snd);
+    free(x->rcv);
+    return -1;
+  }
+  *(uint64_t *)x->snd = 0;
+  *(uint64_t *)x->rcv = 0;
+  x->push = x->snd + 8;
+  x->fifo = x->rcv + 8;
+  return 0;
+}
+
+static void ex1_free(orc_ex1_t *x) {
+  free(x->snd);
+  free(x->rcv);
+}
+
+/* exstack_push (:163-175): 0 when the buffer is full. */
+static int ex1_push(orc_ex1_t *x, const void *item) {
+  uint64_t *ct = (uint64_t *)x->snd;
+  if ((int64_t)*ct >= x->cap) return 0;
+  memcpy(x->push, item, (size_t)x->pkg);
+  x->push += x->pkg;
+  (*ct)++;
+  return 1;
+}
+
+/* exstack_exchange (:185-220). */
+static void ex1_exchange(orc_ex1_t *x) {
+  uint64_t ct = *(uint64_t *)x->snd;
+  if (ct) memcpy(x->rcv, x->snd, (size_t)(8 + (int64_t)ct * x->pkg));
+  else *(uint64_t *)x->rcv = 0;
+  *(uint64_t *)x->snd = 0;
+  x->push = x->snd + 8;
+  x->fifo = x->rcv + 8;
+}
+
+/* exstack_pop / exstack_pop_thread (:231-288): 0 when the receive buffer is empty. */
+static int ex1_pop(orc_ex1_t *x, void *item) {
+  uint64_t *ct = (uint64_t *)x->rcv;
+  if (*ct == 0) return 0;
+  memcpy(item, x->fifo, (size_t)x->pkg);
+  x->fifo += x->pkg;
+  (*ct)--;
+  return 1;
+}
+
+/* apps/histo_src/histo_exstack.upc:52-86 with buf_cnt-package buffers: push
+ * col = pckindx[i] >> 16 to PE pckindx[i] & 0xffff (0) until the buffer is
+ * full, exchange, pull and count; exstack_proceed (exstack.upc:129-152) ends
+ * the loop once every index has been pushed.  -1 if the buffers cannot be had. */
+int orc_histo_exstack_buffered(const int64_t *pckindx, int64_t n, int64_t *lcounts, int64_t buf_cnt) {
+  orc_ex1_t x;
+  if (buf_cnt < 1 || ex1_init(&x, buf_cnt, 8) != 0) return -1;
+  int64_t i = 0, col;
+  while (i < n) {  /* exstack_proceed(ex, i == T) at one PE */
+    for (; i < n; i++) {
+      col = pckindx[i] >> 16;
+      if (!ex1_push(&x, &col)) break;
+    }
+    ex1_exchange(&x);
+    while (ex1_pop(&x, &col)) lcounts[col]++;
+  }
+  ex1_free(&x);
+  return 0;
+}
+
+/* apps/ig_src/ig_exstack.upc:54-102 with buf_cnt-package buffers: push the
+ * requests' local indices, exchange, answer each popped request with
+ * ltable[idx] pushed back, exchange, and retrace the round's requests in
+ * order from the replies. */
+int orc_ig_exstack_buffered(int64_t *tgt, const int64_t *pckindx, int64_t n, const int64_t *ltable,
+                            int64_t buf_cnt) {
+  orc_ex1_t x;
+  if (buf_cnt < 1 || ex1_init(&x, buf_cnt, 8) != 0) return -1;
+  int64_t i = 0, idx;
+  while (i < n) {  /* exstack_proceed(ex, i == l_num_req) at one PE */
+    const int64_t i0 = i;
+    for (; i < n; i++) {
+      idx = pckindx[i] >> 16;
+      if (!ex1_push(&x, &idx)) break;
+    }
+    ex1_exchange(&x);
+    while (ex1_pop(&x, &idx)) {
+      idx = ltable[idx];
+      ex1_push(&x, &idx);  /* as many replies as requests: room is certain */
+    }
+    ex1_exchange(&x);
+    for (int64_t j = i0; j < i; j++) {
+      ex1_pop(&x, &idx);
+      tgt[j] = idx;
+    }
+  }
+  ex1_free(&x);
+  return 0;
+}
+
+/* apps/triangle_src/triangle_exstack.upc:95-168 (alg 0) with bufsiz-package
+ * buffers of the reference's {int32 w, int32 vj} packages: for each nonzero
+ * (i,j), push every w of row i before j to row j's owner; when the buffer is
+ * full, exchange and let the owner scan row j for each popped w (:61-82),
+ * then retry the push.  Rows i = row0, row0 + row_step, ... only (a bounded
+ * sample when row_step > 1).  Returns the count, or -1 without buffers;
+ * *pushed gets the packages pushed. */
+int64_t orc_triangle_exstack_push_buffered(const int64_t *offset, const int64_t *nonzero, int64_t numrows,
+                                           int64_t bufsiz, int64_t row0, int64_t row_step, int64_t *pushed) {
+  typedef struct {
+    int32_t w, vj;
+  } pkg_t;
+  orc_ex1_t x;
+  if (bufsiz < 1 || row_step < 1 || ex1_init(&x, bufsiz, (int64_t)sizeof(pkg_t)) != 0) return -1;
+  int64_t cnt = 0, np = 0;
+  pkg_t pkg;
+  for (int64_t i = row0; i < numrows; i += row_step) {
+    for (int64_t k = offset[i]; k < offset[i + 1]; k++) {
+      const int64_t j = nonzero[k];
+      pkg.vj = (int32_t)j;
+      for (int64_t kk = offset[i]; kk < offset[i + 1]; kk++) {
+        pkg.w = (int32_t)nonzero[kk];
+        if (pkg.w == j) break;
+        np++;
+        while (!ex1_push(&x, &pkg)) {  /* full: exchange, process, push again */
+          ex1_exchange(&x);
+          pkg_t q;
+          while (ex1_pop(&x, &q))
+            for (int64_t t = offset[q.vj]; t < offset[q.vj + 1]; t++) {
+              if (q.w == nonzero[t]) { cnt++; break; }
+              if (q.w < nonzero[t]) break;
+            }
+        }
+      }
+    }
+  }
+  ex1_exchange(&x);
+  pkg_t q;
+  while (ex1_pop(&x, &q))
+    for (int64_t t = offset[q.vj]; t < offset[q.vj + 1]; t++) {
+      if (q.w == nonzero[t]) { cnt++; break; }
+      if (q.w < nonzero[t]) break;
+    }
+  ex1_free(&x);
+  if (pushed) *pushed = np;
+  return cnt;
+}
+
+/* apps/triangle_src/triangle_agi.upc:69-99 (alg 0) over rows i = row0,
+ * row0 + row_step, ... only: a bounded sample of the AGI loop at one PE. */
+static int64_t tri_agi_rows(const int64_t *off, const int64_t *col, int64_t r0, int64_t r1, int64_t *pulled);
+
+int64_t orc_triangle_agi_sampled(const int64_t *offset, const int64_t *nonzero, int64_t numrows, int64_t row0,
+                                 int64_t row_step) {
+  if (row_step < 1) return -1;
+  int64_t cnt = 0;
+  for (int64_t i = row0; i < numrows; i += row_step) cnt += tri_agi_rows(offset, nonzero, i, i + 1, NULL);
+  return cnt;
+}
+
 /* apps/ig_src/ig_agi.upc:61-64: tgt[i] = lgp_get_int64(table, index[i]). */
 void orc_ig_agi(int64_t *tgt, const int64_t *index, int64_t n, const int64_t *table) {
   for (int64_t i = 0; i < n; i++) tgt[i] = table[index[i]];

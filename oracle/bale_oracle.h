@@ -30,6 +30,21 @@ void orc_ig_agi(int64_t *tgt, const int64_t *index, int64_t n, const int64_t *ta
 /* ig, packed request/response: tgt[j] = ltable[pckindx[j] >> 16] (apps/ig_src/ig_exstack.upc:69-94). */
 void orc_ig_exstack(int64_t *tgt, const int64_t *pckindx, int64_t n, const int64_t *ltable);
 
+/* The exstack variants at one PE with their buffers: every package goes
+ * through a buf_cnt-package send buffer, an exchange and FIFO pops
+ * (exstack/exstack.upc:163-340), as in apps/histo_src/histo_exstack.upc:52-86,
+ * apps/ig_src/ig_exstack.upc:54-102 and apps/triangle_src/triangle_exstack.upc:
+ * 95-168.  The triangle one takes rows row0, row0 + row_step, ... only.
+ * -1 when the buffers cannot be allocated or an argument is out of range. */
+int orc_histo_exstack_buffered(const int64_t *pckindx, int64_t n, int64_t *lcounts, int64_t buf_cnt);
+int orc_ig_exstack_buffered(int64_t *tgt, const int64_t *pckindx, int64_t n, const int64_t *ltable,
+                            int64_t buf_cnt);
+int64_t orc_triangle_exstack_push_buffered(const int64_t *offset, const int64_t *nonzero, int64_t numrows,
+                                           int64_t bufsiz, int64_t row0, int64_t row_step, int64_t *pushed);
+/* triangles alg 0, the AGI loop over rows row0, row0 + row_step, ... only. */
+int64_t orc_triangle_agi_sampled(const int64_t *offset, const int64_t *nonzero, int64_t numrows, int64_t row0,
+                                 int64_t row_step);
+
 /* triangles alg 0, AGI merge scan (apps/triangle_src/triangle_agi.upc:69-99).
  * Returns the count; *pulled gets the reference's "shared refs" tally.      */
 int64_t orc_triangle_agi(const int64_t *offset, const int64_t *nonzero, int64_t numrows,

@@ -78,6 +78,10 @@ class Oracle:
             "orc_triangle_agi_alg1": (i64, [P64, P64, i64, P64, P64, i64, P64]),
             "orc_gen_uniform": (None, [P64, i64, i64, C.c_uint64, C.c_int]),
             "orc_gen_values": (None, [P64, i64, C.c_uint64, C.c_int]),
+            "orc_histo_exstack_buffered": (C.c_int, [P64, i64, P64, i64]),
+            "orc_ig_exstack_buffered": (C.c_int, [P64, P64, i64, P64, i64]),
+            "orc_triangle_exstack_push_buffered": (i64, [P64, P64, i64, i64, i64, i64, P64]),
+            "orc_triangle_agi_sampled": (i64, [P64, P64, i64, i64, i64]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(lib, name)
@@ -102,6 +106,11 @@ class Oracle:
     def histo_exstack(self, pckindx: np.ndarray, counts: np.ndarray) -> None:
         self.lib.orc_histo_exstack(_p(pckindx), pckindx.size, _p(counts))
 
+    def histo_exstack_buffered(self, pckindx: np.ndarray, counts: np.ndarray, buf_cnt: int = 1024) -> None:
+        """histo_exstack at one PE through buf_cnt-package exstack buffers."""
+        if self.lib.orc_histo_exstack_buffered(_p(pckindx), pckindx.size, _p(counts), buf_cnt) != 0:
+            raise ValueError("histo_exstack_buffered: bad buffer size")
+
     def histo_agi_mt(self, index: np.ndarray, counts: np.ndarray, nthreads: int = 0) -> None:
         self.lib.orc_histo_agi_mt(_p(index), index.size, _p(counts), nthreads)
 
@@ -114,6 +123,13 @@ class Oracle:
     def ig_exstack(self, pckindx: np.ndarray, table: np.ndarray) -> np.ndarray:
         tgt = np.empty(pckindx.size, np.int64)
         self.lib.orc_ig_exstack(_p(tgt), _p(pckindx), pckindx.size, _p(table))
+        return tgt
+
+    def ig_exstack_buffered(self, pckindx: np.ndarray, table: np.ndarray, buf_cnt: int = 1024) -> np.ndarray:
+        """ig_exstack at one PE through buf_cnt-package exstack buffers."""
+        tgt = np.empty(pckindx.size, np.int64)
+        if self.lib.orc_ig_exstack_buffered(_p(tgt), _p(pckindx), pckindx.size, _p(table), buf_cnt) != 0:
+            raise ValueError("ig_exstack_buffered: bad buffer size")
         return tgt
 
     def ig_agi_mt(self, tgt: np.ndarray, index: np.ndarray, table: np.ndarray, nthreads: int = 0) -> None:
@@ -137,6 +153,21 @@ class Oracle:
         pushed = C.c_int64(0)
         c = self.lib.orc_triangle_exstack_push(_p(offset), _p(nonzero), offset.size - 1, C.byref(pushed))
         return int(c), int(pushed.value)
+
+    def triangle_exstack_push_buffered(self, offset: np.ndarray, nonzero: np.ndarray, bufsiz: int = 1024,
+                                       row0: int = 0, row_step: int = 1) -> tuple[int, int]:
+        """triangle_exstack_push (alg 0) at one PE through bufsiz-package
+        buffers, over rows row0, row0 + row_step, ..."""
+        pushed = C.c_int64(0)
+        c = self.lib.orc_triangle_exstack_push_buffered(_p(offset), _p(nonzero), offset.size - 1, bufsiz, row0,
+                                                        row_step, C.byref(pushed))
+        if c < 0:
+            raise ValueError("triangle_exstack_push_buffered: bad arguments")
+        return int(c), int(pushed.value)
+
+    def triangle_agi_sampled(self, offset: np.ndarray, nonzero: np.ndarray, row0: int, row_step: int) -> int:
+        """The AGI loop (alg 0) over rows row0, row0 + row_step, ..."""
+        return int(self.lib.orc_triangle_agi_sampled(_p(offset), _p(nonzero), offset.size - 1, row0, row_step))
 
     def triangle_work(self, offset: np.ndarray, nonzero: np.ndarray) -> tuple[int, int]:
         pl, ps = C.c_int64(0), C.c_int64(0)

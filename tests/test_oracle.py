@@ -498,3 +498,42 @@ def test_rand_permp_exstack2_is_the_exstack_form(oracle, golden):
     ref = Reference()
     for n, seed, b in ((77, 3, 5), (2048, 11, 1024)):
         np.testing.assert_array_equal(ref.rand_perm_exstack2(n, seed, b), ref.rand_perm_exstack(n, seed, b))
+
+
+def test_buffered_exstack_restatements_match_reference_golden(oracle, golden):
+    """The one-PE exstack model (buffers, exchange, FIFO pops) gives the
+    reference's results for every buffer size, including one package."""
+    d = golden("histo")
+    for name in _cases(d, "/index"):
+        index = d[f"{name}/index"]
+        pck = (index << 16).astype(np.int64)
+        for buf in (1, 7, 1024):
+            c = d[f"{name}/after_agi"].copy()
+            oracle.histo_exstack_buffered(pck, c, buf)
+            np.testing.assert_array_equal(c, d[f"{name}/after_exstack"], err_msg=f"{name} buf {buf}")
+    d = golden("ig")
+    for name in _cases(d, "/index"):
+        index, table = d[f"{name}/index"], d[f"{name}/table"]
+        pck = (index << 16).astype(np.int64)
+        for buf in (1, 7, 1024):
+            np.testing.assert_array_equal(oracle.ig_exstack_buffered(pck, table, buf), d[f"{name}/tgt"],
+                                          err_msg=f"{name} buf {buf}")
+    d = golden("triangles")
+    for g in d["graphs"]:
+        off, col = d[f"{g}/offset"], d[f"{g}/nonzero"]
+        for buf in (1, 5, 1024):
+            assert oracle.triangle_exstack_push_buffered(off, col, buf) == tuple(
+                int(x) for x in d[f"{g}/triangle_exstack_push"]), (g, buf)
+
+
+def test_sampled_row_loops_add_up(oracle, bale):
+    """Row samples of the AGI and buffered exstack loops partition the count."""
+    L = bale.gen_rmat(12, 16, 0.57, 0.19, 0.19, 9)
+    whole = oracle.triangle_agi(L.offset, L.nonzero)[0]
+    assert sum(oracle.triangle_agi_sampled(L.offset, L.nonzero, r, 5) for r in range(5)) == whole
+    assert sum(oracle.triangle_exstack_push_buffered(L.offset, L.nonzero, 64, r, 5)[0] for r in range(5)) == whole
+    for bad in ((0, 0), (0, -1)):
+        with pytest.raises(ValueError):
+            oracle.triangle_exstack_push_buffered(L.offset, L.nonzero, 64, *bad)
+    with pytest.raises(ValueError):
+        oracle.histo_exstack_buffered(np.zeros(3, np.int64), np.zeros(1, np.int64), 0)

@@ -31,6 +31,8 @@
 // A malformed row raises *bad in step 1 and steps 3-4 then return at once;
 // every index stays inside its array either way.  The work tally is the
 // number of probes, sum_i C(d_i,2) -- the reference's exstack push count.
+#include <algorithm>
+
 #include "tri_device.cuh"
 
 namespace bale {
@@ -55,12 +57,25 @@ constexpr int kScanBlocksPerSm = 6;
 constexpr int kFillUnroll = 4;     // the fill's rounds in flight
 constexpr int kProbeInFlight = 5;  // 16-byte prefix vectors per lane in flight when probing
 constexpr int kStagedInFlight = 2; // the same for prefixes probed against staged short rows
+constexpr int kDenseHubs = 16384;  // rows j below this keep a bitmap of their columns for dense pairs
+constexpr int kDenseThreads = 256;
 
-// Workspace words: [1] malformed entries seen by the scan.
-enum { kWBad = 1, kWords = 4 };
+// Workspace words: [1] malformed entries seen by the scan, [2] the dense-pair
+// margin (negative: no dense pairs), [3] the bitmap rows (a multiple of 128).
+enum { kWBad = 1, kWDenseOv = 2, kWDenseHubs = 3, kWords = 4 };
+
+// A nonzero (i, j) at position p of row i is a dense pair when j has a
+// column bitmap (j < hubs) and its prefix row_i[0,p) is longer than the
+// bitmap's ceil(j/32) words plus the margin ov: then one AND and popcount
+// per word of [0,j) costs less than p probes.  Dense pairs get no record;
+// wedge_dense_kernel counts them.
+__device__ __forceinline__ bool dense_pair(uint32_t j, uint32_t p, int64_t ov, uint32_t hubs) {
+  return ov >= 0 && j < hubs && static_cast<int64_t>(p) > static_cast<int64_t>((j + 31u) >> 5) + ov;
+}
 
 struct Layout {
-  size_t col32, in_cnt, in_off, bsum, in_rec, hubs, words, total;
+  size_t col32, in_cnt, in_off, bsum, in_rec, hubs, bits, words, total;
+  uint32_t dense_hubs;  // rows with a column bitmap: min(kDenseHubs, numrows rounded up to 128)
 };
 
 size_t up256(size_t x) { return (x + 255) & ~size_t(255); }
@@ -76,6 +91,9 @@ Layout layout(int64_t n, int64_t nnz) {
   l.bsum = o;   o += up256(nb * 4);
   l.in_rec = o; o += up256(nz * 8);
   l.hubs = o;   o += up256(static_cast<size_t>(num_sms()) * kScanBlocksPerSm * kHub * 4);
+  // a multiple of 128, so each row's bitmap starts on a 16-byte boundary
+  l.dense_hubs = static_cast<uint32_t>(std::min<int64_t>(kDenseHubs, (n + 127) / 128 * 128));
+  l.bits = o;   o += up256(static_cast<size_t>(l.dense_hubs) * (l.dense_hubs / 32) * 4);
   l.words = o;  o += up256(kWords * 8);
   l.total = o;
   return l;
@@ -171,8 +189,13 @@ struct RowGroup {
 __global__ void __launch_bounds__(kScanThreads)
     wedge_scan_kernel(const int64_t *__restrict__ off, const int64_t *__restrict__ col, int64_t n, int64_t nnz,
                       uint32_t *__restrict__ col32, uint32_t *__restrict__ in_cnt, uint32_t *__restrict__ hubs,
-                      unsigned long long *__restrict__ words, unsigned long long *__restrict__ bad, const unsigned *__restrict__ run_if) {
+                      unsigned long long *__restrict__ words, unsigned long long *__restrict__ bad, int64_t ov,
+                      uint32_t dhubs, const unsigned *__restrict__ run_if) {
   if (tri::skipped(run_if, 1u)) return;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    words[kWDenseOv] = static_cast<unsigned long long>(ov);
+    words[kWDenseHubs] = dhubs;
+  }
   __shared__ uint4 stage[kScanWarps][32];
   __shared__ uint32_t hub[kHub];
   for (int h = threadIdx.x; h < kHub; h += kScanThreads) hub[h] = 0;
@@ -207,8 +230,10 @@ __global__ void __launch_bounds__(kScanThreads)
           const bool ok = c[u] >= 0 && c[u] < i && (p[u] == 0 || cu[u] > prv);
           col32[k[u]] = ok ? cu[u] : kBadCol;
           if (!ok) nbad++;
-          else if (p[u] > 0 && cu[u] < static_cast<uint32_t>(kHub)) atomicAdd(&hub[cu[u]], 1u);
-          else if (p[u] > 0) atomicAdd(in_cnt + cu[u], 1u);
+          else if (p[u] > 0 && !dense_pair(cu[u], p[u], ov, dhubs)) {
+            if (cu[u] < static_cast<uint32_t>(kHub)) atomicAdd(&hub[cu[u]], 1u);
+            else atomicAdd(in_cnt + cu[u], 1u);
+          }
         }
       }
       carry = cu[kUnroll - 1];
@@ -331,6 +356,8 @@ __global__ void __launch_bounds__(kScanThreads)
   __shared__ uint4 stage[kScanWarps][32];
   __shared__ uint32_t hubslot[kHub];
   if (words[kWBad]) return;
+  const int64_t ov = static_cast<int64_t>(words[kWDenseOv]);
+  const uint32_t dhubs = static_cast<uint32_t>(words[kWDenseHubs]);
   {
     const uint32_t *mine = hubs + static_cast<size_t>(blockIdx.x) * kHub;
     for (int h = threadIdx.x; h < kHub; h += kScanThreads) hubslot[h] = h < n ? in_off[h] + mine[h] : 0u;
@@ -349,7 +376,8 @@ __global__ void __launch_bounds__(kScanThreads)
         uint32_t r;
         rg.at(base + 32 * u, k[u], p[u], r);
         c[u] = base + 32 * u + lane < rg.tot ? col32[k[u]] : kBadCol;
-        if (p[u] == 0) c[u] = kBadCol;  // the first nonzero of a row closes no wedge
+        // the first nonzero of a row closes no wedge; dense pairs are counted apart
+        if (p[u] == 0 || (c[u] != kBadCol && dense_pair(c[u], p[u], ov, dhubs))) c[u] = kBadCol;
       }
 #pragma unroll
       for (int u = 0; u < kFillUnroll; u++)
@@ -647,6 +675,120 @@ __global__ void __launch_bounds__(kWarpThreads, 3)
   flush(cnt, wk, count, work);
 }
 
+// Column bitmaps of the rows j below dhubs, whose columns all lie in [0, j):
+// row j's at bits + j * (dhubs / 32), zeroed before.
+__global__ void __launch_bounds__(256)
+    wedge_hubbits_kernel(const int64_t *__restrict__ off, const uint32_t *__restrict__ col32, int64_t n,
+                         uint32_t *__restrict__ bits, const unsigned long long *__restrict__ words,
+                         const unsigned *__restrict__ run_if) {
+  if (tri::skipped(run_if, 1u)) return;
+  if (words[kWBad] || static_cast<int64_t>(words[kWDenseOv]) < 0) return;
+  const uint32_t dhubs = static_cast<uint32_t>(words[kWDenseHubs]);
+  const uint32_t stride = dhubs / 32;
+  const unsigned lane = lane_id();
+  const int64_t rows = static_cast<int64_t>(dhubs) < n ? static_cast<int64_t>(dhubs) : n;
+  const int64_t warps = static_cast<int64_t>(gridDim.x) * 8;
+  for (int64_t j = static_cast<int64_t>(blockIdx.x) * 8 + (threadIdx.x >> 5); j < rows; j += warps) {
+    uint32_t *row = bits + static_cast<size_t>(j) * stride;
+    for (int64_t k = off[j] + lane; k < off[j + 1]; k += 32) {
+      const uint32_t c = col32[k];
+      if (c < static_cast<uint32_t>(j)) atomicOr(&row[c >> 5], 1u << (c & 31));  // the scan checked c < j
+    }
+  }
+}
+
+// The dense pairs: one warp per row i that has any, with row i's columns
+// below its largest dense j as bits in the warp's shared memory.  Each pair
+// (i, j) adds popc(row_i & row_j) over the ceil(j/32) words of [0, j) --
+// row j's bits all lie below j.  The 16-byte vectors of up to 32 pairs are
+// flattened over the lanes, kDenseInFlight of them per lane in flight, so a
+// pair costs no round trip of its own.  As the probe kernel would have, each
+// pair adds p to the work tally when row j has columns.
+constexpr int kDenseInFlight = 4;
+
+__global__ void __launch_bounds__(kDenseThreads)
+    wedge_dense_kernel(const int64_t *__restrict__ off, const uint32_t *__restrict__ col32, int64_t n,
+                       const uint32_t *__restrict__ bits, const unsigned long long *__restrict__ words,
+                       unsigned long long *__restrict__ count, unsigned long long *__restrict__ work,
+                       const unsigned *__restrict__ run_if) {
+  if (tri::skipped(run_if, 1u)) return;
+  if (words[kWBad]) return;
+  const int64_t ov = static_cast<int64_t>(words[kWDenseOv]);
+  const uint32_t dhubs = static_cast<uint32_t>(words[kWDenseHubs]);
+  if (ov < 0 || dhubs == 0) return;
+  __shared__ __align__(16) uint32_t bmall[kDenseThreads / 32][kDenseHubs / 32];
+  __shared__ uint32_t stage[kDenseThreads / 32][32];
+  const unsigned lane = lane_id();
+  uint32_t *bm = bmall[threadIdx.x >> 5];
+  uint32_t *stg = stage[threadIdx.x >> 5];
+  for (int w = lane; w < kDenseHubs / 32; w += 32) bm[w] = 0;
+  __syncwarp();
+  const uint32_t stride = dhubs / 32;
+  unsigned long long cnt = 0, wk = 0;
+  const int64_t warps = static_cast<int64_t>(gridDim.x) * (kDenseThreads / 32);
+  for (int64_t i = static_cast<int64_t>(blockIdx.x) * (kDenseThreads / 32) + (threadIdx.x >> 5); i < n; i += warps) {
+    const int64_t b = off[i], d = off[i + 1] - b;
+    if (d < ov + 2) continue;  // p <= d - 1 must exceed ov + 1
+    uint32_t jmax = 0;
+    for (int64_t k = lane; k < d; k += 32) {
+      const uint32_t c = col32[b + k];
+      if (dense_pair(c, static_cast<uint32_t>(k), ov, dhubs)) jmax = c > jmax ? c : jmax;
+    }
+    jmax = __reduce_max_sync(kFull, jmax);
+    if (jmax == 0) continue;  // a dense j is at least ov + 2
+    for (int64_t k = lane; k < d; k += 32) {
+      const uint32_t c = col32[b + k];
+      if (c < jmax) atomicOr(&bm[c >> 5], 1u << (c & 31));
+    }
+    __syncwarp();
+    for (int64_t k0 = 0; k0 < d; k0 += 32) {
+      const int64_t k = k0 + lane;
+      const uint32_t c = k < d ? col32[b + k] : kBadCol;
+      const bool dn = k < d && dense_pair(c, static_cast<uint32_t>(k), ov, dhubs);
+      if (dn && off[c + 1] > off[c]) wk += static_cast<unsigned long long>(k);
+      const unsigned m = __ballot_sync(kFull, dn);
+      if (!m) continue;
+      // the dense columns to the low lanes, so their vector counts strictly increase
+      if (dn) stg[__popc(m & ((1u << lane) - 1u))] = c;
+      __syncwarp();
+      const unsigned nd = __popc(m);
+      const uint32_t cj = lane < nd ? stg[lane] : 0u;
+      __syncwarp();
+      // 16-byte vectors of [0, j): the last may reach past ceil(j/32) words,
+      // where row j's bitmap is zero (its stride is a multiple of 4 words)
+      const uint32_t nv = lane < nd ? (((cj + 31u) >> 5) + 3u) >> 2 : 0u;
+      const uint32_t inc = incl_scan_u32(nv);
+      const uint32_t tot = __shfl_sync(kFull, inc, 31);
+      const uint4 *bm4 = reinterpret_cast<const uint4 *>(bm);
+      for (uint32_t base = 0; base < tot; base += 32u * kDenseInFlight) {
+        uint4 x[kDenseInFlight], y[kDenseInFlight];
+#pragma unroll
+        for (int h = 0; h < kDenseInFlight; h++) {
+          const uint32_t bb = base + 32u * h;
+          const int o = flat_owner(inc, bb);
+          const uint32_t j = __shfl_sync(kFull, cj, o);
+          const uint32_t v = bb + lane - __shfl_sync(kFull, inc - nv, o);
+          const bool act = bb + lane < tot;
+          x[h] = act ? reinterpret_cast<const uint4 *>(bits + static_cast<size_t>(j) * stride)[v]
+                     : make_uint4(0u, 0u, 0u, 0u);
+          y[h] = act ? bm4[v] : make_uint4(0u, 0u, 0u, 0u);
+        }
+#pragma unroll
+        for (int h = 0; h < kDenseInFlight; h++)
+          cnt += __popc(x[h].x & y[h].x) + __popc(x[h].y & y[h].y) + __popc(x[h].z & y[h].z) +
+                 __popc(x[h].w & y[h].w);
+      }
+    }
+    __syncwarp();
+    for (int64_t k = lane; k < d; k += 32) {
+      const uint32_t c = col32[b + k];
+      if (c < jmax) bm[c >> 5] = 0;
+    }
+    __syncwarp();
+  }
+  flush(cnt, wk, count, work);
+}
+
 bool g_count_attr[64];
 
 // log2 of the per-warp bitmap: min(16, labels rounded up to a power of two >= 32).
@@ -678,17 +820,26 @@ int tri_wedge_prepare(const int64_t *offset, const int64_t *nonzero, int64_t num
   uint32_t *bsum = reinterpret_cast<uint32_t *>(p + l.bsum);
   uint2 *in_rec = reinterpret_cast<uint2 *>(p + l.in_rec);
   uint32_t *hubs = reinterpret_cast<uint32_t *>(p + l.hubs);
+  uint32_t *bits = reinterpret_cast<uint32_t *>(p + l.bits);
   unsigned long long *words = reinterpret_cast<unsigned long long *>(p + l.words);
   const int sms = num_sms();
+  // dense pairs (tri.dense 0: none) and their margin over the bitmap's words
+  const int64_t ov = knob_or("tri.dense", 1) == 0 ? -1 : knob_or("tri.dense_ov", 32);
   BALE_CUDA_OK(cudaMemsetAsync(in_cnt, 0, static_cast<size_t>(numrows) * 4, stream));
   BALE_CUDA_OK(cudaMemsetAsync(words, 0, kWords * sizeof(unsigned long long), stream));
   const int64_t groups = (numrows + 31) / 32;
   int64_t sblocks = (groups + kScanWarps - 1) / kScanWarps;
   const int64_t scap = static_cast<int64_t>(sms) * kScanBlocksPerSm;  // the hubs array holds this many blocks
   if (sblocks > scap) sblocks = scap;
-  wedge_scan_kernel<<<static_cast<unsigned>(sblocks), kScanThreads, 0, stream>>>(offset, nonzero, numrows, nnz, col32,
-                                                                                 in_cnt, hubs, words, bad, run_if);
+  wedge_scan_kernel<<<static_cast<unsigned>(sblocks), kScanThreads, 0, stream>>>(
+      offset, nonzero, numrows, nnz, col32, in_cnt, hubs, words, bad, ov, l.dense_hubs, run_if);
   BALE_CUDA_OK(cudaGetLastError());
+  if (ov >= 0 && l.dense_hubs > 0) {
+    BALE_CUDA_OK(cudaMemsetAsync(bits, 0, static_cast<size_t>(l.dense_hubs) * (l.dense_hubs / 32) * 4, stream));
+    wedge_hubbits_kernel<<<static_cast<unsigned>((l.dense_hubs + 7) / 8), 256, 0, stream>>>(offset, col32, numrows,
+                                                                                            bits, words, run_if);
+    BALE_CUDA_OK(cudaGetLastError());
+  }
   wedge_hubscan_kernel<<<kHub / 256, 256, 0, stream>>>(hubs, static_cast<int>(sblocks), run_if);
   BALE_CUDA_OK(cudaGetLastError());
   const int64_t nb = (numrows + kPsumBlock - 1) / kPsumBlock;
@@ -713,6 +864,7 @@ int tri_wedge_run(const int64_t *offset, const void *ws, int64_t numrows, int64_
   const uint32_t *col32 = reinterpret_cast<const uint32_t *>(p + l.col32);
   const uint32_t *in_off = reinterpret_cast<const uint32_t *>(p + l.in_off);
   const uint2 *in_rec = reinterpret_cast<const uint2 *>(p + l.in_rec);
+  const uint32_t *bits = reinterpret_cast<const uint32_t *>(p + l.bits);
   const unsigned long long *words = reinterpret_cast<const unsigned long long *>(p + l.words);
   const int sms = num_sms();
   const int wb = warp_bits(numrows);
@@ -737,6 +889,12 @@ int tri_wedge_run(const int64_t *offset, const void *ws, int64_t numrows, int64_
   if (blocks > need) blocks = need > 0 ? need : 1;
   wedge_count_kernel<<<static_cast<unsigned>(blocks), kWarpThreads, smem, stream>>>(
       offset, col32, in_off, in_rec, numrows, wlim, wb, nvec_all, stage_max, words, count, work, cursor, run_if);
+  BALE_CUDA_OK(cudaGetLastError());
+  // the dense pairs the prepare step left out of the records (none when its
+  // margin was negative: the kernel returns at once)
+  const int64_t dgroups = (numrows + kDenseThreads / 32 - 1) / (kDenseThreads / 32);
+  wedge_dense_kernel<<<static_cast<unsigned>(std::min<int64_t>(dgroups, static_cast<int64_t>(sms) * 8)), kDenseThreads,
+                       0, stream>>>(offset, col32, numrows, bits, words, count, work, run_if);
   BALE_CUDA_OK(cudaGetLastError());
   return BALE_OK;
 }

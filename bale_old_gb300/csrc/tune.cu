@@ -72,6 +72,8 @@ Knob g_knobs[] = {
     {"tri.wedge_pull_pct", -1},     // default mode: wedges when pulls >= this % of pushes (192)
     {"tri.wedge_push_per_nnz", -1}, // ... or when pushes >= this many per nonzero (no such clause)
     {"tri.choose_min_nnz", -1},     // the per-graph choice from this many nonzeros; wedges below (2^23)
+    {"tri.dense", -1},              // wedge mode: 0 probes every prefix; dense pairs by bitmap AND otherwise
+    {"tri.dense_ov", -1},           // ... a pair is dense when its prefix exceeds ceil(j/32) words by this (32)
 };
 std::mutex g_mu;
 }  // namespace

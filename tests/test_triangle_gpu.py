@@ -351,3 +351,46 @@ def test_strategy_thresholds_steer_the_choice(cuda, bale):
     finally:
         for k in ("tri.choose_min_nnz", "tri.wedge_pull_pct", "tri.wedge_push_per_nnz"):
             bale.tune_set(k, -1)
+
+
+@pytest.mark.parametrize("graph", ["rmat16", "rmat20", "kron_hubs", "erdos_renyi", "clique1800", "clique40"])
+def test_dense_pairs_match_the_probes(cuda, bale, oracle, graph):
+    """Wedge mode with the dense pairs (prefix longer than row j's bitmap
+    words plus a margin) counted by bitmap AND instead of probes: off, at the
+    default margin and at margin 0 (every eligible pair).  The count equals
+    the oracle's and the work tally stays the probe count, sum of p over the
+    nonzeros whose row j has columns."""
+    import torch
+
+    if graph.startswith("rmat"):
+        L = bale.gen_rmat(int(graph[4:]), 16, 0.57, 0.19, 0.19, 11)
+        off_h, col_h = L.offset, L.nonzero
+    elif graph == "kron_hubs":
+        L = bale.gen_kronecker(1, [1500, 3])
+        off_h, col_h = L.offset, L.nonzero
+    elif graph == "erdos_renyi":
+        L = bale.gen_erdos_renyi(1 << 14, 64 / (1 << 14), 5)
+        off_h, col_h = L.offset, L.nonzero
+    else:
+        off_h, col_h = _clique(int(graph[6:]))
+    want = oracle.triangle_agi(off_h, col_h)[0]
+    deg = np.diff(off_h)
+    rowid = np.repeat(np.arange(off_h.size - 1), deg)
+    pos = np.arange(col_h.size) - off_h[rowid]
+    tally = int(pos[deg[col_h] > 0].sum())
+    off = torch.from_numpy(off_h).to(cuda)
+    col = torch.from_numpy(col_h).to(cuda)
+    bale.tune_set("tri.mode", 2)
+    try:
+        for dense, ov in ((0, -1), (1, -1), (1, 0), (1, 7)):
+            bale.tune_set("tri.dense", dense)
+            bale.tune_set("tri.dense_ov", ov)
+            count = torch.zeros(1, dtype=torch.int64, device=cuda)
+            work = torch.zeros(1, dtype=torch.int64, device=cuda)
+            bale.triangle_dev(off, col, count, work=work)
+            torch.cuda.synchronize()
+            assert int(count.item()) == want, (graph, dense, ov)
+            assert int(work.item()) == tally, (graph, dense, ov)
+    finally:
+        for k in ("tri.mode", "tri.dense", "tri.dense_ov"):
+            bale.tune_set(k, -1)

@@ -60,9 +60,10 @@ constexpr int kStagedInFlight = 2; // the same for prefixes probed against stage
 constexpr int kDenseHubs = 16384;  // rows j below this keep a bitmap of their columns for dense pairs
 constexpr int kDenseThreads = 256;
 
-// Workspace words: [1] malformed entries seen by the scan, [2] the dense-pair
-// margin (negative: no dense pairs), [3] the bitmap rows (a multiple of 128).
-enum { kWBad = 1, kWDenseOv = 2, kWDenseHubs = 3, kWords = 4 };
+// Workspace words: [0] nonzero when the scan met a dense pair, [1] malformed
+// entries seen by the scan, [2] the dense-pair margin (negative: no dense
+// pairs), [3] the bitmap rows (a multiple of 128).
+enum { kWDenseAny = 0, kWBad = 1, kWDenseOv = 2, kWDenseHubs = 3, kWords = 4 };
 
 // A nonzero (i, j) at position p of row i is a dense pair when j has a
 // column bitmap (j < hubs) and its prefix row_i[0,p) is longer than the
@@ -204,6 +205,7 @@ __global__ void __launch_bounds__(kScanThreads)
   const int64_t warps = static_cast<int64_t>(gridDim.x) * kScanWarps;
   const unsigned lane = lane_id();
   unsigned long long nbad = 0;
+  bool any_dense = false;
   for (int64_t g = static_cast<int64_t>(blockIdx.x) * kScanWarps + (threadIdx.x >> 5); g < groups; g += warps) {
     RowGroup rg;
     rg.load(off, n, nnz, g * 32, stage[threadIdx.x >> 5]);
@@ -230,7 +232,9 @@ __global__ void __launch_bounds__(kScanThreads)
           const bool ok = c[u] >= 0 && c[u] < i && (p[u] == 0 || cu[u] > prv);
           col32[k[u]] = ok ? cu[u] : kBadCol;
           if (!ok) nbad++;
-          else if (p[u] > 0 && !dense_pair(cu[u], p[u], ov, dhubs)) {
+          else if (p[u] > 0 && dense_pair(cu[u], p[u], ov, dhubs)) {
+            any_dense = true;
+          } else if (p[u] > 0) {
             if (cu[u] < static_cast<uint32_t>(kHub)) atomicAdd(&hub[cu[u]], 1u);
             else atomicAdd(in_cnt + cu[u], 1u);
           }
@@ -244,7 +248,7 @@ __global__ void __launch_bounds__(kScanThreads)
     atomicAdd(words + kWBad, nbad);
     if (bad) atomicAdd(bad, nbad);
   }
-  __syncthreads();
+  if (__syncthreads_or(any_dense) && threadIdx.x == 0) words[kWDenseAny] = 1;
   uint32_t *mine = hubs + static_cast<size_t>(blockIdx.x) * kHub;
   for (int h = threadIdx.x; h < kHub; h += kScanThreads) {
     const uint32_t v = hub[h];
@@ -675,14 +679,16 @@ __global__ void __launch_bounds__(kWarpThreads, 3)
   flush(cnt, wk, count, work);
 }
 
-// Column bitmaps of the rows j below dhubs, whose columns all lie in [0, j):
-// row j's at bits + j * (dhubs / 32), zeroed before.
+// Column bitmaps of the rows j below dhubs (their columns all lie in
+// [0, j)), built when the scan met a dense pair: row j's at bits + j *
+// (dhubs / 32), its words zeroed up to a multiple of 4 past ceil(j/32) (the
+// dense kernel reads 16-byte vectors) before its bits are set.
 __global__ void __launch_bounds__(256)
     wedge_hubbits_kernel(const int64_t *__restrict__ off, const uint32_t *__restrict__ col32, int64_t n,
                          uint32_t *__restrict__ bits, const unsigned long long *__restrict__ words,
                          const unsigned *__restrict__ run_if) {
   if (tri::skipped(run_if, 1u)) return;
-  if (words[kWBad] || static_cast<int64_t>(words[kWDenseOv]) < 0) return;
+  if (words[kWBad] || !words[kWDenseAny] || static_cast<int64_t>(words[kWDenseOv]) < 0) return;
   const uint32_t dhubs = static_cast<uint32_t>(words[kWDenseHubs]);
   const uint32_t stride = dhubs / 32;
   const unsigned lane = lane_id();
@@ -690,6 +696,9 @@ __global__ void __launch_bounds__(256)
   const int64_t warps = static_cast<int64_t>(gridDim.x) * 8;
   for (int64_t j = static_cast<int64_t>(blockIdx.x) * 8 + (threadIdx.x >> 5); j < rows; j += warps) {
     uint32_t *row = bits + static_cast<size_t>(j) * stride;
+    const uint32_t nz = ((((static_cast<uint32_t>(j) + 31u) >> 5) + 3u) >> 2) << 2;
+    for (uint32_t w = lane; w < nz; w += 32) row[w] = 0;
+    __syncwarp();
     for (int64_t k = off[j] + lane; k < off[j + 1]; k += 32) {
       const uint32_t c = col32[k];
       if (c < static_cast<uint32_t>(j)) atomicOr(&row[c >> 5], 1u << (c & 31));  // the scan checked c < j
@@ -712,7 +721,7 @@ __global__ void __launch_bounds__(kDenseThreads)
                        unsigned long long *__restrict__ count, unsigned long long *__restrict__ work,
                        const unsigned *__restrict__ run_if) {
   if (tri::skipped(run_if, 1u)) return;
-  if (words[kWBad]) return;
+  if (words[kWBad] || !words[kWDenseAny]) return;
   const int64_t ov = static_cast<int64_t>(words[kWDenseOv]);
   const uint32_t dhubs = static_cast<uint32_t>(words[kWDenseHubs]);
   if (ov < 0 || dhubs == 0) return;
@@ -760,24 +769,32 @@ __global__ void __launch_bounds__(kDenseThreads)
       const uint32_t inc = incl_scan_u32(nv);
       const uint32_t tot = __shfl_sync(kFull, inc, 31);
       const uint4 *bm4 = reinterpret_cast<const uint4 *>(bm);
+      const uint4 *bits4 = reinterpret_cast<const uint4 *>(bits);
+      const uint32_t stride4 = stride >> 2;
+      uint32_t sum = 0;  // at most 32 pairs of at most 2^14 common columns each
       for (uint32_t base = 0; base < tot; base += 32u * kDenseInFlight) {
         uint4 x[kDenseInFlight], y[kDenseInFlight];
+        bool act[kDenseInFlight];
 #pragma unroll
         for (int h = 0; h < kDenseInFlight; h++) {
           const uint32_t bb = base + 32u * h;
           const int o = flat_owner(inc, bb);
           const uint32_t j = __shfl_sync(kFull, cj, o);
           const uint32_t v = bb + lane - __shfl_sync(kFull, inc - nv, o);
-          const bool act = bb + lane < tot;
-          x[h] = act ? reinterpret_cast<const uint4 *>(bits + static_cast<size_t>(j) * stride)[v]
-                     : make_uint4(0u, 0u, 0u, 0u);
-          y[h] = act ? bm4[v] : make_uint4(0u, 0u, 0u, 0u);
+          act[h] = bb + lane < tot;
+          // an idle lane reads vector 0 of row j, and its sum is dropped
+          const uint32_t va = act[h] ? v : 0u;
+          x[h] = bits4[static_cast<size_t>(j) * stride4 + va];
+          y[h] = bm4[va];
         }
 #pragma unroll
-        for (int h = 0; h < kDenseInFlight; h++)
-          cnt += __popc(x[h].x & y[h].x) + __popc(x[h].y & y[h].y) + __popc(x[h].z & y[h].z) +
-                 __popc(x[h].w & y[h].w);
+        for (int h = 0; h < kDenseInFlight; h++) {
+          const uint32_t t = __popc(x[h].x & y[h].x) + __popc(x[h].y & y[h].y) + __popc(x[h].z & y[h].z) +
+                             __popc(x[h].w & y[h].w);
+          sum += act[h] ? t : 0u;
+        }
       }
+      cnt += sum;
     }
     __syncwarp();
     for (int64_t k = lane; k < d; k += 32) {
@@ -835,7 +852,6 @@ int tri_wedge_prepare(const int64_t *offset, const int64_t *nonzero, int64_t num
       offset, nonzero, numrows, nnz, col32, in_cnt, hubs, words, bad, ov, l.dense_hubs, run_if);
   BALE_CUDA_OK(cudaGetLastError());
   if (ov >= 0 && l.dense_hubs > 0) {
-    BALE_CUDA_OK(cudaMemsetAsync(bits, 0, static_cast<size_t>(l.dense_hubs) * (l.dense_hubs / 32) * 4, stream));
     wedge_hubbits_kernel<<<static_cast<unsigned>((l.dense_hubs + 7) / 8), 256, 0, stream>>>(offset, col32, numrows,
                                                                                             bits, words, run_if);
     BALE_CUDA_OK(cudaGetLastError());

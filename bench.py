@@ -421,10 +421,11 @@ def run_triangles(ctx) -> dict:
     pushes = int(pos[live].sum())
     records = int(live.sum())
     del rowid, pos, live
-    # the dominant kernel alone: counting from a prepared graph (the wedge
-    # count kernel); its algorithmic bytes are the push model's -- every
-    # probed prefix element read once as a u32, the 8-byte prefix records,
-    # and rows j read twice (set and clear) as u32
+    # the dominant kernels alone: counting from a prepared graph (the wedge
+    # probe kernel and the dense-pair kernel); their algorithmic bytes are the
+    # push model's -- every probed prefix element read once as a u32 (the
+    # dense pairs counted as the pushes they replace), the 8-byte prefix
+    # records, and rows j read twice (set and clear) as u32
     wedge_bytes = 4 * pushes + 8 * records + 8 * nnz
     with bale.TrianglePrepared(off, col) as g:
         cnt2 = torch.zeros(1, dtype=torch.int64, device=dev)
@@ -443,7 +444,10 @@ def run_triangles(ctx) -> dict:
                                    "note": "the AGI loop's pull model (8 B per row-j element scanned); the "
                                            "wedge kernels probe 4x fewer elements, so this reads above 1"},
            "count_kernel_ms": round(count_ms, 4),
-           "clocks": clocks.summary(), "gpu_launches": 7 * args.steps,
+           # per call: the path choice, the wedge scan, row bitmaps, hub scan, 3
+           # offset kernels, fill, probes, dense pairs, and the 4 hybrid kernels
+           # that return at once when the wedges are chosen
+           "clocks": clocks.summary(), "gpu_launches": 14 * args.steps,
            "config": {"workload": "triangles: R-MAT scale 22, edge factor 16, (0.57,0.19,0.19,0.05), "
                                   "symmetrised, deduplicated, degree-ordered strictly lower L",
                       "n": n, "nnz": nnz, "pulls": pulls, "pushes": pushes, "generate_s": round(gen_s, 2),
@@ -957,17 +961,18 @@ def tri_roofline(ctx, push_bytes: int, count_s: float, step_ms: float) -> dict:
     dram = tr.get("dram_bytes_per_step")
     achieved = dram / count_s / 1e9 if dram else None
     return {"bound": "issue", "kernel": "wedge_count_kernel (one warp per row j: bitmap / staged search over the "
-                                        "incoming prefixes)",
+                                        "incoming prefixes) + wedge_dense_kernel (bitmap AND of the dense pairs)",
             "achieved": round(achieved, 1) if achieved else None, "peak": ctx["peak"], "peak_source": ctx["peak_src"],
             "unit": "GB/s", "frac": round(achieved / ctx["peak"], 4) if achieved else None, "traffic": dram,
-            "what": "DRAM bytes of one count launch (ncu) over the live count-kernel time: the kernel's share of HBM",
+            "what": "DRAM bytes of one count (both kernels, ncu) over their live time: their share of HBM",
             "issue_active_ncu": tr.get("issue_active"), "ncu_source": tr.get("summary"),
             "count_kernel_ms": round(count_s * 1e3, 4),
             "push_model": {"bytes_per_launch": push_bytes, "achieved_gbs": round(push_bytes / count_s / 1e9, 1),
                            "note": "4 B per probed prefix element (exstack pushes, "
-                                   "apps/triangle_src/triangle.upc:344-349), 8 B per prefix record, 8 B per "
-                                   "nonzero for row j: L2 and DRAM bytes together"},
-            "note": f"the step also runs the prepare kernels (validate, transpose): "
+                                   "apps/triangle_src/triangle.upc:344-349; the dense pairs as the pushes they "
+                                   "replace), 8 B per prefix record, 8 B per nonzero for row j: L2 and DRAM bytes "
+                                   "together"},
+            "note": f"the step also runs the prepare kernels (validate, transpose, row bitmaps): "
                     f"{round(step_ms - count_s * 1e3, 3)} ms of the {round(step_ms, 3)} ms step"}
 
 
